@@ -1,0 +1,234 @@
+"""ORACLE -- test infrastructure only.
+
+CPU restatement of the ADPRES static k-eigenvalue path (adpres_oracle.cpp),
+exposed through ctypes.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import this package, and only as the
+checker of the CUDA path; the product never routes through it.
+
+Parity pin: the restatement reproduces the reference's printed IAEA3D
+convergence trace (docs/quick-guides.md:161-191 of the ADPRES project) digit
+for digit; see tests/test_oracle_golden.py.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "adpres_oracle.cpp")
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "libadpres_oracle.so")
+
+# Status codes (same meaning as the product's adp_status values).
+ORA_OK = 0
+ORA_ERR_INPUT = 1
+ORA_ERR_BADXS = 2
+ORA_ERR_PIVOT = 3
+ORA_ERR_DIVERGED = 4
+ORA_ERR_MAXOUTER = 5
+ORA_ERR_ZEROPOWER = 6
+ORA_ERR_UNSUPPORTED = 7
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement with g++ (no FMA contraction) into _build/."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
+        return LIB
+    tmp = LIB + ".tmp.%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
+           "-fPIC", "-shared", SRC, "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        vp, cp, ip, dp = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+        ipp = ctypes.POINTER(ctypes.c_int)
+        L.ora_global_error.restype = cp
+        L.ora_load_deck_text.restype = vp
+        L.ora_load_deck_text.argtypes = [cp, cp]
+        L.ora_load_deck.restype = vp
+        L.ora_load_deck.argtypes = [cp]
+        L.ora_free.argtypes = [vp]
+        L.ora_error.restype = cp
+        L.ora_error.argtypes = [vp]
+        for name in ("ora_xs_updt", "ora_dsigr_updt"):
+            getattr(L, name).argtypes = [vp]
+        L.ora_outer.argtypes = [vp, ip, ip, ip]
+        L.ora_powdis.argtypes = [vp, dp]
+        L.ora_matrix_setup.argtypes = [vp, ip]
+        L.ora_nodal_upd.argtypes = [vp, ip]
+        L.ora_group_solve.argtypes = [vp, ip, ip, dp]
+        L.ora_bicg.argtypes = [vp, ip, ip, dp, dp]
+        L.ora_get_matrix7.argtypes = [vp, dp]
+        L.ora_get_int.argtypes = [vp, cp]
+        L.ora_get_double.restype = ctypes.c_double
+        L.ora_get_double.argtypes = [vp, cp]
+        L.ora_set_double.argtypes = [vp, cp, ctypes.c_double]
+        L.ora_set_int.argtypes = [vp, cp, ip]
+        L.ora_array_len.restype = ctypes.c_long
+        L.ora_array_len.argtypes = [vp, cp]
+        L.ora_get_array.argtypes = [vp, cp, dp]
+        L.ora_set_array.argtypes = [vp, cp, dp]
+        L.ora_get_iarray.argtypes = [vp, cp, ipp]
+        L.ora_get_trace.argtypes = [vp, ipp, dp, dp, dp, ipp, dp, ipp]
+        L.ora_reset.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+@dataclass
+class TraceRow:
+    p: int
+    k: float
+    ser: float
+    fer: float
+    extrapolated: bool
+    nodal: bool
+    ndmax: float
+    loc: tuple
+
+
+class Oracle:
+    """One reference-state instance (the equivalent of one ADPRES process)."""
+
+    def __init__(self, deck_path: str | None = None, text: str | None = None, basedir: str = "."):
+        L = lib()
+        if deck_path is not None:
+            h = L.ora_load_deck(deck_path.encode())
+        else:
+            h = L.ora_load_deck_text(text.encode(), basedir.encode())
+        if not h:
+            msg = L.ora_global_error().decode()
+            code = ORA_ERR_UNSUPPORTED if "outside the static" in msg else ORA_ERR_INPUT
+            raise OracleError(code, msg)
+        self.h = ctypes.c_void_p(h)
+        self.L = L
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            self.L.ora_free(h)
+            self.h = None
+
+    def _check(self, st):
+        if st != ORA_OK:
+            raise OracleError(st, self.L.ora_error(self.h).decode())
+
+    # -- drivers -----------------------------------------------------------
+    def xs_updt(self):
+        self._check(self.L.ora_xs_updt(self.h))
+
+    def dsigr_updt(self):
+        self._check(self.L.ora_dsigr_updt(self.h))
+
+    def outer(self, adjoint=False, popt=1, max_outers=0):
+        self._check(self.L.ora_outer(self.h, int(adjoint), popt, max_outers))
+
+    def run(self):
+        """control::forward / control::adjoint (mod_control.f90:11-86)."""
+        self.xs_updt()
+        self.outer(adjoint=bool(self.geti("adjoint")), popt=1)
+
+    def powdis(self):
+        p = np.zeros(self.geti("nnod"))
+        self._check(self.L.ora_powdis(self.h, _dp(p)))
+        return p
+
+    def matrix_setup(self, opt=1):
+        self._check(self.L.ora_matrix_setup(self.h, opt))
+
+    def nodal_upd(self, nmode=1):
+        self._check(self.L.ora_nodal_upd(self.h, nmode))
+
+    def group_solve(self, g, adjoint=False):
+        bs = np.zeros(self.geti("nnod"))
+        self._check(self.L.ora_group_solve(self.h, g, int(adjoint), _dp(bs)))
+        return bs
+
+    def bicg(self, g, b, x, imax=None):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.array(x, dtype=np.float64)
+        self._check(self.L.ora_bicg(self.h, g, imax or self.geti("nin"), _dp(b), _dp(x)))
+        return x
+
+    def matrix7(self):
+        out = np.zeros((self.geti("ng"), self.geti("nnod"), 7))
+        self._check(self.L.ora_get_matrix7(self.h, _dp(out)))
+        return out
+
+    def reset(self):
+        self.L.ora_reset(self.h)
+
+    # -- accessors ---------------------------------------------------------
+    def geti(self, name):
+        return self.L.ora_get_int(self.h, name.encode())
+
+    def getd(self, name):
+        return self.L.ora_get_double(self.h, name.encode())
+
+    def setd(self, name, v):
+        assert self.L.ora_set_double(self.h, name.encode(), float(v)) == 0
+
+    def seti(self, name, v):
+        assert self.L.ora_set_int(self.h, name.encode(), int(v)) == 0
+
+    def array(self, name):
+        n = self.L.ora_array_len(self.h, name.encode())
+        if n < 0:
+            raise KeyError(name)
+        out = np.zeros(n)
+        if self.L.ora_get_array(self.h, name.encode(), _dp(out)) != 0:
+            out = np.zeros(n, dtype=np.int32)
+            if self.L.ora_get_iarray(self.h, name.encode(), _ip(out)) != 0:
+                raise KeyError(name)
+        return out
+
+    def set_array(self, name, values):
+        n = self.L.ora_array_len(self.h, name.encode())
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        assert v.size == n, (name, v.size, n)
+        assert self.L.ora_set_array(self.h, name.encode(), _dp(v)) == 0
+
+    def fortran(self, name, shape):
+        """Array in its Fortran (column-major) shape, e.g. ('f0', (nnod, ng))."""
+        return self.array(name).reshape(shape, order="F")
+
+    def trace(self):
+        n = self.geti("trace_len")
+        ip = np.zeros(n, dtype=np.int32)
+        k, ser, fer, nd = (np.zeros(n) for _ in range(4))
+        fl = np.zeros(n, dtype=np.int32)
+        loc = np.zeros(3 * n, dtype=np.int32)
+        self.L.ora_get_trace(self.h, _ip(ip), _dp(k), _dp(ser), _dp(fer), _ip(fl), _dp(nd), _ip(loc))
+        return [TraceRow(int(ip[t]), float(k[t]), float(ser[t]), float(fer[t]), bool(fl[t] & 1),
+                         bool(fl[t] & 2), float(nd[t]), tuple(int(v) for v in loc[3 * t:3 * t + 3]))
+                for t in range(n)]
