@@ -1,0 +1,191 @@
+"""Host-side mirror of ADPRES's calculation drivers over the C ABI.
+
+``Core`` owns one adp_handle (one core on one GPU).  Its methods follow the
+reference's call sequence: ``xs_updt`` is XS_updt (mod_xsec.f90:11-46),
+``outer`` is outer/outer_ad (mod_cmfd.f90:415, :602), ``power`` is PowDis
+(:1290) and ``forward``/``adjoint`` are control::forward/adjoint
+(mod_control.f90:11-86).  Errors come back as AdpError with the status the
+reference would have STOPped on.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import AdpError, dptr, iptr
+
+
+@dataclass
+class Report:
+    outers: int
+    converged: bool
+    nodal_updates: int
+    keff: float
+    ser: float
+    fer: float
+    ndmax: float
+    loc: tuple
+    trace_k: np.ndarray
+    trace_ser: np.ndarray
+    trace_fer: np.ndarray
+    trace_flags: np.ndarray
+    trace_ndmax: np.ndarray
+    device_ms: float
+
+
+def _c(a, dt=np.float64):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def _fortran(a, dt=np.float64):
+    """Column-major (node index fastest) copy, the reference's array layout."""
+    return np.asfortranarray(a, dtype=dt).reshape(-1, order="F")
+
+
+class Core:
+    """One static k-eigenvalue core on the current CUDA device."""
+
+    def __init__(self, nxx, nyy, nzz, ix, iy, iz, xdel, ydel, zdel, bc, ng, *, nin=2, nout=500, nac=5,
+                 nupd=0, serc=0.0, ferc=0.0, kern=2, precision="fp64"):
+        self.L = _lib.load()
+        self.nnod = int(len(ix))
+        self.ng = int(ng)
+        self._keep = [_c(ix, np.int32), _c(iy, np.int32), _c(iz, np.int32), _c(xdel), _c(ydel), _c(zdel)]
+        ixa, iya, iza, xd, yd, zd = self._keep
+        g = _lib.AdpGeom(int(nxx), int(nyy), int(nzz), self.nnod, iptr(ixa), iptr(iya), iptr(iza), dptr(xd),
+                         dptr(yd), dptr(zd), *[int(b) for b in bc])
+        prec = {"fp64": _lib.ADP_FP64, "mixed": _lib.ADP_MIXED}[precision]
+        o = _lib.AdpOpts(self.ng, int(nin), int(nout), int(nac), int(nupd), float(serc), float(ferc), int(kern), prec)
+        h = ctypes.c_void_p()
+        st = self.L.adp_create(ctypes.byref(g), ctypes.byref(o), ctypes.byref(h))
+        if st != 0:
+            raise AdpError(st, _lib.last_error(None))
+        self.h = h
+        self.nout = int(nout) if nout and nout > 0 else 500
+        self.precision = precision
+
+    @classmethod
+    def from_deck(cls, dk, precision="fp64", **over):
+        kw = dict(nin=dk.nin, nout=dk.nout, nac=dk.nac, nupd=dk.nupd, serc=dk.serc, ferc=dk.ferc,
+                  kern=dk.kern_code, precision=precision)
+        kw.update(over)
+        core = cls(dk.nxx, dk.nyy, dk.nzz, dk.ix, dk.iy, dk.iz, dk.xdel, dk.ydel, dk.zdel, dk.bc, dk.ng, **kw)
+        core.deck = dk
+        core.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
+        return core
+
+    def close(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            self.L.adp_destroy(h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st):
+        if st != 0:
+            raise AdpError(st, _lib.last_error(self.h))
+
+    # -- cross sections -----------------------------------------------------
+    def xs_updt(self, xsigtr, xsiga, xnuf, xsigf, chi, mat, xsigs, dc=None):
+        """XS_updt from material tables (nmat,ng) / (nmat,ng,ng) and mat (nnod,)."""
+        nmat = int(np.asarray(chi).shape[0])
+        args = [_fortran(xsigtr), _fortran(xsiga), _fortran(xnuf), _fortran(xsigf), _fortran(chi)]
+        m = _c(mat, np.int32)
+        s = _fortran(xsigs)
+        d = None if dc is None else _fortran(dc)
+        self._check(self.L.adp_xs_updt(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
+
+    def xs_updt_nodes(self, sigtr, siga, nuf, sigf, chi, mat, sigs, dc=None):
+        """XS_updt from node tables (nnod,ng) / (nnod,ng,ng)."""
+        nmat = int(np.asarray(chi).shape[0])
+        args = [_fortran(sigtr), _fortran(siga), _fortran(nuf), _fortran(sigf), _fortran(chi)]
+        m = _c(mat, np.int32)
+        s = _fortran(sigs)
+        d = None if dc is None else _fortran(dc)
+        self._check(self.L.adp_xs_updt_nodes(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
+
+    def set_xs(self, D, sigr, nuf, sigf, chi, mat, sigs, dc=None):
+        nmat = int(np.asarray(chi).shape[0])
+        args = [_fortran(D), _fortran(sigr), _fortran(nuf), _fortran(sigf), _fortran(chi)]
+        m = _c(mat, np.int32)
+        s = _fortran(sigs)
+        d = None if dc is None else _fortran(dc)
+        self._check(self.L.adp_set_xs(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
+
+    # -- solver -------------------------------------------------------------
+    def outer(self, adjoint=False, popt=1, trace=True) -> Report:
+        cap = self.nout if trace else 0
+        tk, ts, tf, tn = (np.zeros(cap) for _ in range(4))
+        tfl = np.zeros(cap, dtype=np.int32)
+        rep = _lib.AdpReport()
+        rep.trace_cap = cap
+        if cap:
+            rep.trace_k, rep.trace_ser, rep.trace_fer, rep.trace_ndmax = dptr(tk), dptr(ts), dptr(tf), dptr(tn)
+            rep.trace_flags = iptr(tfl)
+        st = self.L.adp_outer(self.h, int(bool(adjoint)), int(popt), ctypes.byref(rep))
+        n = min(rep.outers, cap)
+        self.last_report = Report(rep.outers, bool(rep.converged), rep.nodal_updates, rep.keff, rep.ser, rep.fer,
+                                  rep.ndmax, (rep.im, rep.jm, rep.km), tk[:n], ts[:n], tf[:n], tfl[:n], tn[:n],
+                                  rep.device_ms)
+        self._check(st)
+        return self.last_report
+
+    def state(self):
+        """(f0 (nnod,ng), fs0 (nnod,), keff, dn (nnod,ng,6)) in the reference layouts."""
+        f0 = np.zeros(self.nnod * self.ng)
+        fs0 = np.zeros(self.nnod)
+        dn = np.zeros(self.nnod * self.ng * 6)
+        k = ctypes.c_double()
+        self._check(self.L.adp_get_state(self.h, dptr(f0), dptr(fs0), ctypes.byref(k), dptr(dn)))
+        return (f0.reshape((self.nnod, self.ng), order="F"), fs0, k.value,
+                dn.reshape((self.nnod, self.ng, 6), order="F"))
+
+    def set_state(self, f0=None, fs0=None, keff=None, dn=None):
+        a = None if f0 is None else _fortran(f0)
+        b = None if fs0 is None else _c(fs0)
+        d = None if dn is None else _fortran(dn)
+        k = None if keff is None else ctypes.byref(ctypes.c_double(keff))
+        self._check(self.L.adp_set_state(self.h, dptr(a), dptr(b), k, dptr(d)))
+
+    def power(self):
+        p = np.zeros(self.nnod)
+        self._check(self.L.adp_power(self.h, dptr(p)))
+        return p
+
+    def timers(self):
+        t = _lib.AdpTimers()
+        self._check(self.L.adp_get_timers(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def set_launch(self, blocks=0, threads=0):
+        self._check(self.L.adp_set_launch(self.h, int(blocks), int(threads)))
+
+    # -- calculation modes (mod_control.f90:11-86) ---------------------------
+    def forward(self):
+        rep = self.outer(adjoint=False, popt=1)
+        return rep, self.power()
+
+    def adjoint(self):
+        rep = self.outer(adjoint=True, popt=1)
+        return rep, self.power()
+
+
+def solve_deck(dk, precision="fp64"):
+    """control::forward / control::adjoint for a parsed deck: (report, power, core)."""
+    core = Core.from_deck(dk, precision=precision)
+    rep, p = core.adjoint() if dk.adjoint else core.forward()
+    return rep, p, core

@@ -1,0 +1,209 @@
+// Device-side building blocks of the GB300 solver: box geometry, the
+// control block that carries the outer-iteration scalars between launches,
+// a grid barrier with a time limit, and deterministic FP64 reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/adpres_gb300.h"
+
+namespace adp {
+
+// Face order of df/dn/dc: X+, X-, Y+, Y-, Z+, Z- (mod_data.f90:59-60).
+enum { FXP = 0, FXM = 1, FYP = 2, FYM = 3, FZP = 4, FZM = 5 };
+
+// Neighbour-mask bits: bit f set when the face f of the node has a node
+// across it (the reference's ystag/xstag/k tests, mod_cmfd.f90:255-298).
+// Bit 6 marks an active node of the padded box.
+enum { NB_ACTIVE = 64 };
+
+constexpr int kMaxGroups = 8;     // nodal kernels are instantiated for 1..8 groups
+constexpr int kMaxBlocks = 1024;  // persistent-grid size limit (reduction partial slots)
+constexpr int kRedQ = 4;          // reduction quantities per phase
+
+// Scalars of the outer iteration that live on the device between launches
+// (the locals of outer()/outer_ad() in mod_cmfd.f90:431-440 plus Ke, ndmax).
+struct OuterCtl {
+  double Ke;          // current eigenvalue
+  double f;           // integrated fission source of the latest fs0
+  double e1;          // L2 norm of the previous fission-source change
+  double ser, fer;    // errors of the latest outer
+  double ndmax;       // last maximum change of dn (persists, mod_cmfd.f90:495)
+  int p;              // outers done by the current adp_outer call
+  int p_total;        // outers done over the life of the handle
+  int cur;            // buffer holding the latest flux / fission source
+  int status;         // first device-side error (adp_status), 0 if none
+  int converged;
+  int nodal_due;      // the latest outer needs a nodal update before its test
+  int max_reached;
+  int need_prologue;  // recompute f and e1 at the start of an outer() call
+  int im, jm, km;     // location of ndmax (1-based)
+  int nodal_updates;
+  int err_node;       // box index attached to a device error, -1 if none
+  int pad0;
+  unsigned bar_count; // grid barrier state
+  unsigned bar_gen;
+  unsigned pad1[14];
+};
+
+// Box geometry shared by all kernels.  Box index b = i + nxx*(j + nyy*k),
+// 0-based.  Vectors that are read at neighbours carry one halo plane on
+// each side: pointer + b is valid for b in [-plane, NB + plane).
+struct BoxGeom {
+  int nxx, nyy, nzz;
+  int NB, plane;
+  int ng;
+  const unsigned char* nbm;    // [NB]
+  const double* xdel;          // [nxx]
+  const double* ydel;          // [nyy]
+  const double* zdel;          // [nzz]
+  const double* vdel;          // [NB], 0 outside the core
+  int bcf[6];                  // boundary condition of each face direction
+};
+
+__device__ __forceinline__ int face_off(const BoxGeom& G, int f) {
+  switch (f) {
+    case FXP: return 1;
+    case FXM: return -1;
+    case FYP: return G.nxx;
+    case FYM: return -G.nxx;
+    case FZP: return G.plane;
+    default: return -G.plane;
+  }
+}
+
+__device__ __forceinline__ double hdir(const BoxGeom& G, int u, int b) {
+  // u = 0 x, 1 y, 2 z
+  if (u == 0) return G.xdel[b % G.nxx];
+  if (u == 1) return G.ydel[(b / G.nxx) % G.nyy];
+  return G.zdel[b / G.plane];
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ unsigned atom_add_acqrel_gpu(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void set_status(OuterCtl* C, int code) {
+  atomicCAS(&C->status, 0, code);
+}
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
+// wait is bounded: after kBarrierTimeoutNs the block records
+// ADP_ERR_TIMEOUT and returns false, so a fault elsewhere can never leave
+// the kernel spinning.  `gen` is the generation this block expects; every
+// block reads it at kernel start, before any block can arrive.
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ bool grid_barrier(OuterCtl* C, unsigned nblocks, unsigned& gen) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    unsigned arrived = atom_add_acqrel_gpu(&C->bar_count, 1u);
+    if (arrived == nblocks - 1) {
+      C->bar_count = 0;
+      st_release_gpu(&C->bar_gen, gen + 1);
+    } else {
+      unsigned long long t0 = globaltimer_ns();
+      while (ld_acquire_gpu(&C->bar_gen) == gen) {
+        if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
+          set_status(C, ADP_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    gen += 1;
+    if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ---- deterministic reductions ------------------------------------------
+// Sums use a fixed tree (xor-butterfly inside warps, warp results in order),
+// so every block that reduces the same partials gets bit-identical totals.
+
+template <bool MAX>
+__device__ __forceinline__ double warp_all(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = MAX ? fmax(v, w) : v + w;
+  }
+  return v;
+}
+
+// Reduce NQ per-thread values over the block; thread 0 writes them to
+// out[q * kMaxBlocks + blockIdx.x].  MAXMASK bit q selects max instead of sum.
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ void block_partials(const double (&v)[NQ], double* out) {
+  __shared__ double sw[NQ][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    double x = ((MAXMASK >> q) & 1u) ? warp_all<true>(v[q]) : warp_all<false>(v[q]);
+    if (lane == 0) sw[q][w] = x;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const bool mx = (MAXMASK >> q) & 1u;
+      double x = lane < nw ? sw[q][lane] : 0.0;   // sums and maxima of |.| start at 0
+      x = mx ? warp_all<true>(x) : warp_all<false>(x);
+      if (lane == 0) out[q * kMaxBlocks + blockIdx.x] = x;
+    }
+  }
+  __syncthreads();
+}
+
+// Totals of NQ quantities from the partials of nblk blocks, identical in
+// every block; every thread of the block receives them.
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ void grid_totals(const double* in, int nblk, double (&tot)[NQ]) {
+  __shared__ double st[NQ];
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const bool mx = (MAXMASK >> q) & 1u;
+      const double* src = in + q * kMaxBlocks;
+      double x = 0.0;
+      for (int k = lane; k < nblk; k += 32) {
+        double y = __ldcg(src + k);   // L2: partials were written by other SMs
+        x = mx ? fmax(x, y) : x + y;
+      }
+      x = mx ? warp_all<true>(x) : warp_all<false>(x);
+      if (lane == 0) st[q] = x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) tot[q] = st[q];
+  __syncthreads();
+}
+
+}  // namespace adp

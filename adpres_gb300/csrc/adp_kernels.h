@@ -1,0 +1,106 @@
+// Kernel parameter blocks and launchers shared by the host side (capi.cu)
+// and the kernel translation units (cmfd.cu, nodal.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "adp_device.cuh"
+
+namespace adp {
+
+// Single-precision default literals of the reference promoted to double.
+constexpr double kF1em2 = (double)1.e-2f;   // mod_cmfd.f90:495
+constexpr double kF1em4 = (double)10e-5f;   // mod_nodal.f90:856
+constexpr double kF1em5 = (double)1.e-5f;   // mod_data.f90:78-79
+
+// Persistent outer-iteration kernel (outer / outer_ad, mod_cmfd.f90:415-699).
+struct OuterParams {
+  BoxGeom G;
+  int ng, nin, nac, nupd, nout, adj, do_nodal, mixed;
+  double serc, ferc;
+  long long NBH;              // group stride of halo'd arrays
+  const double* A;            // [ng][7][NB] FP64 CMFD matrix
+  const float* A32;           // [ng][7][NB] FP32 copy (mixed storage)
+  double* phi[2];             // [ng][NBH] flux double buffer (halo offset applied)
+  double* fs[2];              // [NB] fission source double buffer
+  const double* wsrc;         // weight of fs0 in the group source: chi (fwd) / nuf (adj), [ng][NB]
+  const double* wfis;         // weight of the flux in the fission source: nuf (fwd) / chi (adj)
+  const double* sigs;         // [ng(from)][ng(to)][NB]
+  double* r;                  // Krylov vectors, halo'd [NBH]
+  double* rs;
+  double* pv[2];
+  double* vv[2];
+  double* s;
+  double* t;
+  float* r32;                 // FP32 Krylov vectors (mixed), halo'd [NBH]
+  float* rs32;
+  float* pv32[2];
+  float* vv32[2];
+  float* s32;
+  float* t32;
+  double* red;                // [2][kRedQ][kMaxBlocks]
+  OuterCtl* ctl;
+  double* tr_k;
+  double* tr_ser;
+  double* tr_fer;
+  int* tr_flags;
+  double* tr_ndmax;
+};
+
+// Nodal update (mod_nodal.f90) and matrix set-up (mod_cmfd.f90:11-304).
+struct NodalParams {
+  BoxGeom G;
+  int ng, cmode, pnm, nnod, nout;
+  double serc, ferc;
+  long long NBH;
+  const int* act;             // [nnod] box index of each node in reference order
+  const double* phi[2];
+  const double* D;            // [ng][NB]
+  const double* sigr;
+  const double* nuf;
+  const double* chin;         // chi of the node's material, [ng][NB]
+  const double* sigs;         // [ng][ng][NB]
+  const double* df;           // [ng][6][NB]
+  double* dn;                 // [ng][6][NB]
+  const double* dc;           // [ng][6][NB]
+  const double* sanm;         // [3][6][ng][NB] SANM constants A,B,E,F,G,H per direction
+  double* S;                  // [3][ng][NB] zeroth-order transverse-leakage sources S1..S3
+  double* a2;                 // [3][ng][NB]
+  double* a4;
+  double* L1;
+  const int* evbase;          // [3][NB] sweep-order index of a node's minus face
+  double* nd_val;             // [kMaxBlocks] ndmax partials
+  long long* nd_key;
+  int* nd_loc;
+  int nd_blocks;
+  OuterCtl* ctl;
+  double* tr_ndmax;
+  int* tr_flags;
+};
+
+struct AssembleParams {
+  BoxGeom G;
+  int ng;
+  int with_coupling;          // 1: recompute df first (matrix_setup(1))
+  const double* D;
+  const double* sigr;
+  double* df;
+  const double* dn;
+  double* A;
+  float* A32;
+};
+
+// Launchers (return the launch error, if any)
+cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st);
+cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st);
+cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st);
+int outer_max_blocks_per_sm(int threads, int mixed);
+cudaError_t launch_power(const BoxGeom& G, int ng, long long NBH, const double* phi, const double* sigf,
+                         double* pbox, double* red, OuterCtl* ctl, cudaStream_t st);
+cudaError_t launch_sanm_consts(const NodalParams& P, cudaStream_t st);
+cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st);
+cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, const double* sigtr,
+                           const double* siga, const double* sigs, double* D, double* sigr, OuterCtl* ctl,
+                           cudaStream_t st);
+
+}  // namespace adp

@@ -1,0 +1,908 @@
+// Host side of the C ABI (include/adpres_gb300.h): the core handle, layout
+// conversion between the reference's node order and the padded device box,
+// and the driver loop that stands in for outer()/outer_ad()
+// (mod_cmfd.f90:415-509, :602-699).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/adpres_gb300.h"
+#include "adp_kernels.h"
+
+using namespace adp;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_create_err;
+
+struct DevArena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  void* take(size_t bytes) {
+    size_t off = (used + 255) & ~(size_t)255;
+    used = off + bytes;
+    return base + off;
+  }
+};
+
+}  // namespace
+
+struct adp_handle {
+  std::string err;
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+  // geometry
+  int nxx = 0, nyy = 0, nzz = 0, nnod = 0, NB = 0, plane = 0, ng = 0;
+  long long NBH = 0;
+  std::vector<int> node2box;
+  std::vector<unsigned char> nbm;
+  std::vector<int> ysmin, ysmax, xsmin, xsmax;
+  std::vector<double> xdel, ydel, zdel, vdel;
+  int bcf[6] = {0, 0, 0, 0, 0, 0};
+  adp_opts o{};
+  int nmat = 0;
+  // device memory
+  DevArena ar;
+  unsigned char* d_nbm = nullptr;
+  double *d_xdel = nullptr, *d_ydel = nullptr, *d_zdel = nullptr, *d_vdel = nullptr;
+  int *d_act = nullptr, *d_evbase = nullptr;
+  double *d_D = nullptr, *d_sigr = nullptr, *d_nuf = nullptr, *d_sigf = nullptr, *d_chin = nullptr;
+  double *d_sigs = nullptr, *d_dc = nullptr, *d_sigtr = nullptr, *d_siga = nullptr;
+  double *d_df = nullptr, *d_dn = nullptr, *d_A = nullptr;
+  float* d_A32 = nullptr;
+  double* d_phi[2] = {nullptr, nullptr};
+  double* d_fs[2] = {nullptr, nullptr};
+  double *d_r = nullptr, *d_rs = nullptr, *d_s = nullptr, *d_t = nullptr;
+  double* d_pv[2] = {nullptr, nullptr};
+  double* d_vv[2] = {nullptr, nullptr};
+  float *d_r32 = nullptr, *d_rs32 = nullptr, *d_s32 = nullptr, *d_t32 = nullptr;
+  float* d_pv32[2] = {nullptr, nullptr};
+  float* d_vv32[2] = {nullptr, nullptr};
+  double* d_red = nullptr;
+  OuterCtl* d_ctl = nullptr;
+  OuterCtl* h_ctl = nullptr;   // pinned mirror
+  double *d_tr_k = nullptr, *d_tr_ser = nullptr, *d_tr_fer = nullptr, *d_tr_ndmax = nullptr;
+  int* d_tr_flags = nullptr;
+  double *d_sanm = nullptr, *d_S = nullptr, *d_a2 = nullptr, *d_a4 = nullptr, *d_L1 = nullptr;
+  double* d_ndval = nullptr;
+  long long* d_ndkey = nullptr;
+  int* d_ndloc = nullptr;
+  double* d_pbox = nullptr;
+  // state
+  bool xs_set = false;
+  bool started[2] = {false, false};
+  int launch_blocks = 0, launch_threads = 0;
+  int sms = 0;
+  adp_timers tm{};
+};
+
+namespace {
+
+adp_status fail(adp_handle* h, adp_status s, const std::string& msg) {
+  if (h) h->err = msg;
+  else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_create_err = msg;
+  }
+  return s;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return fail(h, ADP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+  } while (0)
+
+BoxGeom box_geom(const adp_handle* h) {
+  BoxGeom G;
+  G.nxx = h->nxx;
+  G.nyy = h->nyy;
+  G.nzz = h->nzz;
+  G.NB = h->NB;
+  G.plane = h->plane;
+  G.ng = h->ng;
+  G.nbm = h->d_nbm;
+  G.xdel = h->d_xdel;
+  G.ydel = h->d_ydel;
+  G.zdel = h->d_zdel;
+  G.vdel = h->d_vdel;
+  for (int f = 0; f < 6; ++f) G.bcf[f] = h->bcf[f];
+  return G;
+}
+
+// Upload a node-major Fortran array a(nnod, ng[, m]) into the box layout
+// [ng][m][NB] (or [ng][NB]); inactive box positions get 0.
+template <class T>
+void to_box(const adp_handle* h, const T* src, int ncomp, std::vector<T>& out) {
+  const int nn = h->nnod, NB = h->NB;
+  out.assign((size_t)ncomp * NB, T(0));
+  for (int c = 0; c < ncomp; ++c)
+    for (int n = 0; n < nn; ++n) out[(size_t)c * NB + h->node2box[n]] = src[(size_t)c * nn + n];
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t adp_last_error(const adp_handle* h, char* buf, size_t len) {
+  std::string m;
+  if (h) m = h->err;
+  else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    m = g_create_err;
+  }
+  if (buf && len) {
+    size_t n = std::min(len - 1, m.size());
+    std::memcpy(buf, m.data(), n);
+    buf[n] = 0;
+  }
+  return m.size();
+}
+
+adp_status adp_destroy(adp_handle* h) {
+  if (!h) return ADP_OK;
+  cudaSetDevice(h->dev);
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->ar.base) cudaFree(h->ar.base);
+  if (h->h_ctl) cudaFreeHost(h->h_ctl);
+  for (cudaEvent_t e : {h->e0, h->e1, h->e2, h->e3})
+    if (e) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return ADP_OK;
+}
+
+adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** out) {
+  adp_handle* h = nullptr;
+  if (!geom || !opts || !out) return fail(nullptr, ADP_ERR_INPUT, "adp_create: null argument");
+  *out = nullptr;
+  const adp_geom& g = *geom;
+  if (g.nxx < 1 || g.nyy < 1 || g.nzz < 2 || g.nnod < 1 || !g.ix || !g.iy || !g.iz || !g.xdel || !g.ydel || !g.zdel)
+    return fail(nullptr, ADP_ERR_INPUT, "adp_create: bad geometry sizes or null arrays");
+  if (opts->ng < 1 || opts->ng > kMaxGroups)
+    return fail(nullptr, ADP_ERR_UNSUPPORTED, "adp_create: groups must be 1..8");
+  if (opts->kern < 0 || opts->kern > 2 || opts->precision < 0 || opts->precision > 1)
+    return fail(nullptr, ADP_ERR_INPUT, "adp_create: bad kern or precision");
+  int bcs[6] = {g.east, g.west, g.north, g.south, g.bottom, g.top};
+  for (int b : bcs)
+    if (b < 0 || b > 2) return fail(nullptr, ADP_ERR_INPUT, "adp_create: boundary conditions must be 0, 1 or 2");
+  long long nb64 = (long long)g.nxx * g.nyy * g.nzz;
+  if (nb64 > 400000000LL) return fail(nullptr, ADP_ERR_INPUT, "adp_create: box too large");
+
+  h = new adp_handle();
+  h->nxx = g.nxx;
+  h->nyy = g.nyy;
+  h->nzz = g.nzz;
+  h->nnod = g.nnod;
+  h->ng = opts->ng;
+  h->NB = (int)nb64;
+  h->plane = g.nxx * g.nyy;
+  h->NBH = (long long)h->NB + 2LL * h->plane;
+  // face order X+ X- Y+ Y- Z+ Z- : east west north south top bottom
+  h->bcf[FXP] = g.east;
+  h->bcf[FXM] = g.west;
+  h->bcf[FYP] = g.north;
+  h->bcf[FYM] = g.south;
+  h->bcf[FZP] = g.top;
+  h->bcf[FZM] = g.bottom;
+  h->xdel.assign(g.xdel, g.xdel + g.nxx);
+  h->ydel.assign(g.ydel, g.ydel + g.nyy);
+  h->zdel.assign(g.zdel, g.zdel + g.nzz);
+  for (double d : h->xdel) if (!(d > 0)) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: node sizes must be > 0"); }
+  for (double d : h->ydel) if (!(d > 0)) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: node sizes must be > 0"); }
+  for (double d : h->zdel) if (!(d > 0)) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: node sizes must be > 0"); }
+
+  // Outline from the plane iz == 1 (mod_io.f90:1071-1110).
+  const int nxx = g.nxx, nyy = g.nyy, nzz = g.nzz;
+  h->ysmin.assign(nyy, nxx);
+  h->ysmax.assign(nyy, -1);
+  h->xsmin.assign(nxx, nyy);
+  h->xsmax.assign(nxx, -1);
+  for (int n = 0; n < g.nnod; ++n) {
+    int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1;
+    if (i < 0 || i >= nxx || j < 0 || j >= nyy || k < 0 || k >= nzz) {
+      adp_destroy(h);
+      return fail(nullptr, ADP_ERR_INPUT, "adp_create: node index out of the box");
+    }
+    if (k == 0) {
+      h->ysmin[j] = std::min(h->ysmin[j], i);
+      h->ysmax[j] = std::max(h->ysmax[j], i);
+      h->xsmin[i] = std::min(h->xsmin[i], j);
+      h->xsmax[i] = std::max(h->xsmax[i], j);
+    }
+  }
+  // The node order must be the reference's (misc, mod_io.f90:1317-1330).
+  {
+    int n = 0;
+    std::vector<unsigned char> on((size_t)nxx * nyy, 0);
+    for (int k = 0; k < nzz; ++k)
+      for (int j = 0; j < nyy; ++j)
+        for (int i = h->ysmin[j]; i <= h->ysmax[j]; ++i) {
+          if (n >= g.nnod || g.ix[n] - 1 != i || g.iy[n] - 1 != j || g.iz[n] - 1 != k) {
+            adp_destroy(h);
+            return fail(nullptr, ADP_ERR_INPUT, "adp_create: nodes are not in the reference order (k, j, i over the plane-1 outline)");
+          }
+          if (k == 0) on[(size_t)j * nxx + i] = 1;
+          ++n;
+        }
+    if (n != g.nnod) {
+      adp_destroy(h);
+      return fail(nullptr, ADP_ERR_INPUT, "adp_create: node count does not match the outline");
+    }
+    // Column and row outlines must agree (the reference's zero-material
+    // check, mod_io.f90:1112-1132), and every line needs two nodes
+    // (the two-node sweeps read a neighbour at every line end).
+    for (int i = 0; i < nxx; ++i) {
+      if (h->xsmax[i] - h->xsmin[i] < 1) {
+        adp_destroy(h);
+        return fail(nullptr, ADP_ERR_INPUT, "adp_create: a y column holds fewer than two nodes");
+      }
+      for (int j = h->xsmin[i]; j <= h->xsmax[i]; ++j)
+        if (!on[(size_t)j * nxx + i]) {
+          adp_destroy(h);
+          return fail(nullptr, ADP_ERR_INPUT, "adp_create: outline has a hole inside the core");
+        }
+    }
+    for (int j = 0; j < nyy; ++j)
+      if (h->ysmax[j] - h->ysmin[j] < 1) {
+        adp_destroy(h);
+        return fail(nullptr, ADP_ERR_INPUT, "adp_create: an x row holds fewer than two nodes");
+      }
+  }
+  h->node2box.resize(g.nnod);
+  h->nbm.assign(h->NB, 0);
+  h->vdel.assign(h->NB, 0.0);
+  for (int n = 0; n < g.nnod; ++n) {
+    int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1;
+    int b = i + nxx * (j + nyy * k);
+    h->node2box[n] = b;
+    unsigned m = NB_ACTIVE;
+    if (i != h->ysmax[j]) m |= 1u << FXP;
+    if (i != h->ysmin[j]) m |= 1u << FXM;
+    if (j != h->xsmax[i]) m |= 1u << FYP;
+    if (j != h->xsmin[i]) m |= 1u << FYM;
+    if (k != nzz - 1) m |= 1u << FZP;
+    if (k != 0) m |= 1u << FZM;
+    h->nbm[b] = (unsigned char)m;
+    h->vdel[b] = h->xdel[i] * h->ydel[j] * h->zdel[k];
+  }
+  // Sweep-order index of each node's minus face, per direction
+  // (mod_nodal.f90:53-125: x lines over (k,j), y lines over (k,i), z lines
+  // over the plane-1 columns in node order).
+  std::vector<int> evbase((size_t)3 * h->NB, 0);
+  {
+    std::vector<long long> prefx(nyy), prefy(nxx);
+    long long Tx = 0, Ty = 0;
+    for (int j = 0; j < nyy; ++j) { prefx[j] = Tx; Tx += h->ysmax[j] - h->ysmin[j] + 2; }
+    for (int i = 0; i < nxx; ++i) { prefy[i] = Ty; Ty += h->xsmax[i] - h->xsmin[i] + 2; }
+    long long base_y = Tx * nzz, base_z = base_y + Ty * nzz;
+    std::vector<int> col((size_t)nxx * nyy, -1);
+    int c = 0;
+    for (int j = 0; j < nyy; ++j)
+      for (int i = h->ysmin[j]; i <= h->ysmax[j]; ++i) col[(size_t)j * nxx + i] = c++;
+    long long total = base_z + (long long)c * (nzz + 1);
+    if (total * kMaxGroups > 0x7fffffffffffLL) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: too many faces"); }
+    if (total > 0x7fffffffLL) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: too many faces"); }
+    for (int n = 0; n < g.nnod; ++n) {
+      int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1, b = h->node2box[n];
+      evbase[b] = (int)(k * Tx + prefx[j] + (i - h->ysmin[j]));
+      evbase[(size_t)h->NB + b] = (int)(base_y + k * Ty + prefy[i] + (j - h->xsmin[i]));
+      evbase[(size_t)2 * h->NB + b] = (int)(base_z + (long long)col[(size_t)j * nxx + i] * (nzz + 1) + k);
+    }
+  }
+
+  // Options with the reference defaults.
+  h->o = *opts;
+  if (h->o.nin < 1) h->o.nin = 2;
+  if (h->o.nout < 1) h->o.nout = 500;
+  if (h->o.nac < 1) h->o.nac = 5;
+  if (h->o.nupd < 1) h->o.nupd = (int)std::ceil((float)(nxx + nyy + nzz) / 2.5f);
+  if (!(h->o.serc > 0)) h->o.serc = kF1em5;
+  if (!(h->o.ferc > 0)) h->o.ferc = kF1em5;
+  if (h->o.nout < h->o.nupd && h->o.kern != ADP_KERN_FDM) {
+    adp_destroy(h);
+    return fail(nullptr, ADP_ERR_INPUT, "max. number of outer iteration should be bigger than nodal update interval");
+  }
+
+  // Device resources.
+  cudaError_t ce = cudaGetDevice(&h->dev);
+  if (ce != cudaSuccess) { adp_destroy(h); return fail(nullptr, ADP_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(ce)); }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, h->dev);
+  h->sms = prop.multiProcessorCount;
+  if (!prop.cooperativeLaunch) { adp_destroy(h); return fail(nullptr, ADP_ERR_CUDA, "device lacks cooperative launch"); }
+  if ((ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking)) != cudaSuccess ||
+      (ce = cudaEventCreate(&h->e0)) != cudaSuccess || (ce = cudaEventCreate(&h->e1)) != cudaSuccess ||
+      (ce = cudaEventCreate(&h->e2)) != cudaSuccess || (ce = cudaEventCreate(&h->e3)) != cudaSuccess ||
+      (ce = cudaMallocHost((void**)&h->h_ctl, sizeof(OuterCtl))) != cudaSuccess) {
+    adp_destroy(h);
+    return fail(nullptr, ADP_ERR_CUDA, std::string("stream/event set-up: ") + cudaGetErrorString(ce));
+  }
+  const size_t NB = h->NB, G = h->ng, NBH = h->NBH, nn = h->nnod, nout = h->o.nout;
+  const bool mixed = h->o.precision == ADP_MIXED;
+  size_t bytes = 0;
+  auto add = [&](size_t b) { bytes += ((b + 255) & ~(size_t)255) + 256; };
+  add(NB); add(nxx * 8); add(nyy * 8); add(nzz * 8); add(NB * 8); add(nn * 4); add(3 * NB * 4);
+  add(G * NB * 8 * 7);              // D sigr nuf sigf chin sigtr siga
+  add(G * G * NB * 8);              // sigs
+  add(G * 6 * NB * 8 * 3);          // dc df dn
+  add(G * 7 * NB * 8);              // A
+  if (mixed) add(G * 7 * NB * 4);   // A32
+  add(G * NBH * 8 * 2);             // phi
+  add(NB * 8 * 2);                  // fs
+  add(NBH * 8 * 8);                 // Krylov FP64
+  if (mixed) add(NBH * 4 * 8);      // Krylov FP32
+  add(2 * kRedQ * kMaxBlocks * 8);
+  add(sizeof(OuterCtl));
+  add(nout * 8 * 4 + nout * 4);
+  if (opts->kern == ADP_KERN_SANM) add(3 * 6 * G * NB * 8);
+  if (opts->kern != ADP_KERN_FDM) add(3 * G * NB * 8 * 4);
+  add(kMaxBlocks * 8 * 2 + kMaxBlocks * 4);
+  add(NB * 8);
+  h->ar.size = bytes;
+  if ((ce = cudaMalloc((void**)&h->ar.base, bytes)) != cudaSuccess) {
+    adp_destroy(h);
+    return fail(nullptr, ADP_ERR_CUDA, std::string("cudaMalloc of the core state: ") + cudaGetErrorString(ce));
+  }
+  DevArena& A = h->ar;
+  h->d_nbm = (unsigned char*)A.take(NB);
+  h->d_xdel = (double*)A.take(nxx * 8);
+  h->d_ydel = (double*)A.take(nyy * 8);
+  h->d_zdel = (double*)A.take(nzz * 8);
+  h->d_vdel = (double*)A.take(NB * 8);
+  h->d_act = (int*)A.take(nn * 4);
+  h->d_evbase = (int*)A.take(3 * NB * 4);
+  h->d_D = (double*)A.take(G * NB * 8);
+  h->d_sigr = (double*)A.take(G * NB * 8);
+  h->d_nuf = (double*)A.take(G * NB * 8);
+  h->d_sigf = (double*)A.take(G * NB * 8);
+  h->d_chin = (double*)A.take(G * NB * 8);
+  h->d_sigtr = (double*)A.take(G * NB * 8);
+  h->d_siga = (double*)A.take(G * NB * 8);
+  h->d_sigs = (double*)A.take(G * G * NB * 8);
+  h->d_dc = (double*)A.take(G * 6 * NB * 8);
+  h->d_df = (double*)A.take(G * 6 * NB * 8);
+  h->d_dn = (double*)A.take(G * 6 * NB * 8);
+  h->d_A = (double*)A.take(G * 7 * NB * 8);
+  if (mixed) h->d_A32 = (float*)A.take(G * 7 * NB * 4);
+  for (int t = 0; t < 2; ++t) h->d_phi[t] = (double*)A.take(G * NBH * 8) + h->plane;
+  for (int t = 0; t < 2; ++t) h->d_fs[t] = (double*)A.take(NB * 8);
+  double* kv = (double*)A.take(NBH * 8 * 8);
+  double** kp[8] = {&h->d_r, &h->d_rs, &h->d_pv[0], &h->d_pv[1], &h->d_vv[0], &h->d_vv[1], &h->d_s, &h->d_t};
+  for (int q = 0; q < 8; ++q) *kp[q] = kv + (size_t)q * NBH + h->plane;
+  if (mixed) {
+    float* kf = (float*)A.take(NBH * 4 * 8);
+    float** kq[8] = {&h->d_r32, &h->d_rs32, &h->d_pv32[0], &h->d_pv32[1], &h->d_vv32[0], &h->d_vv32[1], &h->d_s32, &h->d_t32};
+    for (int q = 0; q < 8; ++q) *kq[q] = kf + (size_t)q * NBH + h->plane;
+  }
+  h->d_red = (double*)A.take(2 * kRedQ * kMaxBlocks * 8);
+  h->d_ctl = (OuterCtl*)A.take(sizeof(OuterCtl));
+  h->d_tr_k = (double*)A.take(nout * 8);
+  h->d_tr_ser = (double*)A.take(nout * 8);
+  h->d_tr_fer = (double*)A.take(nout * 8);
+  h->d_tr_ndmax = (double*)A.take(nout * 8);
+  h->d_tr_flags = (int*)A.take(nout * 4);
+  if (opts->kern == ADP_KERN_SANM) h->d_sanm = (double*)A.take(3 * 6 * G * NB * 8);
+  if (opts->kern != ADP_KERN_FDM) {
+    h->d_S = (double*)A.take(3 * G * NB * 8);
+    h->d_a2 = (double*)A.take(3 * G * NB * 8);
+    h->d_a4 = (double*)A.take(3 * G * NB * 8);
+    h->d_L1 = (double*)A.take(3 * G * NB * 8);
+  }
+  h->d_ndval = (double*)A.take(kMaxBlocks * 8);
+  h->d_ndkey = (long long*)A.take(kMaxBlocks * 8);
+  h->d_ndloc = (int*)A.take(kMaxBlocks * 4);
+  h->d_pbox = (double*)A.take(NB * 8);
+  if (A.used > A.size) { adp_destroy(h); return fail(nullptr, ADP_ERR_CUDA, "internal: arena overflow"); }
+
+  // Zero everything (halos, inactive positions, dn = 0 as coup_coef's first call).
+  if ((ce = cudaMemsetAsync(A.base, 0, A.size, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_nbm, h->nbm.data(), NB, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_xdel, h->xdel.data(), nxx * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_ydel, h->ydel.data(), nyy * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_zdel, h->zdel.data(), nzz * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_vdel, h->vdel.data(), NB * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_act, h->node2box.data(), nn * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaMemcpyAsync(h->d_evbase, evbase.data(), 3 * NB * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess) {
+    adp_destroy(h);
+    return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
+  }
+  OuterCtl c0;
+  std::memset(&c0, 0, sizeof c0);
+  c0.Ke = 1.0;
+  c0.err_node = -1;
+  *h->h_ctl = c0;
+  if ((ce = cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
+      (ce = cudaStreamSynchronize(h->st)) != cudaSuccess) {
+    adp_destroy(h);
+    return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
+  }
+  h->launch_threads = 512;
+  *out = h;
+  return ADP_OK;
+}
+
+static adp_status upload_xs_common(adp_handle* h, int nmat, const double* nuf, const double* sigf, const double* chi,
+                                   const int* mat, const double* sigs, const double* dc) {
+  const int nn = h->nnod, G = h->ng;
+  if (nmat < 1 || !nuf || !sigf || !chi || !mat || !sigs) return fail(h, ADP_ERR_INPUT, "adp_set_xs: null array");
+  std::vector<double> chin((size_t)G * nn);
+  for (int n = 0; n < nn; ++n) {
+    if (mat[n] < 1 || mat[n] > nmat) return fail(h, ADP_ERR_INPUT, "adp_set_xs: material number out of range");
+    for (int g = 0; g < G; ++g) chin[(size_t)g * nn + n] = chi[(size_t)g * nmat + (mat[n] - 1)];
+  }
+  // check_xs on the inputs that are not recomputed (mod_xsec.f90:90-168)
+  for (size_t q = 0; q < (size_t)G * nn; ++q)
+    if (nuf[q] < 0.) return fail(h, ADP_ERR_BADXS, "nu*fission xs is negative");
+  for (size_t q = 0; q < (size_t)G * nmat; ++q)
+    if (chi[q] < 0.) return fail(h, ADP_ERR_BADXS, "fission spectrum is negative");
+  for (size_t q = 0; q < (size_t)G * G * nn; ++q)
+    if (sigs[q] < 0.) return fail(h, ADP_ERR_BADXS, "scattering xs is negative");
+  std::vector<double> box;
+  to_box(h, nuf, G, box);
+  CK(cudaMemcpyAsync(h->d_nuf, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  to_box(h, sigf, G, box);
+  CK(cudaMemcpyAsync(h->d_sigf, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  to_box(h, chin.data(), G, box);
+  CK(cudaMemcpyAsync(h->d_chin, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  // sigs(n, g, h) (Fortran, n fastest, g -> h) -> device [g][h][b]
+  box.assign((size_t)G * G * h->NB, 0.0);
+  for (int g = 0; g < G; ++g)
+    for (int hh = 0; hh < G; ++hh)
+      for (int n = 0; n < nn; ++n)
+        box[((size_t)g * G + hh) * h->NB + h->node2box[n]] = sigs[((size_t)hh * G + g) * nn + n];
+  CK(cudaMemcpyAsync(h->d_sigs, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (dc) {
+    // dc(n, g, u) (Fortran) -> device [g][u][b]
+    box.assign((size_t)G * 6 * h->NB, 0.0);
+    for (int u = 0; u < 6; ++u)
+      for (int g = 0; g < G; ++g)
+        for (int n = 0; n < nn; ++n)
+          box[((size_t)g * 6 + u) * h->NB + h->node2box[n]] = dc[((size_t)u * G + g) * nn + n];
+  } else {
+    box.assign((size_t)G * 6 * h->NB, 0.0);
+    for (int c = 0; c < G * 6; ++c)
+      for (int n = 0; n < nn; ++n) box[(size_t)c * h->NB + h->node2box[n]] = 1.0;
+  }
+  CK(cudaMemcpyAsync(h->d_dc, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->nmat = nmat;
+  return ADP_OK;
+}
+
+static NodalParams nodal_params(adp_handle* h, int cmode) {
+  NodalParams P;
+  std::memset(&P, 0, sizeof P);
+  P.G = box_geom(h);
+  P.ng = h->ng;
+  P.cmode = cmode;
+  P.pnm = h->o.kern == ADP_KERN_PNM;
+  P.nnod = h->nnod;
+  P.nout = h->o.nout;
+  P.serc = h->o.serc;
+  P.ferc = h->o.ferc;
+  P.NBH = h->NBH;
+  P.act = h->d_act;
+  P.phi[0] = h->d_phi[0];
+  P.phi[1] = h->d_phi[1];
+  P.D = h->d_D;
+  P.sigr = h->d_sigr;
+  P.nuf = h->d_nuf;
+  P.chin = h->d_chin;
+  P.sigs = h->d_sigs;
+  P.df = h->d_df;
+  P.dn = h->d_dn;
+  P.dc = h->d_dc;
+  P.sanm = h->d_sanm;
+  P.S = h->d_S;
+  P.a2 = h->d_a2;
+  P.a4 = h->d_a4;
+  P.L1 = h->d_L1;
+  P.evbase = h->d_evbase;
+  P.nd_val = h->d_ndval;
+  P.nd_key = h->d_ndkey;
+  P.nd_loc = h->d_ndloc;
+  P.ctl = h->d_ctl;
+  P.tr_ndmax = h->d_tr_ndmax;
+  P.tr_flags = h->d_tr_flags;
+  return P;
+}
+
+static adp_status after_xs(adp_handle* h) {
+  if (h->o.kern == ADP_KERN_SANM) {
+    // get_ABEFGH depends on sigr, D and the node sizes only
+    NodalParams P = nodal_params(h, 1);
+    CK(launch_sanm_consts(P, h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
+  h->xs_set = true;
+  return ADP_OK;
+}
+
+adp_status adp_set_xs(adp_handle* h, int nmat, const double* D, const double* sigr, const double* nuf,
+                      const double* sigf, const double* chi, const int* mat, const double* sigs, const double* dc) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!D || !sigr) return fail(h, ADP_ERR_INPUT, "adp_set_xs: null D or sigr");
+  const size_t q = (size_t)h->ng * h->nnod;
+  for (size_t k = 0; k < q; ++k) {
+    if (D[k] < (double)1.e-20f) return fail(h, ADP_ERR_BADXS, "diffusion coef. is close to zero or negative");
+    if (sigr[k] < 0.) return fail(h, ADP_ERR_BADXS, "removal xs is negative");
+  }
+  adp_status s = upload_xs_common(h, nmat, nuf, sigf, chi, mat, sigs, dc);
+  if (s != ADP_OK) return s;
+  std::vector<double> box;
+  to_box(h, D, h->ng, box);
+  CK(cudaMemcpyAsync(h->d_D, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  to_box(h, sigr, h->ng, box);
+  CK(cudaMemcpyAsync(h->d_sigr, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  return after_xs(h);
+}
+
+adp_status adp_xs_updt_nodes(adp_handle* h, int nmat, const double* sigtr, const double* siga, const double* nuf,
+                             const double* sigf, const double* chi, const int* mat, const double* sigs,
+                             const double* dc) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!sigtr || !siga) return fail(h, ADP_ERR_INPUT, "adp_xs_updt: null sigtr or siga");
+  adp_status s = upload_xs_common(h, nmat, nuf, sigf, chi, mat, sigs, dc);
+  if (s != ADP_OK) return s;
+  std::vector<double> box;
+  to_box(h, sigtr, h->ng, box);
+  CK(cudaMemcpyAsync(h->d_sigtr, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  to_box(h, siga, h->ng, box);
+  CK(cudaMemcpyAsync(h->d_siga, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  // reset the device status, then Dsigr_updt + checks on the device
+  h->h_ctl->status = 0;
+  h->h_ctl->err_node = -1;
+  CK(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(&h->d_ctl->err_node, &h->h_ctl->err_node, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CK(launch_xs_updt(box_geom(h), h->ng, h->d_act, h->nnod, h->d_sigtr, h->d_siga, h->d_sigs, h->d_D, h->d_sigr,
+                    h->d_ctl, h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (h->h_ctl->status != 0) {
+    int code = h->h_ctl->status;
+    h->h_ctl->status = 0;
+    CK(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return fail(h, (adp_status)code, "cross-section check failed (sigtr < 1e-5, D < 1e-20 or sigr < 0)");
+  }
+  return after_xs(h);
+}
+
+adp_status adp_xs_updt(adp_handle* h, int nmat, const double* xsigtr, const double* xsiga, const double* xnuf,
+                       const double* xsigf, const double* chi, const int* mat, const double* xsigs, const double* dc) {
+  if (!h) return ADP_ERR_INPUT;
+  if (!xsigtr || !xsiga || !xnuf || !xsigf || !xsigs || !mat || !chi)
+    return fail(h, ADP_ERR_INPUT, "adp_xs_updt: null array");
+  // base_updt (mod_xsec.f90:172-195)
+  const int nn = h->nnod, G = h->ng;
+  std::vector<double> st((size_t)G * nn), sa(st.size()), nf(st.size()), sf(st.size()), ss((size_t)G * G * nn);
+  for (int n = 0; n < nn; ++n) {
+    const int m = mat[n] - 1;
+    if (m < 0 || m >= nmat) return fail(h, ADP_ERR_INPUT, "adp_xs_updt: material number out of range");
+    for (int g = 0; g < G; ++g) {
+      st[(size_t)g * nn + n] = xsigtr[(size_t)g * nmat + m];
+      sa[(size_t)g * nn + n] = xsiga[(size_t)g * nmat + m];
+      nf[(size_t)g * nn + n] = xnuf[(size_t)g * nmat + m];
+      sf[(size_t)g * nn + n] = xsigf[(size_t)g * nmat + m];
+      for (int hh = 0; hh < G; ++hh)
+        ss[((size_t)hh * G + g) * nn + n] = xsigs[((size_t)hh * G + g) * nmat + m];
+    }
+  }
+  return adp_xs_updt_nodes(h, nmat, st.data(), sa.data(), nf.data(), sf.data(), chi, mat, ss.data(), dc);
+}
+
+static OuterParams outer_params(adp_handle* h, int adj) {
+  OuterParams P;
+  std::memset(&P, 0, sizeof P);
+  P.G = box_geom(h);
+  P.ng = h->ng;
+  P.nin = h->o.nin;
+  P.nac = h->o.nac;
+  P.nupd = h->o.nupd;
+  P.nout = h->o.nout;
+  P.adj = adj;
+  P.mixed = h->o.precision == ADP_MIXED;
+  P.serc = h->o.serc;
+  P.ferc = h->o.ferc;
+  P.NBH = h->NBH;
+  P.A = h->d_A;
+  P.A32 = h->d_A32;
+  for (int t = 0; t < 2; ++t) {
+    P.phi[t] = h->d_phi[t];
+    P.fs[t] = h->d_fs[t];
+    P.pv[t] = h->d_pv[t];
+    P.vv[t] = h->d_vv[t];
+    P.pv32[t] = h->d_pv32[t];
+    P.vv32[t] = h->d_vv32[t];
+  }
+  P.wsrc = adj ? h->d_nuf : h->d_chin;
+  P.wfis = adj ? h->d_chin : h->d_nuf;
+  P.sigs = h->d_sigs;
+  P.r = h->d_r;
+  P.rs = h->d_rs;
+  P.s = h->d_s;
+  P.t = h->d_t;
+  P.r32 = h->d_r32;
+  P.rs32 = h->d_rs32;
+  P.s32 = h->d_s32;
+  P.t32 = h->d_t32;
+  P.red = h->d_red;
+  P.ctl = h->d_ctl;
+  P.tr_k = h->d_tr_k;
+  P.tr_ser = h->d_tr_ser;
+  P.tr_fer = h->d_tr_fer;
+  P.tr_flags = h->d_tr_flags;
+  P.tr_ndmax = h->d_tr_ndmax;
+  return P;
+}
+
+static void launch_shape(adp_handle* h, int& blocks, int& threads) {
+  threads = h->launch_threads > 0 ? h->launch_threads : 512;
+  int occ = outer_max_blocks_per_sm(threads, h->o.precision == ADP_MIXED);
+  if (occ < 1) occ = 1;
+  int cap = std::min(h->sms * occ, kMaxBlocks);
+  int want = (int)std::max(1LL, ((long long)h->NB + 2LL * threads - 1) / (2LL * threads));
+  blocks = h->launch_blocks > 0 ? std::min(h->launch_blocks, cap) : std::min(want, cap);
+}
+
+static adp_status ctl_error(adp_handle* h, const OuterCtl& c) {
+  char buf[256];
+  int b = c.err_node;
+  int i = b >= 0 ? b % h->nxx + 1 : 0, j = b >= 0 ? (b / h->nxx) % h->nyy + 1 : 0, k = b >= 0 ? b / h->plane + 1 : 0;
+  switch (c.status) {
+    case ADP_ERR_PIVOT:
+      std::snprintf(buf, sizeof buf, "error in matrix decomp: diagonal elements close to zero at I = %d, J = %d, K = %d", i, j, k);
+      break;
+    case ADP_ERR_DIVERGED:
+      std::snprintf(buf, sizeof buf, "max. change in nodal coupling coefficient = %.1f: the two-node nonlinear iteration seems not stable", c.ndmax);
+      break;
+    case ADP_ERR_BREAKDOWN: std::snprintf(buf, sizeof buf, "BiCGSTAB breakdown (a zero inner product) at outer %d", c.p); break;
+    case ADP_ERR_NAN: std::snprintf(buf, sizeof buf, "non-finite eigenvalue or fission source at outer %d", c.p); break;
+    case ADP_ERR_TIMEOUT: std::snprintf(buf, sizeof buf, "a grid barrier wait ran out of time"); break;
+    case ADP_ERR_ZEROPOWER: std::snprintf(buf, sizeof buf, "total nodes power is zero or less"); break;
+    default: std::snprintf(buf, sizeof buf, "device error %d", c.status);
+  }
+  return fail(h, (adp_status)c.status, buf);
+}
+
+adp_status adp_set_launch(adp_handle* h, int blocks, int threads) {
+  if (!h) return ADP_ERR_INPUT;
+  if (threads != 0 && (threads < 64 || threads > 512 || threads % 32)) return fail(h, ADP_ERR_INPUT, "threads must be 64..512, a multiple of 32");
+  if (blocks < 0 || blocks > kMaxBlocks) return fail(h, ADP_ERR_INPUT, "blocks out of range");
+  h->launch_blocks = blocks;
+  h->launch_threads = threads;
+  return ADP_OK;
+}
+
+adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!h->xs_set) return fail(h, ADP_ERR_STATE, "adp_outer: cross sections not set");
+  if (mode != ADP_FORWARD && mode != ADP_ADJOINT) return fail(h, ADP_ERR_INPUT, "adp_outer: bad mode");
+  const int adj = mode == ADP_ADJOINT;
+  CK(cudaEventRecord(h->e0, h->st));
+  // matrix_setup(1): coupling coefficients + assembly
+  AssembleParams AP;
+  AP.G = box_geom(h);
+  AP.ng = h->ng;
+  AP.with_coupling = 1;
+  AP.D = h->d_D;
+  AP.sigr = h->d_sigr;
+  AP.df = h->d_df;
+  AP.dn = h->d_dn;
+  AP.A = h->d_A;
+  AP.A32 = h->d_A32;
+  CK(launch_assemble(AP, h->st));
+  OuterParams P = outer_params(h, adj);
+  // first-call start (mod_cmfd.f90:448-454 / :635-641)
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  OuterCtl c = *h->h_ctl;
+  if (!h->started[mode] && (!adj || popt > 0)) {
+    CK(launch_init_flux(P, h->st));
+    c.Ke = 1.0;
+    c.cur = 0;
+    h->started[mode] = true;
+  } else if (!h->started[0] && !h->started[1]) {
+    return fail(h, ADP_ERR_STATE, "adp_outer: no flux to start from (adjoint with popt <= 0 before any solve)");
+  }
+  c.p = 0;
+  c.status = 0;
+  c.converged = 0;
+  c.nodal_due = 0;
+  c.max_reached = 0;
+  c.need_prologue = 1;
+  c.err_node = -1;
+  c.bar_count = 0;
+  const int nod0 = c.nodal_updates;
+  const long outers0 = c.p_total;
+  *h->h_ctl = c;
+  CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
+  const int do_nodal = (h->o.kern != ADP_KERN_FDM) && (!adj || popt > 0);
+  P.do_nodal = do_nodal;
+  NodalParams NP = nodal_params(h, adj ? 0 : 1);
+  int blocks, threads;
+  launch_shape(h, blocks, threads);
+  h->tm.grid_blocks = blocks;
+  h->tm.block_threads = threads;
+  adp_status result = ADP_OK;
+  for (int guard = 0; guard < 4 * h->o.nout + 8; ++guard) {
+    CK(cudaMemsetAsync(&h->d_ctl->bar_count, 0, sizeof(unsigned), h->st));
+    CK(cudaEventRecord(h->e2, h->st));
+    CK(launch_outer(P, blocks, threads, h->st));
+    CK(cudaEventRecord(h->e3, h->st));
+    CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->e2, h->e3);
+    h->tm.outer_kernel_ms += ms;
+    h->tm.outer_kernel_launches += 1;
+    c = *h->h_ctl;
+    if (c.status) { result = ctl_error(h, c); break; }
+    if (c.converged) break;
+    if (c.max_reached) {
+      result = fail(h, ADP_ERR_MAXOUTER, "maximum number of outer iteration is reached");
+      break;
+    }
+    if (c.nodal_due) {
+      CK(cudaEventRecord(h->e2, h->st));
+      CK(launch_nodal(NP, h->st));
+      AssembleParams A0 = AP;
+      A0.with_coupling = 0;
+      CK(launch_assemble(A0, h->st));
+      CK(cudaEventRecord(h->e3, h->st));
+      CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      ms = 0.f;
+      cudaEventElapsedTime(&ms, h->e2, h->e3);
+      h->tm.nodal_ms += ms;
+      h->tm.nodal_updates += 1;
+      c = *h->h_ctl;
+      if (c.status) { result = ctl_error(h, c); break; }
+      if (c.converged) break;
+      if (c.max_reached) {
+        result = fail(h, ADP_ERR_MAXOUTER, "maximum number of outer iteration is reached");
+        break;
+      }
+    }
+  }
+  CK(cudaEventRecord(h->e1, h->st));
+  CK(cudaEventSynchronize(h->e1));
+  float total_ms = 0.f;
+  cudaEventElapsedTime(&total_ms, h->e0, h->e1);
+  h->tm.outers += c.p;
+  h->tm.bicg_rows += (long)c.p * h->ng * h->o.nin * (long)h->NB;
+  if (rep) {
+    rep->outers = c.p;
+    rep->converged = c.converged;
+    rep->nodal_updates = c.nodal_updates - nod0;
+    rep->keff = c.Ke;
+    rep->ser = c.ser;
+    rep->fer = c.fer;
+    rep->ndmax = c.ndmax;
+    rep->im = c.im;
+    rep->jm = c.jm;
+    rep->km = c.km;
+    rep->device_ms = total_ms;
+    int n = std::min(std::min(c.p, rep->trace_cap), h->o.nout);
+    if (n > 0) {
+      if (rep->trace_k) CK(cudaMemcpy(rep->trace_k, h->d_tr_k, n * 8, cudaMemcpyDeviceToHost));
+      if (rep->trace_ser) CK(cudaMemcpy(rep->trace_ser, h->d_tr_ser, n * 8, cudaMemcpyDeviceToHost));
+      if (rep->trace_fer) CK(cudaMemcpy(rep->trace_fer, h->d_tr_fer, n * 8, cudaMemcpyDeviceToHost));
+      if (rep->trace_flags) CK(cudaMemcpy(rep->trace_flags, h->d_tr_flags, n * 4, cudaMemcpyDeviceToHost));
+      if (rep->trace_ndmax) CK(cudaMemcpy(rep->trace_ndmax, h->d_tr_ndmax, n * 8, cudaMemcpyDeviceToHost));
+    }
+  }
+  (void)outers0;
+  return result;
+}
+
+adp_status adp_get_state(adp_handle* h, double* f0, double* fs0, double* keff, double* dn) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const int cur = h->h_ctl->cur, nn = h->nnod, G = h->ng, NB = h->NB;
+  if (keff) *keff = h->h_ctl->Ke;
+  std::vector<double> box;
+  if (f0) {
+    box.resize((size_t)G * h->NBH);
+    CK(cudaMemcpy(box.data(), h->d_phi[cur] - h->plane, box.size() * 8, cudaMemcpyDeviceToHost));
+    for (int g = 0; g < G; ++g)
+      for (int n = 0; n < nn; ++n) f0[(size_t)g * nn + n] = box[(size_t)g * h->NBH + h->plane + h->node2box[n]];
+  }
+  if (fs0) {
+    box.resize(NB);
+    CK(cudaMemcpy(box.data(), h->d_fs[cur], (size_t)NB * 8, cudaMemcpyDeviceToHost));
+    for (int n = 0; n < nn; ++n) fs0[n] = box[h->node2box[n]];
+  }
+  if (dn) {
+    box.resize((size_t)G * 6 * NB);
+    CK(cudaMemcpy(box.data(), h->d_dn, box.size() * 8, cudaMemcpyDeviceToHost));
+    // dn(nnod, ng, 6): face is the slowest index
+    for (int u = 0; u < 6; ++u)
+      for (int g = 0; g < G; ++g)
+        for (int n = 0; n < nn; ++n)
+          dn[((size_t)u * G + g) * nn + n] = box[((size_t)g * 6 + u) * NB + h->node2box[n]];
+  }
+  return ADP_OK;
+}
+
+adp_status adp_set_state(adp_handle* h, const double* f0, const double* fs0, const double* keff, const double* dn) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const int cur = h->h_ctl->cur, nn = h->nnod, G = h->ng, NB = h->NB;
+  std::vector<double> box;
+  if (f0) {
+    box.assign((size_t)G * h->NBH, 0.0);
+    for (int g = 0; g < G; ++g)
+      for (int n = 0; n < nn; ++n) box[(size_t)g * h->NBH + h->plane + h->node2box[n]] = f0[(size_t)g * nn + n];
+    CK(cudaMemcpy(h->d_phi[cur] - h->plane, box.data(), box.size() * 8, cudaMemcpyHostToDevice));
+  }
+  if (fs0) {
+    box.assign(NB, 0.0);
+    for (int n = 0; n < nn; ++n) box[h->node2box[n]] = fs0[n];
+    CK(cudaMemcpy(h->d_fs[cur], box.data(), (size_t)NB * 8, cudaMemcpyHostToDevice));
+  }
+  if (dn) {
+    box.assign((size_t)G * 6 * NB, 0.0);
+    for (int u = 0; u < 6; ++u)
+      for (int g = 0; g < G; ++g)
+        for (int n = 0; n < nn; ++n)
+          box[((size_t)g * 6 + u) * NB + h->node2box[n]] = dn[((size_t)u * G + g) * nn + n];
+    CK(cudaMemcpy(h->d_dn, box.data(), box.size() * 8, cudaMemcpyHostToDevice));
+  }
+  if (keff) {
+    h->h_ctl->Ke = *keff;
+    CK(cudaMemcpy(&h->d_ctl->Ke, &h->h_ctl->Ke, sizeof(double), cudaMemcpyHostToDevice));
+  }
+  h->started[0] = h->started[1] = true;
+  return ADP_OK;
+}
+
+adp_status adp_power(adp_handle* h, double* p) {
+  if (!h || !p) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  OuterCtl c = *h->h_ctl;
+  c.status = 0;
+  *h->h_ctl = c;
+  CK(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CK(launch_power(box_geom(h), h->ng, h->NBH, h->d_phi[c.cur], h->d_sigf, h->d_pbox, h->d_red, h->d_ctl, h->st));
+  std::vector<double> box(h->NB);
+  CK(cudaMemcpyAsync(box.data(), h->d_pbox, (size_t)h->NB * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (h->h_ctl->status) return ctl_error(h, *h->h_ctl);
+  for (int n = 0; n < h->nnod; ++n) p[n] = box[h->node2box[n]];
+  return ADP_OK;
+}
+
+adp_status adp_get_timers(const adp_handle* h, adp_timers* t) {
+  if (!h || !t) return ADP_ERR_INPUT;
+  *t = h->tm;
+  return ADP_OK;
+}
+
+}  // extern "C"

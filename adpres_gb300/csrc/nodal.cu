@@ -1,0 +1,654 @@
+// Two-node nonlinear nodal update (SANM and PNM kernels), mod_nodal.f90.
+//
+// The reference sweeps x, y and z lines sequentially (mod_nodal.f90:53-125),
+// but every new coupling coefficient dn depends only on per-node quantities
+// of the two nodes of its interface, all computed from the transverse
+// leakages S1..S3 that get_source builds once from the old dn before the
+// sweeps (:49, :1009-1043).  The update is therefore split into
+//   k_tl_source : get_source / Lxyz               (per node)
+//   k_node_prep : get_B, get_a2matvec, LU_solve, get_a4, TLUpd1/TLUpd2
+//                 -> a2, a4 and the first moment L1 (per node and direction)
+//   k_interface : get_a1matvec[_first|_last], LU_solve, get_a3,
+//                 nodal_coup_upd -> new dn, and the ndmax candidates
+//                 (per node and direction: its minus face, plus the line's
+//                 last face)
+//   k_nodal_finish : ndmax with the sweep's first-maximum tie rule, the
+//                 divergence check and the convergence test of the outer.
+// The SANM constants (get_ABEFGH, :1409-1451) depend only on the cross
+// sections and node sizes and are computed once per cross-section set.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "adp_kernels.h"
+
+namespace adp {
+
+// PNM constants (mod_nodal.f90:180-181)
+__device__ __forceinline__ void pnm_consts(double* c) {
+  c[0] = 1.0 / 15.0;
+  c[1] = 1.0 / 35.0;
+  c[2] = 2.0 / 7.0;
+  c[3] = 2.0 / 5.0;
+  c[4] = 10.0;
+  c[5] = 6.0;
+}
+
+// get_ABEFGH (mod_nodal.f90:1409-1451), stored as sanm[u][k][g][b], k = A,B,E,F,G,H
+__global__ void k_sanm_consts(NodalParams P) {
+  const int NB = P.G.NB, ng = P.ng;
+  const int total = P.nnod * 3 * ng;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    const int n = q % P.nnod, ug = q / P.nnod, u = ug % 3, g = ug / 3;
+    const int b = P.act[n];
+    const double dn = hdir(P.G, u, b);
+    const double alp = 0.5 * sqrt(P.sigr[(size_t)g * NB + b] / P.D[(size_t)g * NB + b]) * dn;
+    const double alp2 = alp * alp;
+    const double sh = sinh(alp), ch = cosh(alp);
+    const double m0c = sh / alp;
+    const double m1s = 3.0 * (ch / alp - sh / alp2);
+    const double m2c = 5.0 * (sh / alp - 3.0 * ch / alp2 + 3.0 * sh / (alp * alp * alp));
+    double* out = (double*)P.sanm + ((size_t)u * 6 * ng + g) * NB + b;
+    const size_t st = (size_t)ng * NB;
+    out[0 * st] = (sh - m1s) / (alp2 * m1s);
+    out[1 * st] = (ch - m0c - m2c) / (alp2 * m2c);
+    out[2 * st] = (m0c / m2c - 3.0 / alp2);
+    out[3 * st] = (alp * ch - m1s) / (alp2 * m1s);
+    out[4 * st] = (alp * sh - 3.0 * m2c) / (ch - m0c - m2c);
+    out[5 * st] = (alp * ch - m1s) / (sh - m1s);
+  }
+}
+
+cudaError_t launch_sanm_consts(const NodalParams& P, cudaStream_t st) {
+  int total = P.nnod * 3 * P.ng;
+  int blocks = (total + 255) / 256;
+  if (blocks > 8192) blocks = 8192;
+  k_sanm_consts<<<blocks, 256, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ const double* latest_phi(const NodalParams& P) { return P.phi[P.ctl->cur]; }
+
+// ---------------------------------------------------------------------------
+// get_source / Lxyz (mod_nodal.f90:901-1043)
+// ---------------------------------------------------------------------------
+__global__ void k_tl_source(NodalParams P) {
+  const BoxGeom& G = P.G;
+  const int NB = G.NB, ng = P.ng;
+  const double* phi = latest_phi(P);
+  const int total = P.nnod * ng;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    const int n = q % P.nnod, g = q / P.nnod;
+    const int b = P.act[n];
+    const unsigned m = G.nbm[b];
+    const double* F = phi + (size_t)g * P.NBH;
+    const double* df = P.df + (size_t)g * 6 * NB;
+    const double* dn = P.dn + (size_t)g * 6 * NB;
+    const double fn = F[b];
+    double L[3];
+    for (int u = 0; u < 3; ++u) {
+      const int fp = 2 * u, fm = 2 * u + 1;
+      const double dfp = df[(size_t)fp * NB + b], dnp = dn[(size_t)fp * NB + b];
+      const double dfm = df[(size_t)fm * NB + b], dnm = dn[(size_t)fm * NB + b];
+      double jp, jm;
+      if (!(m & (1u << fp))) {
+        jp = (G.bcf[fp] == 2) ? 0.0 : dfp * fn - dnp * fn;
+      } else {
+        const double fpv = F[b + face_off(G, fp)];
+        jp = -dfp * (fpv - fn) - dnp * (fpv + fn);
+      }
+      if (!(m & (1u << fm))) {
+        jm = (G.bcf[fm] == 2) ? 0.0 : -dfm * fn - dnm * fn;
+      } else {
+        const double fmv = F[b + face_off(G, fm)];
+        jm = -dfm * (fn - fmv) - dnm * (fn + fmv);
+      }
+      L[u] = (jp - jm) / hdir(G, u, b);
+    }
+    P.S[((size_t)0 * ng + g) * NB + b] = L[1] + L[2];
+    P.S[((size_t)1 * ng + g) * NB + b] = L[0] + L[2];
+    P.S[((size_t)2 * ng + g) * NB + b] = L[0] + L[1];
+  }
+}
+
+// Line position of a node along direction u.
+struct LinePos {
+  bool first, last, refl_first, refl_last;
+  int offp;        // box offset of the plus neighbour
+};
+
+__device__ __forceinline__ LinePos line_pos(const BoxGeom& G, int u, int b) {
+  const unsigned m = G.nbm[b];
+  LinePos L;
+  L.first = !(m & (1u << (2 * u + 1)));
+  L.last = !(m & (1u << (2 * u)));
+  L.refl_first = G.bcf[2 * u + 1] == 2;
+  L.refl_last = G.bcf[2 * u] == 2;
+  L.offp = face_off(G, 2 * u);
+  return L;
+}
+
+// TLUpd1 (mod_nodal.f90:1047-1199): first moment of the transverse leakage.
+__device__ double tlupd1(const NodalParams& P, int u, int b, int g) {
+  const BoxGeom& G = P.G;
+  const LinePos L = line_pos(G, u, b);
+  const double* S = P.S + ((size_t)u * P.ng + g) * G.NB;
+  const double h0 = hdir(G, u, b);
+  double Lm, tm, tp, p1m, p2m, p1p, p2p, hp;
+  if (L.first) {
+    const double hpv = hdir(G, u, b + L.offp);
+    if (L.refl_first) {
+      tm = 1.0;
+      tp = hpv / h0;
+      p1m = tm + 1.0;
+      p2m = 2.0 * tm + 1.0;
+      p1p = tp + 1.0;
+      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+      Lm = (p1m * p2m * (S[b + L.offp] - S[b])) / hp;
+    } else {
+      tp = hpv / h0;
+      p1p = tp + 1.0;
+      Lm = (S[b + L.offp] - S[b]) / p1p;
+    }
+  } else if (L.last) {
+    const double hmv = hdir(G, u, b - L.offp);
+    if (L.refl_last) {
+      tm = hmv / h0;
+      tp = 1.0;
+      p1m = tm + 1.0;
+      p1p = tp + 1.0;
+      p2p = 2.0 * tp + 1.0;
+      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+      Lm = (p1p * p2p * (S[b] - S[b - L.offp])) / hp;
+    } else {
+      tm = hmv / h0;
+      p1m = tm + 1.0;
+      Lm = (S[b] - S[b - L.offp]) / p1m;
+    }
+  } else {
+    tm = hdir(G, u, b - L.offp) / h0;
+    tp = hdir(G, u, b + L.offp) / h0;
+    p1m = tm + 1.0;
+    p2m = 2.0 * tm + 1.0;
+    p1p = tp + 1.0;
+    p2p = 2.0 * tp + 1.0;
+    hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+    Lm = (p1m * p2m * (S[b + L.offp] - S[b]) + p1p * p2p * (S[b] - S[b - L.offp])) / hp;
+  }
+  return 0.25 * (h0 * h0) / P.D[(size_t)g * G.NB + b] * Lm;
+}
+
+// TLUpd2 (mod_nodal.f90:1203-1341): second moment of the transverse leakage.
+__device__ double tlupd2(const NodalParams& P, int u, int b, int g) {
+  const BoxGeom& G = P.G;
+  const LinePos L = line_pos(G, u, b);
+  const double* S = P.S + ((size_t)u * P.ng + g) * G.NB;
+  const double h0 = hdir(G, u, b);
+  double Lm, tm, tp, p1m, p1p, hp;
+  if (L.first) {
+    if (L.refl_first) {
+      tm = 1.0;
+      tp = hdir(G, u, b + L.offp) / h0;
+      p1m = tm + 1.0;
+      p1p = tp + 1.0;
+      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+      Lm = (p1m * (S[b + L.offp] - S[b])) / hp;
+    } else {
+      Lm = 0.0;
+    }
+  } else if (L.last) {
+    if (L.refl_last) {
+      tm = hdir(G, u, b - L.offp) / h0;
+      tp = 1.0;
+      p1m = tm + 1.0;
+      p1p = tp + 1.0;
+      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+      Lm = (p1p * (S[b - L.offp] - S[b])) / hp;
+    } else {
+      Lm = 0.0;
+    }
+  } else {
+    tm = hdir(G, u, b - L.offp) / h0;
+    tp = hdir(G, u, b + L.offp) / h0;
+    p1m = tm + 1.0;
+    p1p = tp + 1.0;
+    hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+    Lm = (p1m * (S[b + L.offp] - S[b]) + p1p * (S[b - L.offp] - S[b])) / hp;
+  }
+  return 0.25 * (h0 * h0) / P.D[(size_t)g * G.NB + b] * Lm;
+}
+
+// get_B (mod_nodal.f90:1345-1405): buckling matrix of node b in direction u.
+// cmode 1 forward, 0 adjoint (transposed group coupling).
+template <int NG>
+__device__ __forceinline__ void get_B(const NodalParams& P, int u, int b, double Ke, double (&B)[NG][NG]) {
+  const int NB = P.G.NB;
+  const double dn = hdir(P.G, u, b);
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    const double fac = 0.25 * (dn * dn) / P.D[(size_t)g * NB + b];
+#pragma unroll
+    for (int h = 0; h < NG; ++h) {
+      double dum;
+      if (g == h) {
+        dum = P.sigr[(size_t)g * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] / Ke;
+      } else if (P.cmode == 1) {
+        dum = -P.sigs[((size_t)h * NG + g) * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] / Ke;
+      } else {
+        dum = -P.sigs[((size_t)g * NG + h) * NB + b] - P.chin[(size_t)h * NB + b] * P.nuf[(size_t)g * NB + b] / Ke;
+      }
+      B[g][h] = fac * dum;
+    }
+  }
+}
+
+// Constants A,B,E,F,G,H of node b in direction u.
+template <int NG>
+__device__ __forceinline__ void get_consts(const NodalParams& P, int u, int b, double (&K)[6][NG]) {
+  if (P.pnm) {
+    double c[6];
+    pnm_consts(c);
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int g = 0; g < NG; ++g) K[k][g] = c[k];
+    return;
+  }
+  const size_t st = (size_t)NG * P.G.NB;
+  const double* src = P.sanm + (size_t)u * 6 * st + b;
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int g = 0; g < NG; ++g) K[k][g] = src[k * st + (size_t)g * P.G.NB];
+}
+
+// LU_solve (mod_nodal.f90:829-897): Doolittle elimination without pivoting,
+// L stored in place of the eliminated entries.  Returns false when an input
+// diagonal is below the reference's 10e-5 (single precision) threshold.
+template <int M>
+__device__ __forceinline__ bool lu_solve(double (&U)[M][M], double (&x)[M]) {
+#pragma unroll
+  for (int i = 0; i < M; ++i)
+    if (fabs(U[i][i]) < kF1em4) return false;
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+#pragma unroll
+    for (int j = i + 1; j < M; ++j) {
+      const double piv = U[j][i] / U[i][i];
+#pragma unroll
+      for (int k = i + 1; k < M; ++k) U[j][k] = U[j][k] - piv * U[i][k];
+      U[j][i] = piv;
+    }
+  }
+  // forward substitution (unit lower), x holds b on entry
+#pragma unroll
+  for (int i = 1; i < M; ++i) {
+    double isum = 0.0;
+#pragma unroll
+    for (int k = 0; k < i; ++k) isum = isum + U[i][k] * x[k];
+    x[i] = x[i] - isum;
+  }
+  x[M - 1] = x[M - 1] / U[M - 1][M - 1];
+#pragma unroll
+  for (int i = M - 2; i >= 0; --i) {
+    double isum = 0.0;
+#pragma unroll
+    for (int k = i + 1; k < M; ++k) isum = isum + U[i][k] * x[k];
+    x[i] = (x[i] - isum) / U[i][i];
+  }
+  return true;
+}
+
+__device__ __forceinline__ void record_error(OuterCtl* C, int code, int b) {
+  if (atomicCAS(&C->status, 0, code) == 0) C->err_node = b;
+}
+
+// ---------------------------------------------------------------------------
+// Per node and direction: a2 (get_a2matvec + LU_solve), a4 (get_a4) and the
+// first transverse-leakage moment (TLUpd1).
+// ---------------------------------------------------------------------------
+template <int NG>
+__global__ void k_node_prep(NodalParams P) {
+  const BoxGeom& G = P.G;
+  const int NB = G.NB;
+  const double* phi = latest_phi(P);
+  const double Ke = P.ctl->Ke;
+  const int total = P.nnod * 3;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    const int n = q % P.nnod, u = q / P.nnod;
+    const int b = P.act[n];
+    double Bc[NG][NG], K[6][NG];
+    get_B<NG>(P, u, b, Ke, Bc);
+    get_consts<NG>(P, u, b, K);
+    const double h = hdir(G, u, b);
+    double M[NG][NG], rhs[NG], Lm2[NG];
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const double Sv = 0.25 * (h * h) / P.D[(size_t)g * NB + b] * P.S[((size_t)u * NG + g) * NB + b];
+      double Bf = 0.0;
+#pragma unroll
+      for (int hh = 0; hh < NG; ++hh) {
+        M[g][hh] = (hh == g) ? Bc[g][hh] * K[2][g] + 3.0 : Bc[g][hh] * K[2][g];
+        Bf = Bf + Bc[g][hh] * phi[(size_t)hh * P.NBH + b];
+      }
+      Lm2[g] = tlupd2(P, u, b, g);
+      rhs[g] = Bf - K[2][g] * Lm2[g] + Sv;
+    }
+    if (!lu_solve<NG>(M, rhs)) {
+      record_error(P.ctl, ADP_ERR_PIVOT, b);
+      continue;
+    }
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      double Bf = 0.0;
+#pragma unroll
+      for (int hh = 0; hh < NG; ++hh) Bf = Bf + Bc[g][hh] * rhs[hh];
+      const size_t o = ((size_t)u * NG + g) * NB + b;
+      P.a2[o] = rhs[g];
+      P.a4[o] = K[1][g] * (Bf + Lm2[g]);
+      P.L1[o] = tlupd1(P, u, b, g);
+    }
+  }
+}
+
+// Per-node data used on both sides of an interface.
+template <int NG>
+struct NodeSide {
+  double Bc[NG][NG];
+  double K[6][NG];   // A,B,E,F,G,H
+  double a2[NG], a4[NG], L1[NG], f[NG], D[NG];
+  double h;
+};
+
+template <int NG>
+__device__ __forceinline__ void load_side(const NodalParams& P, int u, int b, double Ke, const double* phi,
+                                          NodeSide<NG>& S) {
+  const int NB = P.G.NB;
+  get_B<NG>(P, u, b, Ke, S.Bc);
+  get_consts<NG>(P, u, b, S.K);
+  S.h = hdir(P.G, u, b);
+#pragma unroll
+  for (int g = 0; g < NG; ++g) {
+    const size_t o = ((size_t)u * NG + g) * NB + b;
+    S.a2[g] = P.a2[o];
+    S.a4[g] = P.a4[o];
+    S.L1[g] = P.L1[o];
+    S.f[g] = phi[(size_t)g * P.NBH + b];
+    S.D[g] = P.D[(size_t)g * NB + b];
+  }
+}
+
+struct NdBest {
+  double val;
+  long long key;
+  int loc;
+};
+
+__device__ __forceinline__ void nd_consider(NdBest& best, double val, long long key, int loc) {
+  if (val > best.val || (val == best.val && key < best.key)) {
+    best.val = val;
+    best.key = key;
+    best.loc = loc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per node and direction: the minus face of the node (the interior
+// interface with its predecessor, or the first boundary face of the line),
+// plus the last boundary face when the node ends its line.
+// ---------------------------------------------------------------------------
+template <int NG>
+__global__ void k_interface(NodalParams P) {
+  const BoxGeom& G = P.G;
+  const int NB = G.NB;
+  const double* phi = latest_phi(P);
+  const double Ke = P.ctl->Ke;
+  NdBest best{0.0, 0x7fffffffffffffffLL, -1};
+  const int total = P.nnod * 3;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    const int n = q % P.nnod, u = q / P.nnod;
+    const int b = P.act[n];
+    const LinePos L = line_pos(G, u, b);
+    const int sf = 2 * u;         // plus face of u (X+, Y+, Z+); sf+1 is the minus face
+    const long long ev = P.evbase[(size_t)u * NB + b];
+    NodeSide<NG> Sp;
+    load_side<NG>(P, u, b, Ke, phi, Sp);
+    if (!L.first) {
+      // interior interface n = predecessor, p = b (get_coefs + get_a1matvec)
+      const int bn = b - L.offp;
+      NodeSide<NG> Sn;
+      load_side<NG>(P, u, bn, Ke, phi, Sn);
+      double R[2 * NG][2 * NG], x[2 * NG];
+      double Pn[NG], Pp[NG];
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        Pn[g] = 2.0 * Sn.D[g] / Sn.h;
+        Pp[g] = 2.0 * Sp.D[g] / Sp.h;
+#pragma unroll
+        for (int hh = 0; hh < NG; ++hh) {
+          if (hh == g) {
+            R[g][g] = -Pn[g] * (Sn.Bc[g][hh] * Sn.K[3][g] + 1.0);
+            R[g][g + NG] = Pp[g] * (Sp.Bc[g][hh] * Sp.K[3][g] + 1.0);
+          } else {
+            R[g][hh] = -Pn[g] * Sn.Bc[g][hh] * Sn.K[3][g];
+            R[g][hh + NG] = Pp[g] * Sp.Bc[g][hh] * Sp.K[3][g];
+          }
+        }
+        x[g] = Pn[g] * (3.0 * Sn.a2[g] + Sn.K[4][g] * Sn.a4[g] + Sn.K[3][g] * Sn.L1[g]) +
+               Pp[g] * (3.0 * Sp.a2[g] + Sp.K[4][g] * Sp.a4[g] - Sp.K[3][g] * Sp.L1[g]);
+      }
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        const double dcn = P.dc[((size_t)g * 6 + sf) * NB + bn];
+        const double dcp = P.dc[((size_t)g * 6 + sf + 1) * NB + b];
+#pragma unroll
+        for (int hh = 0; hh < NG; ++hh) {
+          if (hh == g) {
+            R[g + NG][g] = dcn * (Sn.Bc[g][hh] * Sn.K[0][g] + 1.0);
+            R[g + NG][g + NG] = dcp * (Sp.Bc[g][hh] * Sp.K[0][g] + 1.0);
+          } else {
+            R[g + NG][hh] = dcn * Sn.Bc[g][hh] * Sn.K[0][g];
+            R[g + NG][hh + NG] = dcp * Sp.Bc[g][hh] * Sp.K[0][g];
+          }
+        }
+        // ADF pairing of mod_nodal.f90:693-694 kept as written there
+        x[g + NG] = dcp * (Sp.a2[g] + Sp.a4[g] + Sp.f[g] - Sn.K[0][g] * Sn.L1[g]) -
+                    dcn * (Sn.a2[g] + Sn.a4[g] + Sn.f[g] + Sp.K[0][g] * Sp.L1[g]);
+      }
+      if (!lu_solve<2 * NG>(R, x)) {
+        record_error(P.ctl, ADP_ERR_PIVOT, bn);
+      } else {
+        double a3[NG];
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          double Bf = 0.0;
+#pragma unroll
+          for (int hh = 0; hh < NG; ++hh) Bf = Bf + Sn.Bc[g][hh] * x[hh];
+          a3[g] = Sn.K[0][g] * (Bf + Sn.L1[g]);
+        }
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          const double jp = -2.0 * Sn.D[g] / Sn.h *
+                            (x[g] + 3.0 * Sn.a2[g] + Sn.K[5][g] * a3[g] + Sn.K[4][g] * Sn.a4[g]);
+          const size_t on = ((size_t)g * 6 + sf) * NB + bn;
+          const double ndpr = P.dn[on];
+          const double dnew = (P.df[on] * (Sn.f[g] - Sp.f[g]) - jp) / (Sn.f[g] + Sp.f[g]);
+          P.dn[on] = dnew;
+          P.dn[((size_t)g * 6 + sf + 1) * NB + b] = dnew;
+          nd_consider(best, fabs(dnew - ndpr), ev * NG + g, bn);
+        }
+      }
+    } else {
+      // first boundary face of the line (get_coefs_first + get_a1matvec_first)
+      const int bc = G.bcf[sf + 1];
+      double A[NG][NG], x[NG];
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        const double Pp = 2.0 * Sp.D[g] / Sp.h;
+        const double dcv = P.dc[((size_t)g * 6 + sf + 1) * NB + b];
+        const double Ap = Sp.K[0][g], Fp = Sp.K[3][g], Gp = Sp.K[4][g], Hp = Sp.K[5][g];
+        const double a2 = Sp.a2[g], a4 = Sp.a4[g], L1 = Sp.L1[g], fv = Sp.f[g];
+#pragma unroll
+        for (int hh = 0; hh < NG; ++hh) {
+          const double Bc = Sp.Bc[g][hh];
+          if (bc == 2) A[g][hh] = (hh == g) ? Pp * (Bc * Fp + 1.0) : Pp * Bc * Fp;
+          else if (bc == 1)
+            A[g][hh] = (hh == g) ? -dcv * (1.0 + Ap * Bc) - 2.0 * Pp * (Ap * Bc * Hp + 1.0)
+                                 : -dcv * Ap * Bc - 2.0 * Pp * Ap * Bc * Hp;
+          else A[g][hh] = (hh == g) ? dcv * (1.0 + Ap * Bc) : dcv * Ap * Bc;
+        }
+        if (bc == 2) x[g] = Pp * (3.0 * a2 + Gp * a4 - Fp * L1);
+        else if (bc == 1) x[g] = 2.0 * Pp * (Ap * Hp * L1 - 3.0 * a2 - Gp * a4) - dcv * (a2 + a4 + fv - Ap * L1);
+        else x[g] = dcv * (a2 + a4 + fv - Ap * L1);
+      }
+      if (!lu_solve<NG>(A, x)) {
+        record_error(P.ctl, ADP_ERR_PIVOT, b);
+      } else {
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          double Bf = 0.0;
+#pragma unroll
+          for (int hh = 0; hh < NG; ++hh) Bf = Bf + Sp.Bc[g][hh] * x[hh];
+          const double a3 = Sp.K[0][g] * (Bf + Sp.L1[g]);
+          const double jp = -2.0 * Sp.D[g] / Sp.h * (x[g] - 3.0 * Sp.a2[g] + Sp.K[5][g] * a3 - Sp.K[4][g] * Sp.a4[g]);
+          const size_t op = ((size_t)g * 6 + sf + 1) * NB + b;
+          const double ndpr = P.dn[op];
+          const double dnew = -(jp / Sp.f[g] + P.df[op]);
+          P.dn[op] = dnew;
+          nd_consider(best, fabs(dnew - ndpr), ev * NG + g, b);
+        }
+      }
+    }
+    if (L.last) {
+      // last boundary face of the line (get_coefs_last + get_a1matvec_last)
+      const int bc = G.bcf[sf];
+      double A[NG][NG], x[NG];
+#pragma unroll
+      for (int g = 0; g < NG; ++g) {
+        const double Pn = 2.0 * Sp.D[g] / Sp.h;
+        const double dcv = P.dc[((size_t)g * 6 + sf) * NB + b];
+        const double An = Sp.K[0][g], Fn = Sp.K[3][g], Gn = Sp.K[4][g], Hn = Sp.K[5][g];
+        const double a2 = Sp.a2[g], a4 = Sp.a4[g], L1 = Sp.L1[g], fv = Sp.f[g];
+#pragma unroll
+        for (int hh = 0; hh < NG; ++hh) {
+          const double Bc = Sp.Bc[g][hh];
+          if (bc == 2) A[g][hh] = (hh == g) ? -Pn * (Bc * Fn + 1.0) : -Pn * Bc * Fn;
+          else if (bc == 1)
+            A[g][hh] = (hh == g) ? dcv * (1.0 + An * Bc) + 2.0 * Pn * (An * Bc * Hn + 1.0)
+                                 : dcv * An * Bc + 2.0 * Pn * An * Bc * Hn;
+          else A[g][hh] = (hh == g) ? dcv * (1.0 + An * Bc) : dcv * An * Bc;
+        }
+        if (bc == 2) x[g] = Pn * (3.0 * a2 + Gn * a4 + Fn * L1);
+        else if (bc == 1) x[g] = -2.0 * Pn * (An * Hn * L1 + 3.0 * a2 + Gn * a4) - dcv * (a2 + a4 + fv + An * L1);
+        else x[g] = -dcv * (a2 + a4 + fv + An * L1);
+      }
+      if (!lu_solve<NG>(A, x)) {
+        record_error(P.ctl, ADP_ERR_PIVOT, b);
+      } else {
+#pragma unroll
+        for (int g = 0; g < NG; ++g) {
+          double Bf = 0.0;
+#pragma unroll
+          for (int hh = 0; hh < NG; ++hh) Bf = Bf + Sp.Bc[g][hh] * x[hh];
+          const double a3 = Sp.K[0][g] * (Bf + Sp.L1[g]);
+          const double jp = -2.0 * Sp.D[g] / Sp.h * (x[g] + 3.0 * Sp.a2[g] + Sp.K[5][g] * a3 + Sp.K[4][g] * Sp.a4[g]);
+          const size_t on = ((size_t)g * 6 + sf) * NB + b;
+          const double ndpr = P.dn[on];
+          const double dnew = -(jp / Sp.f[g] - P.df[on]);
+          P.dn[on] = dnew;
+          nd_consider(best, fabs(dnew - ndpr), (ev + 1) * NG + g, b);
+        }
+      }
+    }
+  }
+  // block reduction of (value, key, location)
+  __shared__ double sv[32];
+  __shared__ long long sk[32];
+  __shared__ int sl[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    NdBest other;
+    other.val = __shfl_xor_sync(0xffffffffu, best.val, o);
+    other.key = __shfl_xor_sync(0xffffffffu, best.key, o);
+    other.loc = __shfl_xor_sync(0xffffffffu, best.loc, o);
+    nd_consider(best, other.val, other.key, other.loc);
+  }
+  if (lane == 0) {
+    sv[w] = best.val;
+    sk[w] = best.key;
+    sl[w] = best.loc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    NdBest bb{sv[0], sk[0], sl[0]};
+    for (int k = 1; k < nw; ++k) nd_consider(bb, sv[k], sk[k], sl[k]);
+    P.nd_val[blockIdx.x] = bb.val;
+    P.nd_key[blockIdx.x] = bb.key;
+    P.nd_loc[blockIdx.x] = bb.loc;
+  }
+}
+
+// ndmax with its location, the divergence check (mod_nodal.f90:131-142) and
+// the convergence test of the outer that triggered the update
+// (mod_cmfd.f90:495-505).
+__global__ void k_nodal_finish(NodalParams P) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  OuterCtl* C = P.ctl;
+  NdBest bb{0.0, 0x7fffffffffffffffLL, -1};
+  for (int k = 0; k < P.nd_blocks; ++k) nd_consider(bb, P.nd_val[k], P.nd_key[k], P.nd_loc[k]);
+  C->ndmax = bb.val;
+  if (bb.val > 0.0 && bb.loc >= 0) {
+    const int b = bb.loc;
+    C->im = b % P.G.nxx + 1;
+    C->jm = (b / P.G.nxx) % P.G.nyy + 1;
+    C->km = b / P.G.plane + 1;
+  }
+  C->nodal_updates += 1;
+  C->nodal_due = 0;
+  const int q = C->p - 1;
+  if (q >= 0 && q < P.nout) {
+    P.tr_ndmax[q] = bb.val;
+    P.tr_flags[q] |= 2;
+  }
+  if (bb.val > 1.e3) {
+    if (C->status == 0) C->status = ADP_ERR_DIVERGED;
+    return;
+  }
+  const bool conv = C->ser < P.serc && C->fer < P.ferc && bb.val < kF1em2;
+  C->converged = conv ? 1 : 0;
+  C->max_reached = (!conv && C->p >= P.nout) ? 1 : 0;
+}
+
+template <int NG>
+static cudaError_t nodal_ng(const NodalParams& P, cudaStream_t st) {
+  const int total = P.nnod * 3;
+  int blocks1 = (P.nnod * NG + 255) / 256;
+  if (blocks1 > 8192) blocks1 = 8192;
+  k_tl_source<<<blocks1, 256, 0, st>>>(P);
+  int blocks2 = (total + 127) / 128;
+  if (blocks2 > 8192) blocks2 = 8192;
+  k_node_prep<NG><<<blocks2, 128, 0, st>>>(P);
+  NodalParams Q = P;
+  int blocks3 = (total + 127) / 128;
+  if (blocks3 > kMaxBlocks) blocks3 = kMaxBlocks;
+  Q.nd_blocks = blocks3;
+  k_interface<NG><<<blocks3, 128, 0, st>>>(Q);
+  k_nodal_finish<<<1, 32, 0, st>>>(Q);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st) {
+  switch (P.ng) {
+    case 1: return nodal_ng<1>(P, st);
+    case 2: return nodal_ng<2>(P, st);
+    case 3: return nodal_ng<3>(P, st);
+    case 4: return nodal_ng<4>(P, st);
+    case 5: return nodal_ng<5>(P, st);
+    case 6: return nodal_ng<6>(P, st);
+    case 7: return nodal_ng<7>(P, st);
+    case 8: return nodal_ng<8>(P, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace adp

@@ -1,0 +1,190 @@
+/*
+ * adpres_gb300.h -- C ABI of the GB300 (sm_103a) static k-eigenvalue solver.
+ *
+ * This ABI replaces ADPRES's module procedures `outer(popt)` and
+ * `outer_ad(popt)` (src/mod_cmfd.f90:415 and :602) together with the state
+ * they read and write through MODULE sdata (src/mod_data.f90), `PowDis`
+ * (src/mod_cmfd.f90:1290) and the static part of `XS_updt`
+ * (src/mod_xsec.f90:11-46).  The reference has no FFI of its own: its seam
+ * is those procedures plus the sdata globals, so every entry point below
+ * names the routine or globals it stands in for.
+ *
+ * Conventions
+ *  - Plain C types only; host pointers are borrowed for the duration of the
+ *    call and copied to or from device memory owned by the handle.
+ *  - Arrays use the reference's Fortran column-major layouts with the node
+ *    index fastest: f0(nnod,ng), dn(nnod,ng,6), sigs(nnod,ng,ng) with
+ *    sigs(n,g,h) the g -> h scattering, dc(nnod,ng,6), chi(nmat,ng).
+ *    Face order of df/dn/dc is X+, X-, Y+, Y-, Z+, Z- (mod_data.f90:59-60).
+ *  - Node indices ix/iy/iz and material numbers mat are 1-based, in the
+ *    reference node order (mod_io.f90:1317-1330).
+ *  - Every call returns an adp_status; 0 is success.  Where the reference
+ *    STOPs the process, the ABI returns a status and the handle stays usable
+ *    (its solver state after an error is unspecified).
+ *  - A handle is not thread-safe; calls on one handle must be serialised.
+ *    Each handle owns one CUDA stream on the device current at adp_create.
+ */
+#ifndef ADPRES_GB300_H
+#define ADPRES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum adp_status {
+  ADP_OK = 0,
+  ADP_ERR_INPUT = 1,        /* invalid geometry, options or arguments          */
+  ADP_ERR_BADXS = 2,        /* check_xs / Dsigr_updt failures (mod_xsec.f90:90-226) */
+  ADP_ERR_PIVOT = 3,        /* LU diagonal below 1e-4 (mod_nodal.f90:856-862)  */
+  ADP_ERR_DIVERGED = 4,     /* nodal ndmax > 1e3 (mod_nodal.f90:131-142)       */
+  ADP_ERR_MAXOUTER = 5,     /* nout outers without convergence (mod_cmfd.f90:498-505) */
+  ADP_ERR_ZEROPOWER = 6,    /* total power <= 0 (mod_cmfd.f90:1322-1326)       */
+  ADP_ERR_UNSUPPORTED = 7,  /* outside the static k-eigenvalue path           */
+  ADP_ERR_CUDA = 8,         /* a CUDA runtime call failed                      */
+  ADP_ERR_NAN = 9,          /* non-finite eigenvalue or fission source         */
+  ADP_ERR_BREAKDOWN = 10,   /* BiCGSTAB rho, (rs,v) or (t,t) exactly zero      */
+  ADP_ERR_TIMEOUT = 11,     /* a device-side wait ran out of its time limit   */
+  ADP_ERR_STATE = 12        /* call made in the wrong order                    */
+} adp_status;
+
+typedef enum adp_mode { ADP_FORWARD = 0, ADP_ADJOINT = 1 } adp_mode;
+typedef enum adp_kern { ADP_KERN_FDM = 0, ADP_KERN_PNM = 1, ADP_KERN_SANM = 2 } adp_kern;
+typedef enum adp_precision { ADP_FP64 = 0, ADP_MIXED = 1 } adp_precision;
+
+typedef struct adp_handle adp_handle;
+
+/* Geometry: the sdata globals nxx, nyy, nzz, nnod, ix, iy, iz, xdel, ydel,
+ * zdel and the boundary conditions xeast..ztop (mod_data.f90:35-43).  The
+ * ragged outline (ystag/xstag) is derived from the plane iz == 1 exactly as
+ * mod_io.f90:1071-1110 derives it. */
+typedef struct adp_geom {
+  int nxx, nyy, nzz;
+  int nnod;
+  const int* ix;            /* [nnod], 1-based */
+  const int* iy;            /* [nnod], 1-based */
+  const int* iz;            /* [nnod], 1-based */
+  const double* xdel;       /* [nxx] */
+  const double* ydel;       /* [nyy] */
+  const double* zdel;       /* [nzz] */
+  int east, west, north, south, bottom, top;   /* 0 zero flux, 1 zero incoming current, 2 reflective */
+} adp_geom;
+
+/* Iteration control (%ITER, mod_data.f90:78-86; %KERN, mod_data.f90:200). */
+typedef struct adp_opts {
+  int ng;                   /* energy groups                                   */
+  int nin;                  /* BiCGSTAB iterations per group solve (default 2) */
+  int nout;                 /* maximum outer iterations (default 500)          */
+  int nac;                  /* fission-source extrapolation interval (5)       */
+  int nupd;                 /* nodal update interval; <= 0 selects
+                               ceiling((nxx+nyy+nzz)/2.5) (mod_io.f90:1363)    */
+  double serc;              /* fission-source criterion; <= 0 selects the
+                               reference default (double)1.e-5f               */
+  double ferc;              /* flux criterion; <= 0 selects (double)1.e-5f     */
+  int kern;                 /* adp_kern                                        */
+  int precision;            /* adp_precision                                   */
+} adp_opts;
+
+/* Outcome of one adp_outer call.  The trace arrays are optional (NULL or
+ * trace_cap == 0); when given, entry t holds outer t+1 of this call, i.e. the
+ * values ADPRES prints per outer (mod_cmfd.f90:492). */
+typedef struct adp_report {
+  int outers;               /* outer iterations performed by this call         */
+  int converged;            /* 1 when ser<serc, fer<ferc and ndmax<1e-2        */
+  int nodal_updates;
+  double keff, ser, fer, ndmax;
+  int im, jm, km;           /* node of the last ndmax (mod_nodal.f90:333-337)  */
+  int trace_cap;
+  double* trace_k;
+  double* trace_ser;
+  double* trace_fer;
+  int* trace_flags;         /* bit 0: source extrapolated, bit 1: nodal update */
+  double* trace_ndmax;
+  double device_ms;         /* device time of the call (CUDA events)           */
+} adp_report;
+
+/* Device timers accumulated over the life of a handle (CUDA events on the
+ * handle's stream). */
+typedef struct adp_timers {
+  double outer_kernel_ms;   /* persistent CMFD kernel                          */
+  long outer_kernel_launches;
+  double nodal_ms;          /* nodal update kernels + matrix re-assembly       */
+  long nodal_updates;
+  double other_ms;
+  long outers;              /* outer iterations performed                      */
+  long bicg_rows;           /* BiCGSTAB row-iterations (rows x nin x groups x outers) */
+  int grid_blocks, block_threads;
+} adp_timers;
+
+/* -- handle life cycle ---------------------------------------------------- */
+
+/* Allocate the device state for one core (the allocations ADPRES makes on
+ * the first calls of outer/matrix_setup/coup_coef, mod_cmfd.f90:25-33,
+ * :232-241, :448-454). */
+adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** out);
+adp_status adp_destroy(adp_handle* h);
+
+/* Copy of the last error message of the handle (or of the last failed
+ * adp_create when h is NULL) into buf; returns the full message length. */
+size_t adp_last_error(const adp_handle* h, char* buf, size_t len);
+
+/* -- cross sections ------------------------------------------------------- */
+
+/* Node-wise cross sections as outer() reads them from sdata: D, sigr, nuf,
+ * sigf (nnod,ng), chi (nmat,ng) with mat (nnod), sigs (nnod,ng,ng) and the
+ * ADFs dc (nnod,ng,6; NULL means all 1, mod_io.f90:307-312).  Resets the
+ * nodal constants that depend on them. */
+adp_status adp_set_xs(adp_handle* h, int nmat, const double* D, const double* sigr, const double* nuf,
+                      const double* sigf, const double* chi, const int* mat, const double* sigs,
+                      const double* dc);
+
+/* XS_updt on the device (mod_xsec.f90:11-46, static path): node cross
+ * sections from the material tables through mat (base_updt :172-195), then
+ * D = 1/(3 sigtr) and sigr = siga + sum_{h/=g} sigs(g->h) (Dsigr_updt
+ * :199-226) and the checks of check_xs (:90-168).  Material tables are
+ * (nmat,ng) and (nmat,ng,ng). */
+adp_status adp_xs_updt(adp_handle* h, int nmat, const double* xsigtr, const double* xsiga, const double* xnuf,
+                       const double* xsigf, const double* chi, const int* mat, const double* xsigs,
+                       const double* dc);
+
+/* The same from node-wise tables (nnod,ng) and (nnod,ng,ng), for perturbed
+ * cores whose nodes no longer share material values. */
+adp_status adp_xs_updt_nodes(adp_handle* h, int nmat, const double* sigtr, const double* siga, const double* nuf,
+                             const double* sigf, const double* chi, const int* mat, const double* sigs,
+                             const double* dc);
+
+/* -- solver --------------------------------------------------------------- */
+
+/* One call of outer(popt) (mode ADP_FORWARD) or outer_ad(popt) (ADP_ADJOINT)
+ * on the state held by the handle: matrix_setup(1), the first-call start
+ * f0 = 1, k = 1 (mod_cmfd.f90:448-454, :635-641), then outer iterations with
+ * nin BiCGSTAB steps per group, fission-source extrapolation every nac
+ * outers, the SANM/PNM nodal update every nupd outers and the reference's
+ * convergence test.  popt only matters for the adjoint (mod_cmfd.f90:635,680). */
+adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* report);
+
+/* The in/out sdata state of outer(): f0(nnod,ng), fs0(nnod), Ke and
+ * nod%dn (nnod,ng,6).  Any pointer may be NULL.  adp_set_state marks the
+ * handle as started, so the next adp_outer warm-starts from it as ADPRES
+ * does when outer() is called again (mod_th.f90:774-795). */
+adp_status adp_get_state(adp_handle* h, double* f0, double* fs0, double* keff, double* dn);
+adp_status adp_set_state(adp_handle* h, const double* f0, const double* fs0, const double* keff,
+                         const double* dn);
+
+/* PowDis (mod_cmfd.f90:1290-1333): p(n) = sum_g max(0, f0 sigf vdel),
+ * normalised to sum 1.  p has nnod entries. */
+adp_status adp_power(adp_handle* h, double* p);
+
+/* Device timers of the handle. */
+adp_status adp_get_timers(const adp_handle* h, adp_timers* t);
+
+/* Launch shape of the persistent CMFD kernel: blocks (0 = automatic) and
+ * threads per block (0 = automatic).  Used by the autotuner. */
+adp_status adp_set_launch(adp_handle* h, int blocks, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ADPRES_GB300_H */

@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import platform
 import subprocess
 from dataclasses import dataclass
 
@@ -22,6 +23,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "adpres_oracle.cpp")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "libadpres_oracle.so")
+# Variant used only to measure how sensitive a deck is to rounding: the same
+# source with multiply-add contraction allowed (FMA on both x86-64 and Arm).
+LIB_FMA = os.path.join(BUILD_DIR, "libadpres_oracle_fma.so")
 
 # Status codes (same meaning as the product's adp_status values).
 ORA_OK = 0
@@ -34,27 +38,35 @@ ORA_ERR_ZEROPOWER = 6
 ORA_ERR_UNSUPPORTED = 7
 
 
-def build(force: bool = False) -> str:
-    """Compile the restatement with g++ (no FMA contraction) into _build/."""
+def build(force: bool = False, variant: str = "plain") -> str:
+    """Compile the restatement with g++ into _build/.
+
+    variant "plain" (the oracle): no multiply-add contraction, as the
+    reference's gfortran build for x86-64 has none.  variant "fma": the same
+    source with contraction, used only to measure rounding sensitivity.
+    """
     os.makedirs(BUILD_DIR, exist_ok=True)
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(SRC)):
-        return LIB
-    tmp = LIB + ".tmp.%d" % os.getpid()
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
-           "-fPIC", "-shared", SRC, "-o", tmp]
+    lib_path = LIB if variant == "plain" else LIB_FMA
+    if (not force and os.path.exists(lib_path)
+            and os.path.getmtime(lib_path) >= os.path.getmtime(SRC)):
+        return lib_path
+    tmp = lib_path + ".tmp.%d" % os.getpid()
+    if variant == "plain":
+        fp = ["-ffp-contract=off"]
+    else:
+        fp = ["-ffp-contract=fast"] + (["-mfma"] if platform.machine() in ("x86_64", "AMD64") else [])
+    cmd = ["g++", "-O2", "-std=c++17"] + fp + ["-fno-fast-math", "-fPIC", "-shared", SRC, "-o", tmp]
     subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = build()
+def lib(variant: str = "plain"):
+    if variant not in _libs:
+        path = build(variant=variant)
         L = ctypes.CDLL(path)
         vp, cp, ip, dp = ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
         ipp = ctypes.POINTER(ctypes.c_int)
@@ -87,8 +99,8 @@ def lib():
         L.ora_get_iarray.argtypes = [vp, cp, ipp]
         L.ora_get_trace.argtypes = [vp, ipp, dp, dp, dp, ipp, dp, ipp]
         L.ora_reset.argtypes = [vp]
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
 def _dp(a):
@@ -120,8 +132,9 @@ class TraceRow:
 class Oracle:
     """One reference-state instance (the equivalent of one ADPRES process)."""
 
-    def __init__(self, deck_path: str | None = None, text: str | None = None, basedir: str = "."):
-        L = lib()
+    def __init__(self, deck_path: str | None = None, text: str | None = None, basedir: str = ".",
+                 variant: str = "plain"):
+        L = lib(variant)
         if deck_path is not None:
             h = L.ora_load_deck(deck_path.encode())
         else:

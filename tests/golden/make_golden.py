@@ -96,6 +96,18 @@ def deck_fixture(path: str) -> dict:
         "out_trace_loc": np.array([r.loc for r in tr], dtype=np.int32).reshape(-1, 3),
     }
     inp.update(out)
+    # Rounding sensitivity of the reference algorithm on this deck: the same
+    # restatement built with multiply-add contraction, compared with itself.
+    q = oracle.Oracle(path, variant="fma")
+    q.run()
+    kq = np.array([r.k for r in q.trace()])
+    n = min(len(kq), len(out["out_trace_k"]))
+    inp["sens_outers"] = q.geti("outers")
+    inp["sens_trace_rel"] = float(np.max(np.abs(kq[:n] - out["out_trace_k"][:n]) / out["out_trace_k"][:n]))
+    inp["sens_k_pcm"] = abs(q.getd("Ke") - out["out_k"]) / out["out_k"] * 1e5
+    pw = out["out_power"]
+    m = pw > 0
+    inp["sens_power_rel"] = float(np.max(np.abs(q.powdis()[m] - pw[m]) / pw[m]))
     return inp
 
 
@@ -110,7 +122,8 @@ def main():
     for name in STATIC_DECKS:
         fx = deck_fixture(os.path.join(args.ref, "smpl", "static", name))
         np.savez_compressed(os.path.join(HERE, "decks", name + ".npz"), **fx)
-        print(name, fx["nnod"], fx["out_k"], fx["out_outers"])
+        print(name, fx["nnod"], fx["out_k"], fx["out_outers"], "sensitivity: outers", fx["sens_outers"],
+              "trace %.1e power %.1e" % (fx["sens_trace_rel"], fx["sens_power_rel"]))
 
 
 if __name__ == "__main__":
