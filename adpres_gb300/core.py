@@ -161,6 +161,10 @@ class Core:
         k = None if keff is None else ctypes.byref(ctypes.c_double(keff))
         self._check(self.L.adp_set_state(self.h, dptr(a), dptr(b), k, dptr(d)))
 
+    def reset(self):
+        """Back to the state of a fresh process (dn = 0; next outer starts from f0 = 1, k = 1)."""
+        self._check(self.L.adp_reset(self.h))
+
     def power(self):
         p = np.zeros(self.nnod)
         self._check(self.L.adp_power(self.h, dptr(p)))

@@ -106,35 +106,41 @@ __device__ __forceinline__ void set_status(OuterCtl* C, int code) {
   atomicCAS(&C->status, 0, code);
 }
 
-// Grid-wide barrier for a cooperative launch (all blocks co-resident).  The
-// wait is bounded: after kBarrierTimeoutNs the block records
-// ADP_ERR_TIMEOUT and returns false, so a fault elsewhere can never leave
-// the kernel spinning.  `gen` is the generation this block expects; every
-// block reads it at kernel start, before any block can arrive.
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).
+// One 32-bit word: block 0 adds 2^31 - (nblocks - 1), every other block
+// adds 1, so the top bit flips exactly when the last block arrives and the
+// low bits return to zero; each block waits until the top bit differs from
+// the value its own add returned.  The word must be 0 at launch.  The wait
+// is bounded: after kBarrierTimeoutNs the block records ADP_ERR_TIMEOUT and
+// returns false, so a fault elsewhere can never leave the kernel spinning.
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
-__device__ __forceinline__ bool grid_barrier(OuterCtl* C, unsigned nblocks, unsigned& gen) {
+__device__ __forceinline__ bool grid_barrier(OuterCtl* C, unsigned nblocks) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
+    const unsigned add = (blockIdx.x == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
     __threadfence();
-    unsigned arrived = atom_add_acqrel_gpu(&C->bar_count, 1u);
-    if (arrived == nblocks - 1) {
-      C->bar_count = 0;
-      st_release_gpu(&C->bar_gen, gen + 1);
+    const unsigned old = atomicAdd(&C->bar_count, add);
+    if (((old + add) ^ old) & 0x80000000u) {
+      // this block completed the barrier
     } else {
-      unsigned long long t0 = globaltimer_ns();
-      while (ld_acquire_gpu(&C->bar_gen) == gen) {
-        if (globaltimer_ns() - t0 > kBarrierTimeoutNs) {
-          set_status(C, ADP_ERR_TIMEOUT);
-          ok = 0;
-          break;
+      unsigned long long t0 = 0;
+      unsigned spins = 0;
+      while (!((ld_acquire_gpu(&C->bar_count) ^ old) & 0x80000000u)) {
+        if ((++spins & 63u) == 0) {
+          const unsigned long long t = globaltimer_ns();
+          if (t0 == 0) t0 = t;
+          else if (t - t0 > kBarrierTimeoutNs) {
+            set_status(C, ADP_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
         }
       }
     }
     __threadfence();
-    gen += 1;
     if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
     s_ok = ok;
   }

@@ -880,6 +880,27 @@ adp_status adp_set_state(adp_handle* h, const double* f0, const double* fs0, con
   return ADP_OK;
 }
 
+adp_status adp_reset(adp_handle* h) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  CK(cudaMemsetAsync(h->d_dn, 0, (size_t)h->ng * 6 * h->NB * sizeof(double), h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  OuterCtl c = *h->h_ctl;
+  c.Ke = 1.0;
+  c.ndmax = 0.0;
+  c.im = c.jm = c.km = 0;
+  c.cur = 0;
+  c.status = 0;
+  c.converged = c.nodal_due = c.max_reached = 0;
+  c.err_node = -1;
+  *h->h_ctl = c;
+  CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->started[0] = h->started[1] = false;
+  return ADP_OK;
+}
+
 adp_status adp_power(adp_handle* h, double* p) {
   if (!h || !p) return ADP_ERR_INPUT;
   CK(cudaSetDevice(h->dev));

@@ -137,8 +137,12 @@ cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
 // convergence test, all in the same order as mod_cmfd.f90:479-495.
 //
 // MIXED: P0 is computed in FP64 with the FP64 matrix (the defect of the
-// current flux); the nin Krylov steps for the correction run with FP32
-// matrix and vectors and FP64 dot products; x stays FP64.
+// current flux); the nin Krylov steps for the correction run with the FP32
+// matrix copy and FP32 vectors; each thread sums its rows' products in FP32
+// and the block and grid sums are FP64; the flux x stays FP64 and receives
+// FP32 increments.  Both forms avoid FP64 division in per-row work (the
+// source uses 1/k computed once per outer; RelE/RelEg divide only when a
+// candidate beats the running maximum).
 // ---------------------------------------------------------------------------
 template <bool MIXED>
 struct KV { using T = double; };
@@ -146,7 +150,7 @@ template <>
 struct KV<true> { using T = float; };
 
 template <bool MIXED>
-__global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
+__global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
   using T = typename KV<MIXED>::T;
   OuterCtl* C = P.ctl;
   const BoxGeom& G = P.G;
@@ -156,15 +160,10 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
   const unsigned nblk = gridDim.x;
   const long long NBH = P.NBH;
 
-  __shared__ unsigned s_gen;
   __shared__ int s_stop;
-  if (threadIdx.x == 0) {
-    s_gen = ld_acquire_gpu(&C->bar_gen);
-    s_stop = (C->status || C->converged || C->max_reached || C->nodal_due) ? 1 : 0;
-  }
+  if (threadIdx.x == 0) s_stop = (C->status || C->converged || C->max_reached || C->nodal_due) ? 1 : 0;
   __syncthreads();
   if (s_stop) return;
-  unsigned gen = s_gen;
 
   double Ke = C->Ke, f = C->f, e1 = C->e1;
   const double ndmax = C->ndmax;
@@ -174,7 +173,7 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
 #define RED(e) (P.red + ((e) & 1) * kRedQ * kMaxBlocks)
 #define BARRIER()                                  \
   do {                                             \
-    if (!grid_barrier(C, nblk, gen)) return;       \
+    if (!grid_barrier(C, nblk)) return;            \
   } while (0)
 
   const T* Ab = MIXED ? (const T*)P.A32 : (const T*)P.A;
@@ -210,6 +209,7 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
     double* phiN = P.phi[nw];
     const double* fsO = P.fs[old];
     double* fsN = P.fs[nw];
+    const double invKe = 1.0 / Ke;
     double fer_acc = 0.0;
 
     for (int gi = 0; gi < ng; ++gi) {
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
 
       // ---- P0: source and initial residual (TSrc + r = b - A x) --------
       {
-        double acc[1] = {0.0};
+        T accT = T(0);
         for (int b = tid0; b < NB; b += nthr) {
           double s0 = 0.0;
           for (int h = 0; h < ng; ++h) {
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
             const double sg = P.adj ? P.sigs[((size_t)g * ng + h) * NB + b] : P.sigs[((size_t)h * ng + g) * NB + b];
             s0 = fma(sg, ph, s0);
           }
-          const double bs = wsrc[b] * fsO[b] / Ke + s0;
+          const double bs = wsrc[b] * fsO[b] * invKe + s0;
           double ax = A64[b] * xO[b - plane];
           ax = fma(A64[(size_t)NB + b], xO[b - nxx], ax);
           ax = fma(A64[(size_t)2 * NB + b], xO[b - 1], ax);
@@ -244,8 +244,9 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
           const T rt = (T)rr;
           r[b] = rt;
           rs[b] = rt;
-          acc[0] = fma((double)rt, (double)rt, acc[0]);
+          accT = fmav(rt, rt, accT);
         }
+        double acc[1] = {(double)accT};
         block_partials<1, 0u>(acc, RED(epoch));
         BARRIER();
       }
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
         const T tb = (T)beta, tom = (T)omega;
         // ---- phase A: p and v = A p ------------------------------------
         {
-          double acc[1] = {0.0};
+          T accT = T(0);
           for (int b = tid0; b < NB; b += nthr) {
             auto pf = [&](int m) -> T {
               return it == 0 ? r[m] : fmav(tb, fmav(-tom, vO[m], pO[m]), r[m]);
@@ -286,8 +287,9 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
             v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
             pN[b] = pb;
             vN[b] = v;
-            acc[0] = fma((double)rs[b], (double)v, acc[0]);
+            accT = fmav(rs[b], v, accT);
           }
+          double acc[1] = {(double)accT};
           block_partials<1, 0u>(acc, RED(epoch));
           BARRIER();
         }
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
         const T ta = (T)alpha;
         // ---- phase B: s and t = A s ------------------------------------
         {
-          double acc[2] = {0.0, 0.0};
+          T acc0 = T(0), acc1 = T(0);
           for (int b = tid0; b < NB; b += nthr) {
             auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
             const T sb = sf(b);
@@ -314,9 +316,10 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
             tt = fmav(Ag[(size_t)6 * NB + b], sf(b + plane), tt);
             s[b] = sb;
             t[b] = tt;
-            acc[0] = fma((double)tt, (double)tt, acc[0]);
-            acc[1] = fma((double)tt, (double)sb, acc[1]);
+            acc0 = fmav(tt, tt, acc0);
+            acc1 = fmav(tt, sb, acc1);
           }
+          double acc[2] = {(double)acc0, (double)acc1};
           block_partials<2, 0u>(acc, RED(epoch));
           BARRIER();
         }
@@ -331,20 +334,30 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
         const T to = (T)omega;
         // ---- phase C: x and r ------------------------------------------
         {
-          double acc[1] = {0.0};
+          T accT = T(0);
           const double* xc = (it == 0) ? xO : xN;
           for (int b = tid0; b < NB; b += nthr) {
-            const double xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
+            double xn;
+            if (MIXED) {
+              // FP32 increment of the correction, accumulated into the FP64 flux
+              const T dx = fmav(to, s[b], ta * pN[b]);
+              xn = xc[b] + (double)dx;
+            } else {
+              xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
+            }
             xN[b] = xn;
             if (!last) {
               const T rn = fmav(-to, t[b], s[b]);
               r[b] = rn;
-              acc[0] = fma((double)rs[b], (double)rn, acc[0]);
-            } else if (fabs(xn) > 1.e-10) {
-              fer_acc = fmax(fer_acc, fabs(xn - xO[b]) / fabs(xn));
+              accT = fmav(rs[b], rn, accT);
+            } else {
+              // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
+              const double ax = fabs(xn), d = fabs(xn - xO[b]);
+              if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
             }
           }
           if (!last) {
+            double acc[1] = {(double)accT};
             block_partials<1, 0u>(acc, RED(epoch));
             BARRIER();
             grid_totals<1, 0u>(RED(epoch), nblk, tot1);
@@ -368,7 +381,9 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
         acc[0] = fma(en, en, acc[0]);
         if (!extrap) {
           acc[1] = fma(G.vdel[b], fs, acc[1]);
-          if (fabs(fs) > 1.e-10) acc[2] = fmax(acc[2], fabs(en) / fabs(fs));
+          // RelE (mod_cmfd.f90:1143-1168)
+          const double af = fabs(fs), d = fabs(en);
+          if (af > 1.e-10 && d > acc[2] * af) acc[2] = fmax(acc[2], d / af);
         }
       }
       block_partials<4, 0xCu>(acc, RED(epoch));
@@ -390,7 +405,8 @@ __global__ void __launch_bounds__(kOuterThreads) k_outer(OuterParams P) {
         fs = fma(c, fs - fo, fs);
         fsN[b] = fs;
         acc[0] = fma(G.vdel[b], fs, acc[0]);
-        if (fabs(fs) > 1.e-10) acc[1] = fmax(acc[1], fabs(fs - fo) / fabs(fs));
+        const double af = fabs(fs), d = fabs(fs - fo);
+        if (af > 1.e-10 && d > acc[1] * af) acc[1] = fmax(acc[1], d / af);
       }
       block_partials<2, 0x2u>(acc, RED(epoch));
       BARRIER();

@@ -1,0 +1,43 @@
+"""Algorithmic memory traffic of the persistent CMFD kernel.
+
+Bytes are counted per box row (one node of the padded box, one group) as
+the words the kernel must move if every neighbour read hits in cache:
+
+  P0  group source + initial residual (TSrc + r = b - A x):
+      FP64 matrix (7 words), x, fs0, the source weight, (G-1) x (sigma_s,
+      flux of the other group) read; r, rs written.
+  per BiCGSTAB iteration (bicg, mod_cmfd.f90:1228-1241):
+      A: r, p, v, rs + 7 coefficients read; p, v written     (13 words)
+      B: r, v + 7 coefficients read; s, t written            (11 words)
+      C: x, p, s, t, rs read; x, r written                   ( 7 words)
+  per outer: FSrc + norms read G fluxes, G weights, fs0c, vdel and write
+      fs0 (2G + 3 words); extrapolation every nac outers reads fs0, fs0c,
+      vdel and writes fs0 (4 words / nac).
+
+FP64 storage: every word is 8 bytes.  Mixed storage: the matrix copy used
+by the Krylov steps and the Krylov vectors are 4 bytes; the flux x, the
+sources and the FP64 matrix read by P0 stay 8 bytes.
+"""
+from __future__ import annotations
+
+
+def bytes_per_row_outer(ng: int, nin: int, nac: int, precision: str) -> float:
+    G = ng
+    if precision == "fp64":
+        p0 = 8 * (7 + 1 + 1 + 1 + 2 * (G - 1)) + 8 * 2
+        it = 8 * 31
+    else:
+        p0 = 8 * (7 + 1 + 1 + 1 + 2 * (G - 1)) + 4 * 2
+        a = 4 * (4 + 7) + 4 * 2
+        b = 4 * (2 + 7) + 4 * 2
+        c = (8 + 4 * 4) + (8 + 4)
+        it = a + b + c
+    fis = 8 * (2 * G + 3) + 8 * 4 / nac
+    return G * (p0 + nin * it) + fis
+
+
+def bicg_bytes_per_row_iteration(precision: str) -> float:
+    """The canonical per-row BiCGSTAB traffic (31 words)."""
+    if precision == "fp64":
+        return 248.0
+    return 4 * (4 + 7) + 4 * 2 + 4 * (2 + 7) + 4 * 2 + (8 + 4 * 4) + (8 + 4)

@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 static k-eigenvalue path.
+
+Workload (one step = one full k-eigenvalue solve from a cold start,
+f0 = 1 and k = 1, to the reference's convergence test, including the SANM
+nodal updates): the 68x68x80-node, 4-group core (17x17 assemblies of 4x4
+nodes, 80 planes of 5 cm, seed 0 of adpres_gb300.synth.core_4g), solved in
+mixed precision (FP32 matrix copy and Krylov vectors, FP64 flux, FP64
+residual per group solve, FP64 reductions and eigenvalue).  The FP64 path is
+timed on the same core in the same run for the mixed-vs-FP64 comparison.
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+
+value: solves/s with the cross sections resident on the device (CUDA
+events on the solver's stream, L2 flushed between steps).  e2e: solves/s
+through the C ABI from host buffers: cross-section upload, solve, power and
+flux read-back inside the timed region.  The reference arm times the CPU
+restatement of the reference's loops (the oracle; no Fortran compiler is
+available) on all host cores, each core running its own solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-eig solves/s (mixed FP32/FP64, |dk| <= 1 pcm vs FP64)"
+UNIT = "solves/s"
+CONFIG_NAME = "core_4g"
+SEED = 0
+# Outer iterations and nodal updates of one full solve of this core by the
+# oracle (FP64, measured: 234 outers, 2 nodal updates, k = 1.232556358).
+ORACLE_OUTERS = 234
+ORACLE_NODAL = 2
+CPU_SAMPLE_OUTERS = 12
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def workload_text():
+    from adpres_gb300 import synth
+    return synth.core_4g(SEED)
+
+
+def workload_config(dk, precision):
+    return {
+        "workload": "core_4g: 17x17 assemblies of 4x4 nodes, 80 planes of 5 cm (68x68x80 = 369,920 nodes), "
+                    "4 groups, down-scatter only, SANM nodal update, full solve from f0=1 to serc=ferc=1e-5",
+        "nodes": int(dk.nnod), "groups": int(dk.ng), "unknowns": int(dk.nnod * dk.ng), "precision": precision,
+        "nin": int(dk.nin), "nupd": int(dk.nupd), "seed": SEED, "l2": "flushed between steps (256 MiB write)",
+        "parallelism": "replicas only",
+    }
+
+
+# ---------------------------------------------------------------- clocks --
+class Clocks:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                                       "-i", str(index), "-lms", "200"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------- CPU baseline --
+def cpu_sample(text, outers):
+    """Time `outers` outer iterations and one nodal update of the oracle."""
+    import oracle
+    o = oracle.Oracle(text=text)
+    o.xs_updt()
+    t0 = time.perf_counter()
+    o.outer(adjoint=False, popt=1, max_outers=outers)
+    t_outer = (time.perf_counter() - t0) / outers
+    t0 = time.perf_counter()
+    o.nodal_upd(1)
+    t_nodal = time.perf_counter() - t0
+    return t_outer, t_nodal
+
+
+def _worker(args):
+    text, outers = args
+    return cpu_sample(text, outers)
+
+
+def est_solve_seconds(t_outer, t_nodal):
+    return ORACLE_OUTERS * t_outer + ORACLE_NODAL * t_nodal
+
+
+def cpu_baseline_single(text):
+    t_outer, t_nodal = cpu_sample(text, CPU_SAMPLE_OUTERS)
+    est = est_solve_seconds(t_outer, t_nodal)
+    return {"value": 1.0 / est, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle (CPU restatement of the reference loops, -O2, 1 core): {CPU_SAMPLE_OUTERS} outer "
+                      f"iterations ({t_outer * 1e3:.1f} ms each) and one nodal update ({t_nodal * 1e3:.0f} ms) of this "
+                      f"core, scaled to its full solve of {ORACLE_OUTERS} outers and {ORACLE_NODAL} nodal updates "
+                      f"({est:.1f} s)"}
+
+
+# ------------------------------------------------------------ our arm ----
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from adpres_gb300 import _lib, deck, perfmodel
+    from adpres_gb300.core import Core
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if not os.path.exists(_lib.LIB_PATH):
+        from adpres_gb300 import build as libbuild
+        libbuild.build()
+
+    text = workload_text()
+    dk = deck.parse(text)
+    prec = args.precision
+    core = Core.from_deck(dk, precision=prec)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    def step(c):
+        c.reset()
+        return c.outer(adjoint=False, popt=1, trace=False)
+
+    for _ in range(args.warmup):
+        step(core)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t_before = core.timers()
+    clocks = Clocks(local)
+    dev_ms, outers, nodal = [], [], []
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        rep = step(core)
+        dev_ms.append(rep.device_ms)
+        outers.append(rep.outers)
+        nodal.append(rep.nodal_updates)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    t_after = core.timers()
+    total_s = sum(dev_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * args.steps / total_s
+    keff_mixed = rep.keff
+    p_mixed = core.power()
+
+    # dominant kernel: the persistent outer-iteration kernel
+    launches = t_after["outer_kernel_launches"] - t_before["outer_kernel_launches"]
+    kms = t_after["outer_kernel_ms"] - t_before["outer_kernel_ms"]
+    n_outers = sum(outers)
+    NB = dk.nxx * dk.nyy * dk.nzz
+    bytes_per_outer = NB * perfmodel.bytes_per_row_outer(dk.ng, dk.nin, dk.nac, prec)
+    bytes_per_launch = bytes_per_outer * n_outers / launches
+    avg_launch_s = kms / 1e3 / launches
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        peak, peak_src = 6800.0, "fallback"
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "k_outer_mixed_core_4g.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pj = json.load(f)
+        traffic = pj.get("dram_bytes_per_launch_full")
+    gpu_launches = int(sum(2 + 0 for _ in outers) + launches + 5 * sum(nodal))
+
+    # FP64 path on the same core: solves/s and the mixed-precision error
+    core64 = Core.from_deck(dk, precision="fp64")
+    step(core64)
+    d64 = []
+    for _ in range(2):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r64 = step(core64)
+        d64.append(r64.device_ms)
+    p64 = core64.power()
+    fp64_value = 2 / (sum(d64) / 1e3)
+    dk_pcm = abs(keff_mixed - r64.keff) / r64.keff * 1e5
+    m = p64 > 0
+    perr = np.abs(p_mixed[m] - p64[m]) / p64[m]
+    core64.close()
+
+    # e2e through the C ABI from host buffers
+    e2e_steps = max(2, min(args.steps, 5))
+    h2d = (dk.ng * 5 + dk.ng * dk.ng + 6 * dk.ng) * dk.nnod * 8 + dk.nnod * 4
+    d2h = dk.nnod * 8 + dk.nnod * dk.ng * 8
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        core.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
+        core.reset()
+        core.outer(adjoint=False, popt=1, trace=False)
+        core.power()
+        core.state()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * e2e_steps / e2e_s
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    cpu = cpu_baseline_single(text) if world == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage / f64 reductions" if prec == "mixed" else "f64",
+        "data": "synthetic (seeded core, reference deck format)", "config": workload_config(dk, prec),
+        "outers_per_solve": statistics.mean(outers), "nodal_updates_per_solve": statistics.mean(nodal),
+        "keff": keff_mixed,
+        "fp64": {"value": fp64_value, "unit": UNIT, "keff": r64.keff, "outers": r64.outers,
+                 "mixed_speedup": value / fp64_value},
+        "accuracy_vs_fp64": {"dk_pcm": dk_pcm, "power_max_rel": float(perr.max()),
+                             "power_rms_rel": float(np.sqrt(np.mean(perr ** 2)))},
+        "roofline": {"kernel": "k_outer<mixed>" if prec == "mixed" else "k_outer<fp64>", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
+                     "launches": launches},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": gpu_launches,
+        "clocks": ck,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------ reference arm ----
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    from adpres_gb300 import deck
+    oracle.build()
+    text = workload_text()
+    dk = deck.parse(text)
+    cores = os.cpu_count() or 1
+    outers = 4
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_worker, [(text, outers)] * cores)
+        times = []
+        per = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_worker, [(text, outers)] * cores)
+            times.append(time.perf_counter() - t0)
+            per.extend(res)
+    t_outer = statistics.mean(r[0] for r in per)
+    t_nodal = statistics.mean(r[1] for r in per)
+    est = est_solve_seconds(t_outer, t_nodal)
+    value = cores / est
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(times) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded core, reference deck format)",
+        "config": workload_config(dk, "fp64"), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"each step: {cores} independent processes, each timing {outers} outer iterations "
+                                   f"and one nodal update of the oracle (CPU restatement of the reference loops) on "
+                                   f"this core; solves/s = processes / ({ORACLE_OUTERS} x t_outer + {ORACLE_NODAL} x "
+                                   f"t_nodal) = {cores} / {est:.1f} s"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        log("warm-up raised to 3 steps")
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

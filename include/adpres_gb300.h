@@ -172,6 +172,12 @@ adp_status adp_get_state(adp_handle* h, double* f0, double* fs0, double* keff, d
 adp_status adp_set_state(adp_handle* h, const double* f0, const double* fs0, const double* keff,
                          const double* dn);
 
+/* Return the solver state to that of a fresh ADPRES process (dn = 0 as on
+ * coup_coef's first call, mod_cmfd.f90:25-33; the next adp_outer of either
+ * mode starts from f0 = 1, k = 1; ndmax = 0).  Cross sections are kept.
+ * Device-side only: no host copies. */
+adp_status adp_reset(adp_handle* h);
+
 /* PowDis (mod_cmfd.f90:1290-1333): p(n) = sum_g max(0, f0 sigf vdel),
  * normalised to sum 1.  p has nnod entries. */
 adp_status adp_power(adp_handle* h, double* p);

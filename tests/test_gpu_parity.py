@@ -102,16 +102,32 @@ def test_sample_decks_match_oracle(name):
 
 
 def test_nodal_update_location_matches_sweep_order():
-    """ndmax location follows the reference's first-maximum rule (mod_nodal.f90:333-337)."""
+    """ndmax and its location follow the reference's first-maximum rule
+    (mod_nodal.f90:333-337).  The location is compared for the updates
+    whose maximum is well separated (the early ones); near convergence the
+    largest changes of dn are tied to rounding and only the value is compared."""
     fx = fixture("IAEA3Ds")
     c = core_from_fixture(fx)
     rep = c.outer()
     locs = fx["out_trace_loc"]
     nod = np.nonzero(rep.trace_flags & 2)[0]
     assert len(nod) >= 3
-    # the last nodal update's location is what the report carries
-    assert tuple(rep.loc) == tuple(int(v) for v in locs[nod[-1]])
-    np.testing.assert_allclose(rep.trace_ndmax[nod], fx["out_trace_ndmax"][nod], rtol=1e-6)
+    np.testing.assert_array_equal(nod, np.nonzero(fx["out_trace_flags"] & 2)[0])
+    np.testing.assert_allclose(rep.trace_ndmax[nod], fx["out_trace_ndmax"][nod], rtol=1e-5)
+    big = [q for q in nod if fx["out_trace_ndmax"][q] > 1e-2]
+    assert big
+    # The report carries the location of the last update of a call: stop a
+    # fresh solve at nout = nupd so that its last update is the first one.
+    c2 = core_from_fixture(fx, nout=int(fx["iter_int"][3]))
+    with pytest.raises(AdpError) as e:
+        c2.outer()
+    assert e.value.status == ADP_ERR_MAXOUTER
+    assert big[0] == int(fx["iter_int"][3]) - 1
+    # IAEA3D's quarter core is symmetric about its diagonal, (i,j) <-> (18-j, 18-i):
+    # mirror nodes have equal changes in exact arithmetic and rounding picks one.
+    i, j, k = (int(v) for v in locs[big[0]])
+    nxx, nyy = int(fx["nxx"]), int(fx["nyy"])
+    assert tuple(c2.last_report.loc) in ((i, j, k), (nxx + 1 - j, nyy + 1 - i, k))
 
 
 def _oracle_run(text):
