@@ -1,0 +1,111 @@
+!
+! adpres_gb300_bind.f90 -- Fortran 2003 ISO_C_BINDING interface to the C ABI
+! declared in adpres_gb300.h, for a Fortran host (such as ADPRES) that
+! replaces its own outer()/outer_ad() (mod_cmfd.f90:415, :602) and PowDis
+! (:1290) with the GB300 solver.  Arrays are passed in the host's own
+! column-major layouts (node index fastest), 1-based indices as in sdata.
+!
+! This module has not been compiled in the build environment, which has no
+! Fortran compiler; it follows the C declarations one to one.
+!
+module adpres_gb300_bind
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: ADP_OK = 0
+  integer(c_int), parameter :: ADP_FORWARD = 0, ADP_ADJOINT = 1
+  integer(c_int), parameter :: ADP_KERN_FDM = 0, ADP_KERN_PNM = 1, ADP_KERN_SANM = 2
+  integer(c_int), parameter :: ADP_FP64 = 0, ADP_MIXED = 1
+
+  type, bind(C) :: adp_geom
+    integer(c_int) :: nxx, nyy, nzz
+    integer(c_int) :: nnod
+    type(c_ptr)    :: ix, iy, iz          ! int[nnod]
+    type(c_ptr)    :: xdel, ydel, zdel    ! double[nxx], [nyy], [nzz]
+    integer(c_int) :: east, west, north, south, bottom, top
+  end type
+
+  type, bind(C) :: adp_opts
+    integer(c_int) :: ng, nin, nout, nac, nupd
+    real(c_double) :: serc, ferc
+    integer(c_int) :: kern, precision
+  end type
+
+  type, bind(C) :: adp_report
+    integer(c_int) :: outers, converged, nodal_updates
+    real(c_double) :: keff, ser, fer, ndmax
+    integer(c_int) :: im, jm, km
+    integer(c_int) :: trace_cap
+    type(c_ptr)    :: trace_k, trace_ser, trace_fer, trace_flags, trace_ndmax
+    real(c_double) :: device_ms
+  end type
+
+  interface
+    integer(c_int) function adp_create(geom, opts, h) bind(C, name="adp_create")
+      import :: adp_geom, adp_opts, c_int, c_ptr
+      type(adp_geom), intent(in) :: geom
+      type(adp_opts), intent(in) :: opts
+      type(c_ptr), intent(out)   :: h
+    end function
+
+    integer(c_int) function adp_destroy(h) bind(C, name="adp_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    integer(c_size_t) function adp_last_error(h, buf, len) bind(C, name="adp_last_error")
+      import :: c_size_t, c_ptr, c_char
+      type(c_ptr), value :: h
+      character(kind=c_char), intent(out) :: buf(*)
+      integer(c_size_t), value :: len
+    end function
+
+    integer(c_int) function adp_xs_updt(h, nmat, xsigtr, xsiga, xnuf, xsigf, chi, mat, xsigs, dc) &
+        bind(C, name="adp_xs_updt")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: nmat
+      real(c_double), intent(in) :: xsigtr(*), xsiga(*), xnuf(*), xsigf(*), chi(*), xsigs(*), dc(*)
+      integer(c_int), intent(in) :: mat(*)
+    end function
+
+    integer(c_int) function adp_set_xs(h, nmat, D, sigr, nuf, sigf, chi, mat, sigs, dc) bind(C, name="adp_set_xs")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: nmat
+      real(c_double), intent(in) :: D(*), sigr(*), nuf(*), sigf(*), chi(*), sigs(*), dc(*)
+      integer(c_int), intent(in) :: mat(*)
+    end function
+
+    integer(c_int) function adp_outer(h, mode, popt, rep) bind(C, name="adp_outer")
+      import :: c_int, c_ptr, adp_report
+      type(c_ptr), value :: h
+      integer(c_int), value :: mode, popt
+      type(adp_report), intent(inout) :: rep
+    end function
+
+    integer(c_int) function adp_get_state(h, f0, fs0, keff, dn) bind(C, name="adp_get_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: f0(*), fs0(*), keff, dn(*)
+    end function
+
+    integer(c_int) function adp_set_state(h, f0, fs0, keff, dn) bind(C, name="adp_set_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: f0(*), fs0(*), keff, dn(*)
+    end function
+
+    integer(c_int) function adp_reset(h) bind(C, name="adp_reset")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+    end function
+
+    integer(c_int) function adp_power(h, p) bind(C, name="adp_power")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: p(*)
+    end function
+  end interface
+
+end module adpres_gb300_bind
