@@ -81,6 +81,8 @@ SIGNATURES = {
     "adp_set_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
     "adp_power": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "adp_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "adp_power_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "adp_get_timers": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpTimers)]),
     "adp_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }

@@ -34,6 +34,14 @@ struct DevArena {
 
 }  // namespace
 
+namespace adp {
+// Message for adp_last_error(NULL) from entry points that take no handle.
+void set_global_error(const std::string& msg) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_create_err = msg;
+}
+}  // namespace adp
+
 struct adp_handle {
   std::string err;
   int dev = 0;

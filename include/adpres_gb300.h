@@ -182,6 +182,25 @@ adp_status adp_reset(adp_handle* h);
  * normalised to sum 1.  p has nnod entries. */
 adp_status adp_power(adp_handle* h, double* p);
 
+/* PowDis without a handle and without allocating: no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc -- a host whose device
+ * memory belongs to another allocator (a framework's caching allocator, or a
+ * budget fixed at start-up), or a path where cudaMalloc/cudaFree and their
+ * implicit device synchronisation are not acceptable.  f0 (nnod,ng) and
+ * sigf (nnod,ng) (node index fastest), vdel (nnod) and the output p (nnod)
+ * are device pointers owned by the caller; stream is a cudaStream_t (NULL
+ * for the default stream); the call returns when p is written.  Limits:
+ * 1 <= ng <= 8 and nnod * ng <= 2^31 - 1; larger sizes return
+ * ADP_ERR_INPUT.  Its scratch (block partial sums and a status word) is a
+ * fixed 8,448-byte array of device memory inside the library, held on every
+ * GPU that loads the library until the process exits.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress), so
+ * make the first call on each device before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race; serialise them.
+ * Errors: message through adp_last_error(NULL). */
+adp_status adp_power_noalloc(int nnod, int ng, const double* f0, const double* sigf, const double* vdel, double* p,
+                             void* stream);
+
 /* Device timers of the handle. */
 adp_status adp_get_timers(const adp_handle* h, adp_timers* t);
 
