@@ -187,29 +187,137 @@ __device__ __forceinline__ void block_partials(const double (&v)[NQ], double* ou
 }
 
 // Totals of NQ quantities from the partials of nblk blocks, identical in
-// every block; every thread of the block receives them.
+// every block; every thread of the block receives them.  Warp q reduces
+// quantity q; each lane issues its loads eight at a time before adding, so
+// the partials cost one L2 round trip per 256 blocks instead of one per
+// loop step.  The summation order is fixed by (lane, k), hence the same in
+// every block.
 template <int NQ, unsigned MAXMASK>
 __device__ __forceinline__ void grid_totals(const double* in, int nblk, double (&tot)[NQ]) {
   __shared__ double st[NQ];
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x < 32) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (w < NQ) {
+    const bool mx = (MAXMASK >> w) & 1u;
+    const double* src = in + w * kMaxBlocks;
+    double x = 0.0;
+    for (int base = 0; base < nblk; base += 256) {
+      double v[8];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-      const bool mx = (MAXMASK >> q) & 1u;
-      const double* src = in + q * kMaxBlocks;
-      double x = 0.0;
-      for (int k = lane; k < nblk; k += 32) {
-        double y = __ldcg(src + k);   // L2: partials were written by other SMs
-        x = mx ? fmax(x, y) : x + y;
+      for (int k = 0; k < 8; ++k) {
+        const int i = base + lane + 32 * k;
+        v[k] = (i < nblk) ? __ldcg(src + i) : 0.0;   // L2: partials were written by other SMs
       }
-      x = mx ? warp_all<true>(x) : warp_all<false>(x);
-      if (lane == 0) st[q] = x;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) x = mx ? fmax(x, v[k]) : x + v[k];
     }
+    x = mx ? warp_all<true>(x) : warp_all<false>(x);
+    if (lane == 0) st[w] = x;
   }
   __syncthreads();
 #pragma unroll
   for (int q = 0; q < NQ; ++q) tot[q] = st[q];
   __syncthreads();
+}
+
+// xor-butterfly over a warp for NQ independent values at once (the steps of
+// the different quantities are interleaved, so their latencies overlap).
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ void warp_all_n(double (&x)[NQ]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double y[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) y[q] = __shfl_xor_sync(0xffffffffu, x[q], o);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) x[q] = ((MAXMASK >> q) & 1u) ? fmax(x[q], y[q]) : x[q] + y[q];
+  }
+}
+
+// Block reduction, grid barrier and totals in one step, with two block-wide
+// synchronisations: every warp reduces its values; after the first
+// __syncthreads warp 0 forms the block partials, lane 0 publishes them and
+// waits at the grid barrier, and warp 0 then sums every block's partials
+// (same order in every block) into shared memory for the whole block.
+// Returns false when the barrier wait ran out of time.
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ bool grid_reduce(OuterCtl* C, unsigned nblocks, double* slot, const double (&v)[NQ],
+                                            double (&tot)[NQ]) {
+  __shared__ double sw[NQ][32];
+  __shared__ double st[NQ];
+  __shared__ int s_ok;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  double x[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) x[q] = v[q];
+  warp_all_n<NQ, MAXMASK>(x);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) sw[q][w] = x[q];
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) x[q] = lane < nw ? sw[q][lane] : 0.0;   // sums and maxima of |.| start at 0
+    warp_all_n<NQ, MAXMASK>(x);
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) slot[q * kMaxBlocks + blockIdx.x] = x[q];
+    }
+    int ok = 1;
+    if (lane == 0) {
+      const unsigned add = (blockIdx.x == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
+      __threadfence();
+      const unsigned old = atomicAdd(&C->bar_count, add);
+      if (!(((old + add) ^ old) & 0x80000000u)) {
+        unsigned long long t0 = 0;
+        unsigned spins = 0;
+        while (!((ld_acquire_gpu(&C->bar_count) ^ old) & 0x80000000u)) {
+          if ((++spins & 63u) == 0) {
+            const unsigned long long t = globaltimer_ns();
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > kBarrierTimeoutNs) {
+              set_status(C, ADP_ERR_TIMEOUT);
+              ok = 0;
+              break;
+            }
+          }
+        }
+      }
+      __threadfence();
+      if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
+    }
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    if (ok) {
+      const int nblk = (int)nblocks;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) x[q] = 0.0;
+      for (int base = 0; base < nblk; base += 256) {
+        double y[NQ][8];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int i = base + lane + 32 * k;
+            y[q][k] = (i < nblk) ? __ldcg(slot + q * kMaxBlocks + i) : 0.0;   // L2: written by other SMs
+          }
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+#pragma unroll
+          for (int q = 0; q < NQ; ++q) x[q] = ((MAXMASK >> q) & 1u) ? fmax(x[q], y[q][k]) : x[q] + y[q][k];
+      }
+      warp_all_n<NQ, MAXMASK>(x);
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) st[q] = x[q];
+      }
+    }
+    if (lane == 0) s_ok = ok;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) tot[q] = st[q];
+  return s_ok != 0;
 }
 
 }  // namespace adp

@@ -68,6 +68,7 @@ struct NodalParams {
   double* a2;                 // [3][ng][NB]
   double* a4;
   double* L1;
+  double* Bc;                 // [3][ng][ng][NB] buckling matrix per node and direction
   const int* evbase;          // [3][NB] sweep-order index of a node's minus face
   double* nd_val;             // [kMaxBlocks] ndmax partials
   long long* nd_key;

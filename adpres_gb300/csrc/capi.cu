@@ -79,7 +79,7 @@ struct adp_handle {
   OuterCtl* h_ctl = nullptr;   // pinned mirror
   double *d_tr_k = nullptr, *d_tr_ser = nullptr, *d_tr_fer = nullptr, *d_tr_ndmax = nullptr;
   int* d_tr_flags = nullptr;
-  double *d_sanm = nullptr, *d_S = nullptr, *d_a2 = nullptr, *d_a4 = nullptr, *d_L1 = nullptr;
+  double *d_sanm = nullptr, *d_S = nullptr, *d_a2 = nullptr, *d_a4 = nullptr, *d_L1 = nullptr, *d_Bc = nullptr;
   double* d_ndval = nullptr;
   long long* d_ndkey = nullptr;
   int* d_ndloc = nullptr;
@@ -354,6 +354,7 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
   add(nout * 8 * 4 + nout * 4);
   if (opts->kern == ADP_KERN_SANM) add(3 * 6 * G * NB * 8);
   if (opts->kern != ADP_KERN_FDM) add(3 * G * NB * 8 * 4);
+  if (opts->kern != ADP_KERN_FDM) add(3 * G * G * NB * 8);
   add(kMaxBlocks * 8 * 2 + kMaxBlocks * 4);
   add(NB * 8);
   h->ar.size = bytes;
@@ -405,6 +406,7 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
     h->d_a2 = (double*)A.take(3 * G * NB * 8);
     h->d_a4 = (double*)A.take(3 * G * NB * 8);
     h->d_L1 = (double*)A.take(3 * G * NB * 8);
+    h->d_Bc = (double*)A.take(3 * G * G * NB * 8);
   }
   h->d_ndval = (double*)A.take(kMaxBlocks * 8);
   h->d_ndkey = (long long*)A.take(kMaxBlocks * 8);
@@ -519,6 +521,7 @@ static NodalParams nodal_params(adp_handle* h, int cmode) {
   P.a2 = h->d_a2;
   P.a4 = h->d_a4;
   P.L1 = h->d_L1;
+  P.Bc = h->d_Bc;
   P.evbase = h->d_evbase;
   P.nd_val = h->d_ndval;
   P.nd_key = h->d_ndkey;
@@ -662,13 +665,24 @@ static OuterParams outer_params(adp_handle* h, int adj) {
   return P;
 }
 
+// Launch shape of the persistent kernel: at most one 512-thread block per SM
+// (more co-resident blocks only add barrier participants), and a block
+// count that gives every thread the same number of rows, so no block waits
+// at a grid barrier for blocks holding one row more.
 static void launch_shape(adp_handle* h, int& blocks, int& threads) {
   threads = h->launch_threads > 0 ? h->launch_threads : 512;
   int occ = outer_max_blocks_per_sm(threads, h->o.precision == ADP_MIXED);
   if (occ < 1) occ = 1;
-  int cap = std::min(h->sms * occ, kMaxBlocks);
-  int want = (int)std::max(1LL, ((long long)h->NB + 2LL * threads - 1) / (2LL * threads));
-  blocks = h->launch_blocks > 0 ? std::min(h->launch_blocks, cap) : std::min(want, cap);
+  const int cap = std::min(h->sms * occ, kMaxBlocks);
+  if (h->launch_blocks > 0) {
+    blocks = std::min(h->launch_blocks, cap);
+    return;
+  }
+  const long long NB = h->NB;
+  const long long full = (long long)std::min(cap, h->sms) * threads;
+  const long long rows = std::max(1LL, (NB + full - 1) / full);       // rows per thread
+  blocks = (int)std::max(1LL, (NB + rows * threads - 1) / (rows * threads));
+  blocks = std::min(blocks, cap);
 }
 
 static adp_status ctl_error(adp_handle* h, const OuterCtl& c) {
@@ -693,7 +707,7 @@ static adp_status ctl_error(adp_handle* h, const OuterCtl& c) {
 
 adp_status adp_set_launch(adp_handle* h, int blocks, int threads) {
   if (!h) return ADP_ERR_INPUT;
-  if (threads != 0 && (threads < 64 || threads > 512 || threads % 32)) return fail(h, ADP_ERR_INPUT, "threads must be 64..512, a multiple of 32");
+  if (threads != 0 && (threads < 64 || threads > 1024 || threads % 32)) return fail(h, ADP_ERR_INPUT, "threads must be 64..1024, a multiple of 32");
   if (blocks < 0 || blocks > kMaxBlocks) return fail(h, ADP_ERR_INPUT, "blocks out of range");
   h->launch_blocks = blocks;
   h->launch_threads = threads;

@@ -125,13 +125,18 @@ cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
 // barrier; neighbour reads and global dot products are separated by
 // grid_barrier.  Per group solve (bicg, mod_cmfd.f90:1203-1243):
 //   P0: b = TSrc, r = b - A x, rs = r, partial (rs,r)              | barrier
-//   per iteration i = 1..nin:
-//   A : beta, p = r + beta (p - omega v) (neighbours recomputed),
-//       v = A p, partial (rs,v)                                     | barrier
+//   per step i = 1..nin:
+//   A : (i > 1: the previous step's x += alpha p + omega s and
+//       r = s - omega t, r recomputed at neighbours), beta,
+//       p = r + beta (p - omega v) (neighbours recomputed), v = A p,
+//       partial (rs,v)                                               | barrier
 //   B : alpha, s = r - alpha v (neighbours recomputed), t = A s,
-//       partials (t,t), (t,s)                                       | barrier
-//   C : omega, x += alpha p + omega s, r = s - omega t,
-//       partial (rs,r) (not after the last iteration)               | barrier
+//       partials (t,t), (t,s) and, before another step, (rs,s), (rs,t),
+//       whence (rs, r_next) = (rs,s) - omega (rs,t)                  | barrier
+//   C (last step only, no barrier): x += alpha p + omega s, RelEg.
+// Two grid barriers per BiCGSTAB step instead of three: the (rs,r)
+// reduction of bicg (mod_cmfd.f90:1230) is formed algebraically from
+// phase-B partials, so the r/x update joins the next step's phase A.
 // After the last group: FSrc, |fs - fs0c|^2, Integrate, RelE, RelEg
 // (barrier), extrapolation every nac outers (barrier), k update and the
 // convergence test, all in the same order as mod_cmfd.f90:479-495.
@@ -171,10 +176,6 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
   int epoch = 0;
   const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
 #define RED(e) (P.red + ((e) & 1) * kRedQ * kMaxBlocks)
-#define BARRIER()                                  \
-  do {                                             \
-    if (!grid_barrier(C, nblk)) return;            \
-  } while (0)
 
   const T* Ab = MIXED ? (const T*)P.A32 : (const T*)P.A;
   T* r = MIXED ? (T*)P.r32 : (T*)P.r;
@@ -192,10 +193,8 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
       acc[0] = fma(G.vdel[b], fsc[b], acc[0]);
       acc[1] += G.vdel[b];
     }
-    block_partials<2, 0u>(acc, RED(epoch));
-    BARRIER();
     double tot[2];
-    grid_totals<2, 0u>(RED(epoch), nblk, tot);
+    if (!grid_reduce<2, 0u>(C, nblk, RED(epoch), acc, tot)) return;
     ++epoch;
     f = tot[0];
     e1 = tot[1];
@@ -221,6 +220,7 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
       const double* wsrc = P.wsrc + (size_t)g * NB;
 
       // ---- P0: source and initial residual (TSrc + r = b - A x) --------
+      double tot1[1];
       {
         T accT = T(0);
         for (int b = tid0; b < NB; b += nthr) {
@@ -247,11 +247,8 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
           accT = fmav(rt, rt, accT);
         }
         double acc[1] = {(double)accT};
-        block_partials<1, 0u>(acc, RED(epoch));
-        BARRIER();
+        if (!grid_reduce<1, 0u>(C, nblk, RED(epoch), acc, tot1)) return;
       }
-      double tot1[1];
-      grid_totals<1, 0u>(RED(epoch), nblk, tot1);
       ++epoch;
       double rsr = tot1[0];
       double rho = 1.0, alpha = 1.0, omega = 1.0;
@@ -269,31 +266,53 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
         const T* pO = pv[(it & 1) ^ 1];
         T* vN = vv[it & 1];
         const T* vO = vv[(it & 1) ^ 1];
-        const T tb = (T)beta, tom = (T)omega;
-        // ---- phase A: p and v = A p ------------------------------------
+        const T tb = (T)beta, tom = (T)omega, tap = (T)alpha;
+        // ---- phase A: (previous step's x and r), p and v = A p -----------
         {
           T accT = T(0);
-          for (int b = tid0; b < NB; b += nthr) {
-            auto pf = [&](int m) -> T {
-              return it == 0 ? r[m] : fmav(tb, fmav(-tom, vO[m], pO[m]), r[m]);
-            };
-            const T pb = pf(b);
-            T v = Ag[b] * pf(b - plane);
-            v = fmav(Ag[(size_t)NB + b], pf(b - nxx), v);
-            v = fmav(Ag[(size_t)2 * NB + b], pf(b - 1), v);
-            v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-            v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
-            v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
-            v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
-            pN[b] = pb;
-            vN[b] = v;
-            accT = fmav(rs[b], v, accT);
+          if (it == 0) {
+            for (int b = tid0; b < NB; b += nthr) {
+              const T pb = r[b];
+              T v = Ag[b] * r[b - plane];
+              v = fmav(Ag[(size_t)NB + b], r[b - nxx], v);
+              v = fmav(Ag[(size_t)2 * NB + b], r[b - 1], v);
+              v = fmav(Ag[(size_t)3 * NB + b], pb, v);
+              v = fmav(Ag[(size_t)4 * NB + b], r[b + 1], v);
+              v = fmav(Ag[(size_t)5 * NB + b], r[b + nxx], v);
+              v = fmav(Ag[(size_t)6 * NB + b], r[b + plane], v);
+              pN[b] = pb;
+              vN[b] = v;
+              accT = fmav(rs[b], v, accT);
+            }
+          } else {
+            const double* xc = (it == 1) ? xO : xN;
+            for (int b = tid0; b < NB; b += nthr) {
+              auto rf = [&](int m) -> T { return fmav(-tom, t[m], s[m]); };
+              auto pf = [&](int m) -> T { return fmav(tb, fmav(-tom, vO[m], pO[m]), rf(m)); };
+              const T rb = rf(b);
+              r[b] = rb;
+              if (MIXED) {
+                const T dx = fmav(tom, s[b], tap * pO[b]);
+                xN[b] = xc[b] + (double)dx;
+              } else {
+                xN[b] = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
+              }
+              const T pb = fmav(tb, fmav(-tom, vO[b], pO[b]), rb);
+              T v = Ag[b] * pf(b - plane);
+              v = fmav(Ag[(size_t)NB + b], pf(b - nxx), v);
+              v = fmav(Ag[(size_t)2 * NB + b], pf(b - 1), v);
+              v = fmav(Ag[(size_t)3 * NB + b], pb, v);
+              v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
+              v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
+              v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
+              pN[b] = pb;
+              vN[b] = v;
+              accT = fmav(rs[b], v, accT);
+            }
           }
           double acc[1] = {(double)accT};
-          block_partials<1, 0u>(acc, RED(epoch));
-          BARRIER();
+          if (!grid_reduce<1, 0u>(C, nblk, RED(epoch), acc, tot1)) return;
         }
-        grid_totals<1, 0u>(RED(epoch), nblk, tot1);
         ++epoch;
         if (tot1[0] == 0.0) {
           if (lead) set_status(C, ADP_ERR_BREAKDOWN);
@@ -301,9 +320,11 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
         }
         alpha = rho / tot1[0];
         const T ta = (T)alpha;
-        // ---- phase B: s and t = A s ------------------------------------
+        // ---- phase B: s and t = A s; (t,t), (t,s) and, for the next step,
+        //      (rs,s), (rs,t): (rs, s - omega t) = (rs,s) - omega (rs,t) ------
+        double tot4[4];
         {
-          T acc0 = T(0), acc1 = T(0);
+          T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
           for (int b = tid0; b < NB; b += nthr) {
             auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
             const T sb = sf(b);
@@ -318,23 +339,35 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
             t[b] = tt;
             acc0 = fmav(tt, tt, acc0);
             acc1 = fmav(tt, sb, acc1);
+            if (!last) {
+              const T rb = rs[b];
+              acc2 = fmav(rb, sb, acc2);
+              acc3 = fmav(rb, tt, acc3);
+            }
           }
-          double acc[2] = {(double)acc0, (double)acc1};
-          block_partials<2, 0u>(acc, RED(epoch));
-          BARRIER();
+          if (last) {
+            double acc[2] = {(double)acc0, (double)acc1}, tot2[2];
+            if (!grid_reduce<2, 0u>(C, nblk, RED(epoch), acc, tot2)) return;
+            tot4[0] = tot2[0];
+            tot4[1] = tot2[1];
+          } else {
+            double acc[4] = {(double)acc0, (double)acc1, (double)acc2, (double)acc3};
+            if (!grid_reduce<4, 0u>(C, nblk, RED(epoch), acc, tot4)) return;
+          }
         }
-        double tot2[2];
-        grid_totals<2, 0u>(RED(epoch), nblk, tot2);
         ++epoch;
-        if (tot2[0] == 0.0) {
+        if (tot4[0] == 0.0) {
           if (lead) set_status(C, ADP_ERR_BREAKDOWN);
           return;
         }
-        omega = tot2[1] / tot2[0];
-        const T to = (T)omega;
-        // ---- phase C: x and r ------------------------------------------
-        {
-          T accT = T(0);
+        omega = tot4[1] / tot4[0];
+        if (!last) {
+          rsr = tot4[2] - omega * tot4[3];
+        } else {
+          // ---- phase C of the last step: x, and RelEg's running maximum.
+          // No barrier follows: the next group's P0 (or the fission source)
+          // reads only this thread's own rows of x.
+          const T to = (T)omega;
           const double* xc = (it == 0) ? xO : xN;
           for (int b = tid0; b < NB; b += nthr) {
             double xn;
@@ -346,23 +379,9 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
               xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
             }
             xN[b] = xn;
-            if (!last) {
-              const T rn = fmav(-to, t[b], s[b]);
-              r[b] = rn;
-              accT = fmav(rs[b], rn, accT);
-            } else {
-              // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
-              const double ax = fabs(xn), d = fabs(xn - xO[b]);
-              if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
-            }
-          }
-          if (!last) {
-            double acc[1] = {(double)accT};
-            block_partials<1, 0u>(acc, RED(epoch));
-            BARRIER();
-            grid_totals<1, 0u>(RED(epoch), nblk, tot1);
-            ++epoch;
-            rsr = tot1[0];
+            // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
+            const double ax = fabs(xn), d = fabs(xn - xO[b]);
+            if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
           }
         }
       }
@@ -386,9 +405,7 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
           if (af > 1.e-10 && d > acc[2] * af) acc[2] = fmax(acc[2], d / af);
         }
       }
-      block_partials<4, 0xCu>(acc, RED(epoch));
-      BARRIER();
-      grid_totals<4, 0xCu>(RED(epoch), nblk, tot4);
+      if (!grid_reduce<4, 0xCu>(C, nblk, RED(epoch), acc, tot4)) return;
       ++epoch;
     }
     const double e2 = sqrt(tot4[0]);
@@ -408,10 +425,8 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
         const double af = fabs(fs), d = fabs(fs - fo);
         if (af > 1.e-10 && d > acc[1] * af) acc[1] = fmax(acc[1], d / af);
       }
-      block_partials<2, 0x2u>(acc, RED(epoch));
-      BARRIER();
       double tot[2];
-      grid_totals<2, 0x2u>(RED(epoch), nblk, tot);
+      if (!grid_reduce<2, 0x2u>(C, nblk, RED(epoch), acc, tot)) return;
       ++epoch;
       fsum = tot[0];
       ser = tot[1];
@@ -457,7 +472,6 @@ __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
     }
   }
 #undef RED
-#undef BARRIER
 }
 
 int outer_max_blocks_per_sm(int threads, int mixed) {

@@ -127,159 +127,125 @@ __device__ __forceinline__ LinePos line_pos(const BoxGeom& G, int u, int b) {
   return L;
 }
 
-// TLUpd1 (mod_nodal.f90:1047-1199): first moment of the transverse leakage.
-__device__ double tlupd1(const NodalParams& P, int u, int b, int g) {
-  const BoxGeom& G = P.G;
+// Geometry factors of the transverse-leakage moments of node b along u
+// (TLUpd1, mod_nodal.f90:1047-1199; TLUpd2, :1203-1341).  With S the
+// zeroth-order source along u and n, p, m the node and its plus and minus
+// neighbours:
+//   first moment  = c1p (S_p - S_n) + c1m (S_n - S_m)
+//   second moment = c2p (S_p - S_n) + c2m (S_m - S_n)
+// multiplied by 0.25 h^2 / D_g.  A reflective line end mirrors the missing
+// neighbour (tm or tp = 1); any other line end uses the one-sided forms.
+// The factors do not depend on the group, so they are formed once per
+// node and direction.
+struct TLGeom {
+  double c1p, c1m, c2p, c2m;
+  int offp;
+  bool has_p, has_m;
+};
+
+__device__ __forceinline__ TLGeom tl_geom(const BoxGeom& G, int u, int b) {
   const LinePos L = line_pos(G, u, b);
-  const double* S = P.S + ((size_t)u * P.ng + g) * G.NB;
+  TLGeom T;
+  T.offp = L.offp;
+  T.has_p = !L.last;
+  T.has_m = !L.first;
+  T.c1p = T.c1m = T.c2p = T.c2m = 0.0;
   const double h0 = hdir(G, u, b);
-  double Lm, tm, tp, p1m, p2m, p1p, p2p, hp;
   if (L.first) {
-    const double hpv = hdir(G, u, b + L.offp);
+    const double tp = hdir(G, u, b + L.offp) / h0;
+    const double p1p = tp + 1.0;
     if (L.refl_first) {
-      tm = 1.0;
-      tp = hpv / h0;
-      p1m = tm + 1.0;
-      p2m = 2.0 * tm + 1.0;
-      p1p = tp + 1.0;
-      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
-      Lm = (p1m * p2m * (S[b + L.offp] - S[b])) / hp;
+      const double tm = 1.0, p1m = tm + 1.0, p2m = 2.0 * tm + 1.0;
+      const double hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+      T.c1p = p1m * p2m / hp;
+      T.c2p = p1m / hp;
     } else {
-      tp = hpv / h0;
-      p1p = tp + 1.0;
-      Lm = (S[b + L.offp] - S[b]) / p1p;
+      T.c1p = 1.0 / p1p;
     }
   } else if (L.last) {
-    const double hmv = hdir(G, u, b - L.offp);
+    const double tm = hdir(G, u, b - L.offp) / h0;
+    const double p1m = tm + 1.0;
     if (L.refl_last) {
-      tm = hmv / h0;
-      tp = 1.0;
-      p1m = tm + 1.0;
-      p1p = tp + 1.0;
-      p2p = 2.0 * tp + 1.0;
-      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
-      Lm = (p1p * p2p * (S[b] - S[b - L.offp])) / hp;
+      const double tp = 1.0, p1p = tp + 1.0, p2p = 2.0 * tp + 1.0;
+      const double hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+      T.c1m = p1p * p2p / hp;
+      T.c2m = p1p / hp;
     } else {
-      tm = hmv / h0;
-      p1m = tm + 1.0;
-      Lm = (S[b] - S[b - L.offp]) / p1m;
+      T.c1m = 1.0 / p1m;
     }
   } else {
-    tm = hdir(G, u, b - L.offp) / h0;
-    tp = hdir(G, u, b + L.offp) / h0;
-    p1m = tm + 1.0;
-    p2m = 2.0 * tm + 1.0;
-    p1p = tp + 1.0;
-    p2p = 2.0 * tp + 1.0;
-    hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
-    Lm = (p1m * p2m * (S[b + L.offp] - S[b]) + p1p * p2p * (S[b] - S[b - L.offp])) / hp;
+    const double tm = hdir(G, u, b - L.offp) / h0;
+    const double tp = hdir(G, u, b + L.offp) / h0;
+    const double p1m = tm + 1.0, p2m = 2.0 * tm + 1.0;
+    const double p1p = tp + 1.0, p2p = 2.0 * tp + 1.0;
+    const double hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
+    T.c1p = p1m * p2m / hp;
+    T.c1m = p1p * p2p / hp;
+    T.c2p = p1m / hp;
+    T.c2m = p1p / hp;
   }
-  return 0.25 * (h0 * h0) / P.D[(size_t)g * G.NB + b] * Lm;
+  return T;
 }
 
-// TLUpd2 (mod_nodal.f90:1203-1341): second moment of the transverse leakage.
-__device__ double tlupd2(const NodalParams& P, int u, int b, int g) {
-  const BoxGeom& G = P.G;
-  const LinePos L = line_pos(G, u, b);
-  const double* S = P.S + ((size_t)u * P.ng + g) * G.NB;
-  const double h0 = hdir(G, u, b);
-  double Lm, tm, tp, p1m, p1p, hp;
-  if (L.first) {
-    if (L.refl_first) {
-      tm = 1.0;
-      tp = hdir(G, u, b + L.offp) / h0;
-      p1m = tm + 1.0;
-      p1p = tp + 1.0;
-      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
-      Lm = (p1m * (S[b + L.offp] - S[b])) / hp;
-    } else {
-      Lm = 0.0;
-    }
-  } else if (L.last) {
-    if (L.refl_last) {
-      tm = hdir(G, u, b - L.offp) / h0;
-      tp = 1.0;
-      p1m = tm + 1.0;
-      p1p = tp + 1.0;
-      hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
-      Lm = (p1p * (S[b - L.offp] - S[b])) / hp;
-    } else {
-      Lm = 0.0;
-    }
-  } else {
-    tm = hdir(G, u, b - L.offp) / h0;
-    tp = hdir(G, u, b + L.offp) / h0;
-    p1m = tm + 1.0;
-    p1p = tp + 1.0;
-    hp = 2.0 * p1m * p1p * (tm + tp + 1.0);
-    Lm = (p1m * (S[b + L.offp] - S[b]) + p1p * (S[b - L.offp] - S[b])) / hp;
-  }
-  return 0.25 * (h0 * h0) / P.D[(size_t)g * G.NB + b] * Lm;
-}
-
-// get_B (mod_nodal.f90:1345-1405): buckling matrix of node b in direction u.
-// cmode 1 forward, 0 adjoint (transposed group coupling).
+// get_B (mod_nodal.f90:1345-1405): buckling matrix of node b in direction u,
+// B(g,h) = 0.25 h^2 / D_g * (sigr_g delta_gh - sigs(h->g) - chi_g nuf_h / k)
+// (forward, cmode 1) or the transposed group coupling (adjoint, cmode 0).
 template <int NG>
-__device__ __forceinline__ void get_B(const NodalParams& P, int u, int b, double Ke, double (&B)[NG][NG]) {
+__device__ __forceinline__ void get_B(const NodalParams& P, int b, double invKe, const double (&fac)[NG],
+                                      double (&B)[NG][NG]) {
   const int NB = P.G.NB;
-  const double dn = hdir(P.G, u, b);
 #pragma unroll
   for (int g = 0; g < NG; ++g) {
-    const double fac = 0.25 * (dn * dn) / P.D[(size_t)g * NB + b];
 #pragma unroll
     for (int h = 0; h < NG; ++h) {
       double dum;
       if (g == h) {
-        dum = P.sigr[(size_t)g * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] / Ke;
+        dum = P.sigr[(size_t)g * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] * invKe;
       } else if (P.cmode == 1) {
-        dum = -P.sigs[((size_t)h * NG + g) * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] / Ke;
+        dum = -P.sigs[((size_t)h * NG + g) * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] * invKe;
       } else {
-        dum = -P.sigs[((size_t)g * NG + h) * NB + b] - P.chin[(size_t)h * NB + b] * P.nuf[(size_t)g * NB + b] / Ke;
+        dum = -P.sigs[((size_t)g * NG + h) * NB + b] - P.chin[(size_t)h * NB + b] * P.nuf[(size_t)g * NB + b] * invKe;
       }
-      B[g][h] = fac * dum;
+      B[g][h] = fac[g] * dum;
     }
   }
 }
 
-// Constants A,B,E,F,G,H of node b in direction u.
-template <int NG>
-__device__ __forceinline__ void get_consts(const NodalParams& P, int u, int b, double (&K)[6][NG]) {
+// Constant k (0..5 = A,B,E,F,G,H) of node b, direction u, group g.
+__device__ __forceinline__ double nconst(const NodalParams& P, int u, int k, int g, int b) {
   if (P.pnm) {
     double c[6];
     pnm_consts(c);
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-#pragma unroll
-      for (int g = 0; g < NG; ++g) K[k][g] = c[k];
-    return;
+    return c[k];
   }
-  const size_t st = (size_t)NG * P.G.NB;
-  const double* src = P.sanm + (size_t)u * 6 * st + b;
-#pragma unroll
-  for (int k = 0; k < 6; ++k)
-#pragma unroll
-    for (int g = 0; g < NG; ++g) K[k][g] = src[k * st + (size_t)g * P.G.NB];
+  return P.sanm[(((size_t)u * 6 + k) * P.ng + g) * P.G.NB + b];
+}
+
+__device__ __forceinline__ double bc_at(const NodalParams& P, int u, int g, int h, int b) {
+  return P.Bc[(((size_t)u * P.ng + g) * P.ng + h) * P.G.NB + b];
 }
 
 // LU_solve (mod_nodal.f90:829-897): Doolittle elimination without pivoting,
-// L stored in place of the eliminated entries.  Returns false when an input
-// diagonal is below the reference's 10e-5 (single precision) threshold.
+// L stored in place of the eliminated entries, one reciprocal per pivot.
+// Returns false when an input diagonal is below the reference's 10e-5
+// (single precision) threshold.
 template <int M>
 __device__ __forceinline__ bool lu_solve(double (&U)[M][M], double (&x)[M]) {
 #pragma unroll
   for (int i = 0; i < M; ++i)
     if (fabs(U[i][i]) < kF1em4) return false;
+  double inv[M];
 #pragma unroll
   for (int i = 0; i < M; ++i) {
+    inv[i] = 1.0 / U[i][i];
 #pragma unroll
     for (int j = i + 1; j < M; ++j) {
-      const double piv = U[j][i] / U[i][i];
+      const double piv = U[j][i] * inv[i];
 #pragma unroll
       for (int k = i + 1; k < M; ++k) U[j][k] = U[j][k] - piv * U[i][k];
       U[j][i] = piv;
     }
   }
-  // forward substitution (unit lower), x holds b on entry
 #pragma unroll
   for (int i = 1; i < M; ++i) {
     double isum = 0.0;
@@ -287,13 +253,13 @@ __device__ __forceinline__ bool lu_solve(double (&U)[M][M], double (&x)[M]) {
     for (int k = 0; k < i; ++k) isum = isum + U[i][k] * x[k];
     x[i] = x[i] - isum;
   }
-  x[M - 1] = x[M - 1] / U[M - 1][M - 1];
+  x[M - 1] = x[M - 1] * inv[M - 1];
 #pragma unroll
   for (int i = M - 2; i >= 0; --i) {
     double isum = 0.0;
 #pragma unroll
     for (int k = i + 1; k < M; ++k) isum = isum + U[i][k] * x[k];
-    x[i] = (x[i] - isum) / U[i][i];
+    x[i] = (x[i] - isum) * inv[i];
   }
   return true;
 }
@@ -303,35 +269,48 @@ __device__ __forceinline__ void record_error(OuterCtl* C, int code, int b) {
 }
 
 // ---------------------------------------------------------------------------
-// Per node and direction: a2 (get_a2matvec + LU_solve), a4 (get_a4) and the
-// first transverse-leakage moment (TLUpd1).
+// Per node and direction: the buckling matrix (stored for k_interface),
+// a2 (get_a2matvec + LU_solve), a4 (get_a4) and the first transverse-leakage
+// moment (TLUpd1).
 // ---------------------------------------------------------------------------
 template <int NG>
-__global__ void k_node_prep(NodalParams P) {
+__global__ void __launch_bounds__(128) k_node_prep(NodalParams P) {
   const BoxGeom& G = P.G;
   const int NB = G.NB;
   const double* phi = latest_phi(P);
-  const double Ke = P.ctl->Ke;
+  const double invKe = 1.0 / P.ctl->Ke;
   const int total = P.nnod * 3;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const int n = q % P.nnod, u = q / P.nnod;
     const int b = P.act[n];
-    double Bc[NG][NG], K[6][NG];
-    get_B<NG>(P, u, b, Ke, Bc);
-    get_consts<NG>(P, u, b, K);
     const double h = hdir(G, u, b);
+    double fac[NG];
+#pragma unroll
+    for (int g = 0; g < NG; ++g) fac[g] = 0.25 * (h * h) / P.D[(size_t)g * NB + b];
+    double Bc[NG][NG];
+    get_B<NG>(P, b, invKe, fac, Bc);
+#pragma unroll
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+      for (int hh = 0; hh < NG; ++hh) P.Bc[(((size_t)u * NG + g) * NG + hh) * NB + b] = Bc[g][hh];
+    const TLGeom T = tl_geom(G, u, b);
+    const double* S = P.S + (size_t)u * NG * NB;
     double M[NG][NG], rhs[NG], Lm2[NG];
 #pragma unroll
     for (int g = 0; g < NG; ++g) {
-      const double Sv = 0.25 * (h * h) / P.D[(size_t)g * NB + b] * P.S[((size_t)u * NG + g) * NB + b];
+      const double Ev = nconst(P, u, 2, g, b);
+      const double Sn = S[(size_t)g * NB + b];
+      const double dSp = T.has_p ? S[(size_t)g * NB + b + T.offp] - Sn : 0.0;
+      const double dSm = T.has_m ? S[(size_t)g * NB + b - T.offp] - Sn : 0.0;
       double Bf = 0.0;
 #pragma unroll
       for (int hh = 0; hh < NG; ++hh) {
-        M[g][hh] = (hh == g) ? Bc[g][hh] * K[2][g] + 3.0 : Bc[g][hh] * K[2][g];
+        M[g][hh] = (hh == g) ? Bc[g][hh] * Ev + 3.0 : Bc[g][hh] * Ev;
         Bf = Bf + Bc[g][hh] * phi[(size_t)hh * P.NBH + b];
       }
-      Lm2[g] = tlupd2(P, u, b, g);
-      rhs[g] = Bf - K[2][g] * Lm2[g] + Sv;
+      Lm2[g] = fac[g] * (T.c2p * dSp + T.c2m * dSm);                          // TLUpd2
+      rhs[g] = Bf - Ev * Lm2[g] + fac[g] * Sn;
+      P.L1[((size_t)u * NG + g) * NB + b] = fac[g] * (T.c1p * dSp - T.c1m * dSm);  // TLUpd1
     }
     if (!lu_solve<NG>(M, rhs)) {
       record_error(P.ctl, ADP_ERR_PIVOT, b);
@@ -344,36 +323,8 @@ __global__ void k_node_prep(NodalParams P) {
       for (int hh = 0; hh < NG; ++hh) Bf = Bf + Bc[g][hh] * rhs[hh];
       const size_t o = ((size_t)u * NG + g) * NB + b;
       P.a2[o] = rhs[g];
-      P.a4[o] = K[1][g] * (Bf + Lm2[g]);
-      P.L1[o] = tlupd1(P, u, b, g);
+      P.a4[o] = nconst(P, u, 1, g, b) * (Bf + Lm2[g]);
     }
-  }
-}
-
-// Per-node data used on both sides of an interface.
-template <int NG>
-struct NodeSide {
-  double Bc[NG][NG];
-  double K[6][NG];   // A,B,E,F,G,H
-  double a2[NG], a4[NG], L1[NG], f[NG], D[NG];
-  double h;
-};
-
-template <int NG>
-__device__ __forceinline__ void load_side(const NodalParams& P, int u, int b, double Ke, const double* phi,
-                                          NodeSide<NG>& S) {
-  const int NB = P.G.NB;
-  get_B<NG>(P, u, b, Ke, S.Bc);
-  get_consts<NG>(P, u, b, S.K);
-  S.h = hdir(P.G, u, b);
-#pragma unroll
-  for (int g = 0; g < NG; ++g) {
-    const size_t o = ((size_t)u * NG + g) * NB + b;
-    S.a2[g] = P.a2[o];
-    S.a4[g] = P.a4[o];
-    S.L1[g] = P.L1[o];
-    S.f[g] = phi[(size_t)g * P.NBH + b];
-    S.D[g] = P.D[(size_t)g * NB + b];
   }
 }
 
@@ -391,17 +342,39 @@ __device__ __forceinline__ void nd_consider(NdBest& best, double val, long long 
   }
 }
 
+// Per-node, per-direction, per-group quantities of one side of a face.
+struct Side {
+  double A, F, Gc, H, a2, a4, L1, f, D;
+};
+
+__device__ __forceinline__ Side side_at(const NodalParams& P, const double* phi, int u, int g, int b) {
+  const int NB = P.G.NB;
+  const size_t o = ((size_t)u * P.ng + g) * NB + b;
+  Side s;
+  s.A = nconst(P, u, 0, g, b);
+  s.F = nconst(P, u, 3, g, b);
+  s.Gc = nconst(P, u, 4, g, b);
+  s.H = nconst(P, u, 5, g, b);
+  s.a2 = P.a2[o];
+  s.a4 = P.a4[o];
+  s.L1 = P.L1[o];
+  s.f = phi[(size_t)g * P.NBH + b];
+  s.D = P.D[(size_t)g * NB + b];
+  return s;
+}
+
 // ---------------------------------------------------------------------------
 // Per node and direction: the minus face of the node (the interior
 // interface with its predecessor, or the first boundary face of the line),
-// plus the last boundary face when the node ends its line.
+// plus the last boundary face when the node ends its line.  Per-node
+// quantities are read from memory where they are used, to keep the 2G x 2G
+// system in registers.
 // ---------------------------------------------------------------------------
 template <int NG>
-__global__ void k_interface(NodalParams P) {
+__global__ void __launch_bounds__(128) k_interface(NodalParams P) {
   const BoxGeom& G = P.G;
   const int NB = G.NB;
   const double* phi = latest_phi(P);
-  const double Ke = P.ctl->Ke;
   NdBest best{0.0, 0x7fffffffffffffffLL, -1};
   const int total = P.nnod * 3;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
@@ -410,68 +383,52 @@ __global__ void k_interface(NodalParams P) {
     const LinePos L = line_pos(G, u, b);
     const int sf = 2 * u;         // plus face of u (X+, Y+, Z+); sf+1 is the minus face
     const long long ev = P.evbase[(size_t)u * NB + b];
-    NodeSide<NG> Sp;
-    load_side<NG>(P, u, b, Ke, phi, Sp);
+    const double two_hp = 2.0 / hdir(G, u, b);
     if (!L.first) {
       // interior interface n = predecessor, p = b (get_coefs + get_a1matvec)
       const int bn = b - L.offp;
-      NodeSide<NG> Sn;
-      load_side<NG>(P, u, bn, Ke, phi, Sn);
+      const double two_hn = 2.0 / hdir(G, u, bn);
       double R[2 * NG][2 * NG], x[2 * NG];
-      double Pn[NG], Pp[NG];
 #pragma unroll
       for (int g = 0; g < NG; ++g) {
-        Pn[g] = 2.0 * Sn.D[g] / Sn.h;
-        Pp[g] = 2.0 * Sp.D[g] / Sp.h;
-#pragma unroll
-        for (int hh = 0; hh < NG; ++hh) {
-          if (hh == g) {
-            R[g][g] = -Pn[g] * (Sn.Bc[g][hh] * Sn.K[3][g] + 1.0);
-            R[g][g + NG] = Pp[g] * (Sp.Bc[g][hh] * Sp.K[3][g] + 1.0);
-          } else {
-            R[g][hh] = -Pn[g] * Sn.Bc[g][hh] * Sn.K[3][g];
-            R[g][hh + NG] = Pp[g] * Sp.Bc[g][hh] * Sp.K[3][g];
-          }
-        }
-        x[g] = Pn[g] * (3.0 * Sn.a2[g] + Sn.K[4][g] * Sn.a4[g] + Sn.K[3][g] * Sn.L1[g]) +
-               Pp[g] * (3.0 * Sp.a2[g] + Sp.K[4][g] * Sp.a4[g] - Sp.K[3][g] * Sp.L1[g]);
-      }
-#pragma unroll
-      for (int g = 0; g < NG; ++g) {
+        const Side sn = side_at(P, phi, u, g, bn), sp = side_at(P, phi, u, g, b);
+        const double Pn = sn.D * two_hn, Pp = sp.D * two_hp;
         const double dcn = P.dc[((size_t)g * 6 + sf) * NB + bn];
         const double dcp = P.dc[((size_t)g * 6 + sf + 1) * NB + b];
 #pragma unroll
         for (int hh = 0; hh < NG; ++hh) {
+          const double Bn = bc_at(P, u, g, hh, bn), Bp = bc_at(P, u, g, hh, b);
           if (hh == g) {
-            R[g + NG][g] = dcn * (Sn.Bc[g][hh] * Sn.K[0][g] + 1.0);
-            R[g + NG][g + NG] = dcp * (Sp.Bc[g][hh] * Sp.K[0][g] + 1.0);
+            R[g][g] = -Pn * (Bn * sn.F + 1.0);
+            R[g][g + NG] = Pp * (Bp * sp.F + 1.0);
+            R[g + NG][g] = dcn * (Bn * sn.A + 1.0);
+            R[g + NG][g + NG] = dcp * (Bp * sp.A + 1.0);
           } else {
-            R[g + NG][hh] = dcn * Sn.Bc[g][hh] * Sn.K[0][g];
-            R[g + NG][hh + NG] = dcp * Sp.Bc[g][hh] * Sp.K[0][g];
+            R[g][hh] = -Pn * Bn * sn.F;
+            R[g][hh + NG] = Pp * Bp * sp.F;
+            R[g + NG][hh] = dcn * Bn * sn.A;
+            R[g + NG][hh + NG] = dcp * Bp * sp.A;
           }
         }
+        x[g] = Pn * (3.0 * sn.a2 + sn.Gc * sn.a4 + sn.F * sn.L1) + Pp * (3.0 * sp.a2 + sp.Gc * sp.a4 - sp.F * sp.L1);
         // ADF pairing of mod_nodal.f90:693-694 kept as written there
-        x[g + NG] = dcp * (Sp.a2[g] + Sp.a4[g] + Sp.f[g] - Sn.K[0][g] * Sn.L1[g]) -
-                    dcn * (Sn.a2[g] + Sn.a4[g] + Sn.f[g] + Sp.K[0][g] * Sp.L1[g]);
+        x[g + NG] = dcp * (sp.a2 + sp.a4 + sp.f - sn.A * sn.L1) - dcn * (sn.a2 + sn.a4 + sn.f + sp.A * sp.L1);
       }
       if (!lu_solve<2 * NG>(R, x)) {
         record_error(P.ctl, ADP_ERR_PIVOT, bn);
       } else {
-        double a3[NG];
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
+          const Side sn = side_at(P, phi, u, g, bn);
+          const double fp = phi[(size_t)g * P.NBH + b];
           double Bf = 0.0;
 #pragma unroll
-          for (int hh = 0; hh < NG; ++hh) Bf = Bf + Sn.Bc[g][hh] * x[hh];
-          a3[g] = Sn.K[0][g] * (Bf + Sn.L1[g]);
-        }
-#pragma unroll
-        for (int g = 0; g < NG; ++g) {
-          const double jp = -2.0 * Sn.D[g] / Sn.h *
-                            (x[g] + 3.0 * Sn.a2[g] + Sn.K[5][g] * a3[g] + Sn.K[4][g] * Sn.a4[g]);
+          for (int hh = 0; hh < NG; ++hh) Bf = Bf + bc_at(P, u, g, hh, bn) * x[hh];
+          const double a3 = sn.A * (Bf + sn.L1);
+          const double jp = -sn.D * two_hn * (x[g] + 3.0 * sn.a2 + sn.H * a3 + sn.Gc * sn.a4);
           const size_t on = ((size_t)g * 6 + sf) * NB + bn;
           const double ndpr = P.dn[on];
-          const double dnew = (P.df[on] * (Sn.f[g] - Sp.f[g]) - jp) / (Sn.f[g] + Sp.f[g]);
+          const double dnew = (P.df[on] * (sn.f - fp) - jp) / (sn.f + fp);
           P.dn[on] = dnew;
           P.dn[((size_t)g * 6 + sf + 1) * NB + b] = dnew;
           nd_consider(best, fabs(dnew - ndpr), ev * NG + g, bn);
@@ -483,36 +440,37 @@ __global__ void k_interface(NodalParams P) {
       double A[NG][NG], x[NG];
 #pragma unroll
       for (int g = 0; g < NG; ++g) {
-        const double Pp = 2.0 * Sp.D[g] / Sp.h;
+        const Side sp = side_at(P, phi, u, g, b);
+        const double Pp = sp.D * two_hp;
         const double dcv = P.dc[((size_t)g * 6 + sf + 1) * NB + b];
-        const double Ap = Sp.K[0][g], Fp = Sp.K[3][g], Gp = Sp.K[4][g], Hp = Sp.K[5][g];
-        const double a2 = Sp.a2[g], a4 = Sp.a4[g], L1 = Sp.L1[g], fv = Sp.f[g];
 #pragma unroll
         for (int hh = 0; hh < NG; ++hh) {
-          const double Bc = Sp.Bc[g][hh];
-          if (bc == 2) A[g][hh] = (hh == g) ? Pp * (Bc * Fp + 1.0) : Pp * Bc * Fp;
+          const double Bc = bc_at(P, u, g, hh, b);
+          if (bc == 2) A[g][hh] = (hh == g) ? Pp * (Bc * sp.F + 1.0) : Pp * Bc * sp.F;
           else if (bc == 1)
-            A[g][hh] = (hh == g) ? -dcv * (1.0 + Ap * Bc) - 2.0 * Pp * (Ap * Bc * Hp + 1.0)
-                                 : -dcv * Ap * Bc - 2.0 * Pp * Ap * Bc * Hp;
-          else A[g][hh] = (hh == g) ? dcv * (1.0 + Ap * Bc) : dcv * Ap * Bc;
+            A[g][hh] = (hh == g) ? -dcv * (1.0 + sp.A * Bc) - 2.0 * Pp * (sp.A * Bc * sp.H + 1.0)
+                                 : -dcv * sp.A * Bc - 2.0 * Pp * sp.A * Bc * sp.H;
+          else A[g][hh] = (hh == g) ? dcv * (1.0 + sp.A * Bc) : dcv * sp.A * Bc;
         }
-        if (bc == 2) x[g] = Pp * (3.0 * a2 + Gp * a4 - Fp * L1);
-        else if (bc == 1) x[g] = 2.0 * Pp * (Ap * Hp * L1 - 3.0 * a2 - Gp * a4) - dcv * (a2 + a4 + fv - Ap * L1);
-        else x[g] = dcv * (a2 + a4 + fv - Ap * L1);
+        if (bc == 2) x[g] = Pp * (3.0 * sp.a2 + sp.Gc * sp.a4 - sp.F * sp.L1);
+        else if (bc == 1)
+          x[g] = 2.0 * Pp * (sp.A * sp.H * sp.L1 - 3.0 * sp.a2 - sp.Gc * sp.a4) - dcv * (sp.a2 + sp.a4 + sp.f - sp.A * sp.L1);
+        else x[g] = dcv * (sp.a2 + sp.a4 + sp.f - sp.A * sp.L1);
       }
       if (!lu_solve<NG>(A, x)) {
         record_error(P.ctl, ADP_ERR_PIVOT, b);
       } else {
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
+          const Side sp = side_at(P, phi, u, g, b);
           double Bf = 0.0;
 #pragma unroll
-          for (int hh = 0; hh < NG; ++hh) Bf = Bf + Sp.Bc[g][hh] * x[hh];
-          const double a3 = Sp.K[0][g] * (Bf + Sp.L1[g]);
-          const double jp = -2.0 * Sp.D[g] / Sp.h * (x[g] - 3.0 * Sp.a2[g] + Sp.K[5][g] * a3 - Sp.K[4][g] * Sp.a4[g]);
+          for (int hh = 0; hh < NG; ++hh) Bf = Bf + bc_at(P, u, g, hh, b) * x[hh];
+          const double a3 = sp.A * (Bf + sp.L1);
+          const double jp = -sp.D * two_hp * (x[g] - 3.0 * sp.a2 + sp.H * a3 - sp.Gc * sp.a4);
           const size_t op = ((size_t)g * 6 + sf + 1) * NB + b;
           const double ndpr = P.dn[op];
-          const double dnew = -(jp / Sp.f[g] + P.df[op]);
+          const double dnew = -(jp / sp.f + P.df[op]);
           P.dn[op] = dnew;
           nd_consider(best, fabs(dnew - ndpr), ev * NG + g, b);
         }
@@ -524,36 +482,37 @@ __global__ void k_interface(NodalParams P) {
       double A[NG][NG], x[NG];
 #pragma unroll
       for (int g = 0; g < NG; ++g) {
-        const double Pn = 2.0 * Sp.D[g] / Sp.h;
+        const Side sn = side_at(P, phi, u, g, b);
+        const double Pn = sn.D * two_hp;
         const double dcv = P.dc[((size_t)g * 6 + sf) * NB + b];
-        const double An = Sp.K[0][g], Fn = Sp.K[3][g], Gn = Sp.K[4][g], Hn = Sp.K[5][g];
-        const double a2 = Sp.a2[g], a4 = Sp.a4[g], L1 = Sp.L1[g], fv = Sp.f[g];
 #pragma unroll
         for (int hh = 0; hh < NG; ++hh) {
-          const double Bc = Sp.Bc[g][hh];
-          if (bc == 2) A[g][hh] = (hh == g) ? -Pn * (Bc * Fn + 1.0) : -Pn * Bc * Fn;
+          const double Bc = bc_at(P, u, g, hh, b);
+          if (bc == 2) A[g][hh] = (hh == g) ? -Pn * (Bc * sn.F + 1.0) : -Pn * Bc * sn.F;
           else if (bc == 1)
-            A[g][hh] = (hh == g) ? dcv * (1.0 + An * Bc) + 2.0 * Pn * (An * Bc * Hn + 1.0)
-                                 : dcv * An * Bc + 2.0 * Pn * An * Bc * Hn;
-          else A[g][hh] = (hh == g) ? dcv * (1.0 + An * Bc) : dcv * An * Bc;
+            A[g][hh] = (hh == g) ? dcv * (1.0 + sn.A * Bc) + 2.0 * Pn * (sn.A * Bc * sn.H + 1.0)
+                                 : dcv * sn.A * Bc + 2.0 * Pn * sn.A * Bc * sn.H;
+          else A[g][hh] = (hh == g) ? dcv * (1.0 + sn.A * Bc) : dcv * sn.A * Bc;
         }
-        if (bc == 2) x[g] = Pn * (3.0 * a2 + Gn * a4 + Fn * L1);
-        else if (bc == 1) x[g] = -2.0 * Pn * (An * Hn * L1 + 3.0 * a2 + Gn * a4) - dcv * (a2 + a4 + fv + An * L1);
-        else x[g] = -dcv * (a2 + a4 + fv + An * L1);
+        if (bc == 2) x[g] = Pn * (3.0 * sn.a2 + sn.Gc * sn.a4 + sn.F * sn.L1);
+        else if (bc == 1)
+          x[g] = -2.0 * Pn * (sn.A * sn.H * sn.L1 + 3.0 * sn.a2 + sn.Gc * sn.a4) - dcv * (sn.a2 + sn.a4 + sn.f + sn.A * sn.L1);
+        else x[g] = -dcv * (sn.a2 + sn.a4 + sn.f + sn.A * sn.L1);
       }
       if (!lu_solve<NG>(A, x)) {
         record_error(P.ctl, ADP_ERR_PIVOT, b);
       } else {
 #pragma unroll
         for (int g = 0; g < NG; ++g) {
+          const Side sn = side_at(P, phi, u, g, b);
           double Bf = 0.0;
 #pragma unroll
-          for (int hh = 0; hh < NG; ++hh) Bf = Bf + Sp.Bc[g][hh] * x[hh];
-          const double a3 = Sp.K[0][g] * (Bf + Sp.L1[g]);
-          const double jp = -2.0 * Sp.D[g] / Sp.h * (x[g] + 3.0 * Sp.a2[g] + Sp.K[5][g] * a3 + Sp.K[4][g] * Sp.a4[g]);
+          for (int hh = 0; hh < NG; ++hh) Bf = Bf + bc_at(P, u, g, hh, b) * x[hh];
+          const double a3 = sn.A * (Bf + sn.L1);
+          const double jp = -sn.D * two_hp * (x[g] + 3.0 * sn.a2 + sn.H * a3 + sn.Gc * sn.a4);
           const size_t on = ((size_t)g * 6 + sf) * NB + b;
           const double ndpr = P.dn[on];
-          const double dnew = -(jp / Sp.f[g] - P.df[on]);
+          const double dnew = -(jp / sn.f - P.df[on]);
           P.dn[on] = dnew;
           nd_consider(best, fabs(dnew - ndpr), (ev + 1) * NG + g, b);
         }

@@ -145,8 +145,11 @@ def _mat4(D, sa, nuf, ss, chi):
     return rows
 
 
-def core_4g(seed=0, nout=2000):
-    """17x17 assemblies of 4x4 nodes, 80 planes of 5 cm, 4 groups, down-scatter only."""
+def core_4g(seed=0, nout=2000, planes=80):
+    """17x17 assemblies of 4x4 nodes, 80 planes of 5 cm, 4 groups, down-scatter only.
+
+    planes = 80 / zdiv with zdiv in {1, 2, 4} gives the same core with coarser
+    axial nodes (used for smaller profiling cases)."""
     rng = np.random.default_rng(2000 + seed)
     D = np.geomspace(2.0, 0.35, 4)
     chi = (0.75, 0.25, 0.0, 0.0)
@@ -171,10 +174,13 @@ def core_4g(seed=0, nout=2000):
     fuel = _circle_outline(n, 7.2)
     types = rng.integers(0, 3, size=(n, n))
     pl = np.where(fuel, 2 + types, 1)
+    zdiv = planes // 20
+    if zdiv not in (1, 2, 4) or zdiv * 20 != planes:
+        raise ValueError("planes must be 20, 40 or 80")
     nxx = nyy = 68
-    nzz = 80
+    nzz = planes
     it = [nout, 2, "1.0e-5", "1.0e-5", 5, _nupd(nxx, nyy, nzz), 30, 20]
-    return _deck("CORE4G", 4, mats, n, n, 20, [20.0] * n, [4] * n, [20.0] * n, [4] * n, [20.0] * 20, [4] * 20,
+    return _deck("CORE4G", 4, mats, n, n, 20, [20.0] * n, [4] * n, [20.0] * n, [4] * n, [20.0] * 20, [zdiv] * 20,
                  [pl], [1] * 20, (1, 1, 1, 1, 1, 1), iter_=it)
 
 

@@ -23,9 +23,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "adpres_oracle.cpp")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD_DIR, "libadpres_oracle.so")
-# Variant used only to measure how sensitive a deck is to rounding: the same
-# source with multiply-add contraction allowed (FMA on both x86-64 and Arm).
+# Variants used only to measure how sensitive a deck is to rounding:
+#   "fma"       the same source with multiply-add contraction (FMA on x86-64 and Arm);
+#   "fma_rhost" also forming BiCGSTAB's (rs, r) as (rs,s) - omega (rs,t), an
+#               algebraically equal evaluation that the CUDA path uses.
 LIB_FMA = os.path.join(BUILD_DIR, "libadpres_oracle_fma.so")
+VARIANTS = {
+    "plain": (LIB, ["-ffp-contract=off"]),
+    "fma": (LIB_FMA, ["-ffp-contract=fast"]),
+    "fma_rhost": (os.path.join(BUILD_DIR, "libadpres_oracle_fma_rhost.so"),
+                  ["-ffp-contract=fast", "-DORA_RHO_FROM_S_T"]),
+}
 
 # Status codes (same meaning as the product's adp_status values).
 ORA_OK = 0
@@ -42,19 +50,17 @@ def build(force: bool = False, variant: str = "plain") -> str:
     """Compile the restatement with g++ into _build/.
 
     variant "plain" (the oracle): no multiply-add contraction, as the
-    reference's gfortran build for x86-64 has none.  variant "fma": the same
-    source with contraction, used only to measure rounding sensitivity.
+    reference's gfortran build for x86-64 has none.  The other VARIANTS are
+    used only to measure rounding sensitivity.
     """
     os.makedirs(BUILD_DIR, exist_ok=True)
-    lib_path = LIB if variant == "plain" else LIB_FMA
+    lib_path, fp = VARIANTS[variant]
     if (not force and os.path.exists(lib_path)
             and os.path.getmtime(lib_path) >= os.path.getmtime(SRC)):
         return lib_path
     tmp = lib_path + ".tmp.%d" % os.getpid()
-    if variant == "plain":
-        fp = ["-ffp-contract=off"]
-    else:
-        fp = ["-ffp-contract=fast"] + (["-mfma"] if platform.machine() in ("x86_64", "AMD64") else [])
+    if variant != "plain" and platform.machine() in ("x86_64", "AMD64"):
+        fp = fp + ["-mfma"]
     cmd = ["g++", "-O2", "-std=c++17"] + fp + ["-fno-fast-math", "-fPIC", "-shared", SRC, "-o", tmp]
     subprocess.run(cmd, check=True)
     os.replace(tmp, lib_path)

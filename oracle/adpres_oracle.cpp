@@ -775,9 +775,19 @@ static void bicg(Ora& o, int imax, int g, const std::vector<double>& b, double* 
   for (int n = 0; n < N; ++n) r[n] = b[n] - tmp[n];
   rs = r;
   double rho = 1.0, alpha = 1.0, omega = 1.0, rho_prev, beta, theta;
+#ifdef ORA_RHO_FROM_S_T
+  // Sensitivity build only: (rs, r) of the next step formed as
+  // (rs,s) - omega (rs,t), algebraically equal to dproduct(rs, r) of
+  // mod_cmfd.f90:1230, the way the CUDA path evaluates it.
+  double rho_next = dproduct(rs, r);
+#endif
   for (int i = 1; i <= imax; ++i) {
     rho_prev = rho;
+#ifdef ORA_RHO_FROM_S_T
+    rho = rho_next;
+#else
     rho = dproduct(rs, r);
+#endif
     beta = (rho / rho_prev) * (alpha / omega);
     for (int n = 0; n < N; ++n) p[n] = r[n] + beta * (p[n] - omega * v[n]);
     sp_matvec(o, g, p.data(), v.data());
@@ -786,6 +796,9 @@ static void bicg(Ora& o, int imax, int g, const std::vector<double>& b, double* 
     sp_matvec(o, g, s.data(), t.data());
     theta = dproduct(t, t);
     omega = dproduct(t, s) / theta;
+#ifdef ORA_RHO_FROM_S_T
+    rho_next = dproduct(rs, s) - omega * dproduct(rs, t);
+#endif
     for (int n = 0; n < N; ++n) x[n] = x[n] + alpha * p[n] + omega * s[n];
     for (int n = 0; n < N; ++n) r[n] = s[n] - omega * t[n];
   }

@@ -77,17 +77,18 @@ def test_sample_decks_match_oracle(name):
     """End point at the full bar (k within 0.1 pcm; power within 1e-6, or
     within 4x the reference algorithm's own rounding sensitivity on the deck
     when that is larger).  The fixture records that sensitivity: the oracle
-    rebuilt with multiply-add contraction, against itself.  Where it changes
-    the outer count (FDM, FDM-1D: the BiCGSTAB/extrapolation iteration is
-    chaotic at rounding level) the outer count and trajectory are not
-    compared; elsewhere they must agree."""
+    rebuilt with multiply-add contraction, and with BiCGSTAB's (rs, r) formed
+    as (rs,s) - omega (rs,t), against the oracle.  Where either changes the
+    outer count (FDM, FDM-1D: the BiCGSTAB/extrapolation iteration is chaotic
+    at rounding level; DVP: ser/fer hover at the 1e-5 threshold) the outer
+    count and trajectory are not compared; elsewhere they must agree."""
     fx = fixture(name)
     c = core_from_fixture(fx)
     adj = bool(int(fx["adjoint"]))
     rep = c.outer(adjoint=adj, popt=1)
     assert rep.converged
     assert pcm(rep.keff, float(fx["out_k"])) <= KTOL_PCM
-    stable = int(fx["sens_outers"]) == int(fx["out_outers"])
+    stable = bool(np.all(np.atleast_1d(fx["sens_outers"]) == int(fx["out_outers"])))
     if stable:
         assert rep.outers == int(fx["out_outers"])
         n = rep.outers
