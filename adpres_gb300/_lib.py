@@ -32,7 +32,7 @@ STATUS_NAMES = {
     9: "ADP_ERR_NAN", 10: "ADP_ERR_BREAKDOWN", 11: "ADP_ERR_TIMEOUT", 12: "ADP_ERR_STATE",
 }
 
-ADP_FORWARD, ADP_ADJOINT = 0, 1
+ADP_FORWARD, ADP_ADJOINT, ADP_FROZEN_DN = 0, 1, 4
 ADP_KERN_FDM, ADP_KERN_PNM, ADP_KERN_SANM = 0, 1, 2
 ADP_FP64, ADP_MIXED = 0, 1
 
@@ -65,7 +65,7 @@ class AdpTimers(ctypes.Structure):
     _fields_ = [("outer_kernel_ms", ctypes.c_double), ("outer_kernel_launches", ctypes.c_long),
                 ("nodal_ms", ctypes.c_double), ("nodal_updates", ctypes.c_long), ("other_ms", ctypes.c_double),
                 ("outers", ctypes.c_long), ("bicg_rows", ctypes.c_long), ("grid_blocks", ctypes.c_int),
-                ("block_threads", ctypes.c_int)]
+                ("block_threads", ctypes.c_int), ("adjoint_ms", ctypes.c_double), ("adjoint_outers", ctypes.c_long)]
 
 
 # Every entry point declared in include/adpres_gb300.h, with its ctypes signature.
@@ -83,6 +83,7 @@ SIGNATURES = {
     "adp_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "adp_power_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "adp_adjoint_sens": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _dp, _dp, ctypes.POINTER(AdpReport)]),
     "adp_get_timers": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpTimers)]),
     "adp_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }

@@ -127,22 +127,47 @@ class Core:
         self._check(self.L.adp_set_xs(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
 
     # -- solver -------------------------------------------------------------
-    def outer(self, adjoint=False, popt=1, trace=True) -> Report:
+    def _report(self, trace):
         cap = self.nout if trace else 0
-        tk, ts, tf, tn = (np.zeros(cap) for _ in range(4))
-        tfl = np.zeros(cap, dtype=np.int32)
+        bufs = [np.zeros(cap) for _ in range(4)] + [np.zeros(cap, dtype=np.int32)]
         rep = _lib.AdpReport()
         rep.trace_cap = cap
         if cap:
-            rep.trace_k, rep.trace_ser, rep.trace_fer, rep.trace_ndmax = dptr(tk), dptr(ts), dptr(tf), dptr(tn)
-            rep.trace_flags = iptr(tfl)
-        st = self.L.adp_outer(self.h, int(bool(adjoint)), int(popt), ctypes.byref(rep))
-        n = min(rep.outers, cap)
-        self.last_report = Report(rep.outers, bool(rep.converged), rep.nodal_updates, rep.keff, rep.ser, rep.fer,
-                                  rep.ndmax, (rep.im, rep.jm, rep.km), tk[:n], ts[:n], tf[:n], tfl[:n], tn[:n],
-                                  rep.device_ms)
+            rep.trace_k, rep.trace_ser, rep.trace_fer, rep.trace_ndmax = (dptr(b) for b in bufs[:4])
+            rep.trace_flags = iptr(bufs[4])
+        return rep, bufs
+
+    @staticmethod
+    def _to_report(rep, bufs):
+        n = min(rep.outers, rep.trace_cap)
+        tk, ts, tf, tn, tfl = bufs
+        return Report(rep.outers, bool(rep.converged), rep.nodal_updates, rep.keff, rep.ser, rep.fer, rep.ndmax,
+                      (rep.im, rep.jm, rep.km), tk[:n], ts[:n], tf[:n], tfl[:n], tn[:n], rep.device_ms)
+
+    def outer(self, adjoint=False, popt=1, trace=True, frozen_dn=False) -> Report:
+        """outer(popt) / outer_ad(popt); frozen_dn keeps dn fixed (no nodal update)."""
+        rep, bufs = self._report(trace)
+        mode = int(bool(adjoint)) | (_lib.ADP_FROZEN_DN if frozen_dn else 0)
+        st = self.L.adp_outer(self.h, mode, int(popt), ctypes.byref(rep))
+        self.last_report = self._to_report(rep, bufs)
         self._check(st)
         return self.last_report
+
+    def adjoint_sens(self, tol=0.0, trace=False):
+        """Discrete adjoint at frozen dn and dk/dSigma after a converged forward outer.
+
+        Returns (dkdp (nnod, ng, 4 + ng), psi (nnod, ng), Report of the adjoint
+        solve); dkdp[:, g, c] for c = 0 D, 1 siga, 2 nuf, 3 sigtr, 4 + h sigs(g->h).
+        """
+        nn, G = self.nnod, self.ng
+        dk = np.zeros(nn * G * (4 + G))
+        psi = np.zeros(nn * G)
+        rep, bufs = self._report(trace)
+        st = self.L.adp_adjoint_sens(self.h, float(tol), dptr(dk), dptr(psi), ctypes.byref(rep))
+        r = self._to_report(rep, bufs)
+        self.last_adjoint_ms = rep.device_ms
+        self._check(st)
+        return dk.reshape((nn, G, 4 + G), order="F"), psi.reshape((nn, G), order="F"), r
 
     def state(self):
         """(f0 (nnod,ng), fs0 (nnod,), keff, dn (nnod,ng,6)) in the reference layouts."""

@@ -1,0 +1,151 @@
+// Discrete adjoint of the converged forward CMFD eigenproblem and the
+// sensitivity of k to every node's cross sections.
+//
+// With the nodal coupling coefficients dn frozen at the converged forward
+// state, the CMFD equations (matrix_setup + TSrc, mod_cmfd.f90:217-304,
+// :1006-1033) are the generalized eigenproblem
+//     M phi = (1/k) F phi,
+//     (M phi)_g = A_g phi_g - sum_{h/=g} sigs(h->g) phi_h,
+//     (F phi)_g = chi_g sum_h nuf_h phi_h.
+// Its discrete adjoint M^T psi = (1/k) F^T psi has the source structure of
+// outer_ad / TSrcAd (mod_cmfd.f90:602-699, :1037-1064) with the transposed
+// stencil A_g^T, so it is solved by the same persistent kernel given A^T.
+// Then, for a parameter p of node n,
+//     dk/dp = k^2 psi^T (lambda dF/dp - dM/dp) phi / (psi^T F phi),  lambda = 1/k.
+// The reference has no sensitivity edit; its closest relative is the
+// adjoint-weighted reactivity of mod_trans.f90:648-688.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "adp_kernels.h"
+
+namespace adp {
+
+// A^T in the same 7-slot layout: the coefficient of x[b + off_c] in row b of
+// A^T is the coefficient of x[b] in row b + off_c of A, i.e. that row's
+// opposite slot.
+__global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, float* AT32) {
+  const int NB = G.NB;
+  const long long total = (long long)NB * ng;
+  const int off[7] = {-G.plane, -G.nxx, -1, 0, 1, G.nxx, G.plane};
+  const int face[7] = {FZM, FYM, FXM, -1, FXP, FYP, FZP};
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(q / NB), b = (int)(q - (long long)g * NB);
+    const unsigned m = G.nbm[b];
+    const double* Ag = A + (size_t)g * 7 * NB;
+    for (int c = 0; c < 7; ++c) {
+      double v = 0.0;
+      if (c == 3) v = Ag[(size_t)3 * NB + b];
+      else if ((m & NB_ACTIVE) && (m & (1u << face[c]))) v = Ag[(size_t)(6 - c) * NB + b + off[c]];
+      AT[(size_t)g * 7 * NB + (size_t)c * NB + b] = v;
+      if (AT32) AT32[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)v;
+    }
+  }
+}
+
+cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, cudaStream_t st) {
+  long long total = (long long)G.NB * ng;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 65535 * 4) blocks = 65535 * 4;
+  k_transpose<<<blocks, 256, 0, st>>>(G, ng, A, AT, AT32);
+  return cudaGetLastError();
+}
+
+// psi^T F phi = sum_n (sum_g chi_g psi_g)(sum_h nuf_h phi_h), block partials.
+__global__ void k_sens_den(SensParams P, double* part) {
+  const BoxGeom& G = P.G;
+  double acc[1] = {0.0};
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < G.NB; b += gridDim.x * blockDim.x) {
+    double fa = 0.0, ff = 0.0;
+    for (int g = 0; g < P.ng; ++g) {
+      fa = fma(P.chin[(size_t)g * G.NB + b], P.psi[(size_t)g * P.NBH + b], fa);
+      ff = fma(P.nuf[(size_t)g * G.NB + b], P.phi[(size_t)g * P.NBH + b], ff);
+    }
+    acc[0] = fma(fa, ff, acc[0]);
+  }
+  block_partials<1, 0u>(acc, part);
+}
+
+// dF of the harmonic-mean coupling coefficient of coup_coef
+// (mod_cmfd.f90:54-55) with respect to the node's own D:
+//   df = 2 Dn Dm / (Dn hm + Dm hn)  ->  d df / d Dn = 2 Dm^2 hn / (Dn hm + Dm hn)^2
+// and of the boundary forms (:45-50): zero flux 2 alb^2 h / (2 Dn + alb h)^2,
+// zero incoming current 0.5 h / (2 Dn + 0.5 h)^2, reflective 0.
+__device__ __forceinline__ double ddf_dD(bool interior, int bc, double Dn, double Dm, double hn, double hm) {
+  if (interior) {
+    const double den = Dn * hm + Dm * hn;
+    return 2.0 * Dm * Dm * hn / (den * den);
+  }
+  if (bc == 0) {
+    const double alb = 1.e30, den = 2.0 * Dn + alb * hn;
+    return 2.0 * alb * alb * hn / (den * den);
+  }
+  if (bc == 1) {
+    const double den = 2.0 * Dn + 0.5 * hn;
+    return 0.5 * hn / (den * den);
+  }
+  return 0.0;
+}
+
+// Per node and group: out[(c * ng + g) * nnod + n], the Fortran array
+// dkdp(nnod, ng, 4 + ng) with c = 0 D, 1 siga, 2 nuf, 3 sigtr (through
+// D = 1/(3 sigtr), dD/dsigtr = -3 D^2, mod_xsec.f90:199-226) and 4 + h the
+// g -> h scattering (through sigr and the scattering source).
+__global__ void k_sens(SensParams P, const double* part, int nblk, double* out) {
+  double tot[1];
+  grid_totals<1, 0u>(part, nblk, tot);
+  const double den = tot[0];
+  const BoxGeom& G = P.G;
+  const int NB = G.NB, ng = P.ng, nn = P.nnod;
+  const double k = P.keff, lam = 1.0 / k, scale = k * k / den;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+    const int b = P.act[n];
+    const unsigned m = G.nbm[b];
+    double fsa = 0.0;   // sum_g chi_g psi_g at this node
+    for (int g = 0; g < ng; ++g) fsa = fma(P.chin[(size_t)g * NB + b], P.psi[(size_t)g * P.NBH + b], fsa);
+    for (int g = 0; g < ng; ++g) {
+      const double ph = P.phi[(size_t)g * P.NBH + b], ps = P.psi[(size_t)g * P.NBH + b];
+      const double Dn = P.D[(size_t)g * NB + b];
+      // D: every face of the node; an interior face enters its own row and
+      // the neighbour's row with the same (harmonic-mean) coefficient.
+      double nD = 0.0;
+      for (int f = 0; f < 6; ++f) {
+        const int u = f >> 1;
+        const double hn = hdir(G, u, b);
+        if (m & (1u << f)) {
+          const int bm = b + face_off(G, f);
+          const double Dm = P.D[(size_t)g * NB + bm], hm = hdir(G, u, bm);
+          const double phm = P.phi[(size_t)g * P.NBH + bm], psm = P.psi[(size_t)g * P.NBH + bm];
+          const double d = ddf_dD(true, 0, Dn, Dm, hn, hm);
+          nD += d * (ps * (ph - phm) / hn + psm * (phm - ph) / hm);
+        } else {
+          const double d = ddf_dD(false, G.bcf[f], Dn, 0.0, hn, 0.0);
+          nD += d * ps * ph / hn;
+        }
+      }
+      const double sD = -nD * scale;
+      out[((size_t)0 * ng + g) * nn + n] = sD;
+      out[((size_t)1 * ng + g) * nn + n] = -ps * ph * scale;        // siga (through sigr)
+      out[((size_t)2 * ng + g) * nn + n] = lam * fsa * ph * scale;   // nuf of group g
+      out[((size_t)3 * ng + g) * nn + n] = -3.0 * Dn * Dn * sD;      // sigtr
+      for (int h = 0; h < ng; ++h) {
+        double v = 0.0;
+        if (h != g) v = -(ps - P.psi[(size_t)h * P.NBH + b]) * ph * scale;
+        out[((size_t)(4 + h) * ng + g) * nn + n] = v;
+      }
+    }
+  }
+}
+
+cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st) {
+  int blocks = (P.G.NB + 255) / 256;
+  if (blocks > kMaxBlocks) blocks = kMaxBlocks;
+  k_sens_den<<<blocks, 256, 0, st>>>(P, part);
+  int b2 = (P.nnod + 255) / 256;
+  if (b2 > 4096) b2 = 4096;
+  k_sens<<<b2, 256, 0, st>>>(P, part, blocks, out);
+  return cudaGetLastError();
+}
+
+}  // namespace adp

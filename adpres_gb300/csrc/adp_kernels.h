@@ -91,6 +91,20 @@ struct AssembleParams {
   float* A32;
 };
 
+// Contraction of forward and adjoint fluxes into dk/dSigma (adjoint.cu).
+struct SensParams {
+  BoxGeom G;
+  int ng, nnod;
+  long long NBH;
+  double keff;                // forward eigenvalue
+  const int* act;             // [nnod] box index of each node
+  const double* phi;          // forward flux [ng][NBH] (halo offset applied)
+  const double* psi;          // discrete adjoint flux, same layout
+  const double* D;            // [ng][NB]
+  const double* nuf;
+  const double* chin;
+};
+
 // Launchers (return the launch error, if any)
 cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st);
 cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st);
@@ -103,5 +117,7 @@ cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st);
 cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, const double* sigtr,
                            const double* siga, const double* sigs, double* D, double* sigr, OuterCtl* ctl,
                            cudaStream_t st);
+cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, cudaStream_t st);
+cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st);
 
 }  // namespace adp

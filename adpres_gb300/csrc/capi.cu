@@ -84,8 +84,17 @@ struct adp_handle {
   long long* d_ndkey = nullptr;
   int* d_ndloc = nullptr;
   double* d_pbox = nullptr;
+  // discrete adjoint (adp_adjoint_sens), allocated on its first call
+  char* adj_base = nullptr;
+  double* d_AT = nullptr;
+  float* d_AT32 = nullptr;
+  double* d_psi[2] = {nullptr, nullptr};
+  double* d_fsa[2] = {nullptr, nullptr};
+  OuterCtl* d_ctla = nullptr;
+  double *d_sens = nullptr, *d_spart = nullptr;
   // state
   bool xs_set = false;
+  bool fwd_ok = false;        // the flux is a converged forward solution of the current XS
   bool started[2] = {false, false};
   int launch_blocks = 0, launch_threads = 0;
   int sms = 0;
@@ -161,6 +170,7 @@ adp_status adp_destroy(adp_handle* h) {
   cudaSetDevice(h->dev);
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->ar.base) cudaFree(h->ar.base);
+  if (h->adj_base) cudaFree(h->adj_base);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   for (cudaEvent_t e : {h->e0, h->e1, h->e2, h->e3})
     if (e) cudaEventDestroy(e);
@@ -444,6 +454,7 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
 static adp_status upload_xs_common(adp_handle* h, int nmat, const double* nuf, const double* sigf, const double* chi,
                                    const int* mat, const double* sigs, const double* dc) {
   const int nn = h->nnod, G = h->ng;
+  h->fwd_ok = false;
   if (nmat < 1 || !nuf || !sigf || !chi || !mat || !sigs) return fail(h, ADP_ERR_INPUT, "adp_set_xs: null array");
   std::vector<double> chin((size_t)G * nn);
   for (int n = 0; n < nn; ++n) {
@@ -718,8 +729,11 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   if (!h) return ADP_ERR_INPUT;
   CK(cudaSetDevice(h->dev));
   if (!h->xs_set) return fail(h, ADP_ERR_STATE, "adp_outer: cross sections not set");
-  if (mode != ADP_FORWARD && mode != ADP_ADJOINT) return fail(h, ADP_ERR_INPUT, "adp_outer: bad mode");
+  if (mode & ~(ADP_ADJOINT | ADP_FROZEN_DN)) return fail(h, ADP_ERR_INPUT, "adp_outer: bad mode");
+  const bool frozen = (mode & ADP_FROZEN_DN) != 0;
+  mode &= ADP_ADJOINT;
   const int adj = mode == ADP_ADJOINT;
+  h->fwd_ok = false;
   CK(cudaEventRecord(h->e0, h->st));
   // matrix_setup(1): coupling coefficients + assembly
   AssembleParams AP;
@@ -754,11 +768,12 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   c.need_prologue = 1;
   c.err_node = -1;
   c.bar_count = 0;
+  if (frozen) c.ndmax = 0.0;
   const int nod0 = c.nodal_updates;
   const long outers0 = c.p_total;
   *h->h_ctl = c;
   CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
-  const int do_nodal = (h->o.kern != ADP_KERN_FDM) && (!adj || popt > 0);
+  const int do_nodal = !frozen && (h->o.kern != ADP_KERN_FDM) && (!adj || popt > 0);
   P.do_nodal = do_nodal;
   NodalParams NP = nodal_params(h, adj ? 0 : 1);
   int blocks, threads;
@@ -834,6 +849,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
     }
   }
   (void)outers0;
+  h->fwd_ok = !adj && result == ADP_OK && c.converged;
   return result;
 }
 
@@ -899,6 +915,7 @@ adp_status adp_set_state(adp_handle* h, const double* f0, const double* fs0, con
     CK(cudaMemcpy(&h->d_ctl->Ke, &h->h_ctl->Ke, sizeof(double), cudaMemcpyHostToDevice));
   }
   h->started[0] = h->started[1] = true;
+  h->fwd_ok = false;
   return ADP_OK;
 }
 
@@ -920,6 +937,7 @@ adp_status adp_reset(adp_handle* h) {
   CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
   h->started[0] = h->started[1] = false;
+  h->fwd_ok = false;
   return ADP_OK;
 }
 
@@ -939,6 +957,138 @@ adp_status adp_power(adp_handle* h, double* p) {
   CK(cudaStreamSynchronize(h->st));
   if (h->h_ctl->status) return ctl_error(h, *h->h_ctl);
   for (int n = 0; n < h->nnod; ++n) p[n] = box[h->node2box[n]];
+  return ADP_OK;
+}
+
+// Device state of the discrete adjoint, allocated once per handle.
+static adp_status adj_alloc(adp_handle* h) {
+  if (h->adj_base) return ADP_OK;
+  const size_t NB = h->NB, G = h->ng, NBH = h->NBH, nn = h->nnod;
+  const bool mixed = h->o.precision == ADP_MIXED;
+  size_t bytes = 0;
+  auto add = [&](size_t b) { bytes += ((b + 255) & ~(size_t)255) + 256; };
+  add(G * 7 * NB * 8);
+  if (mixed) add(G * 7 * NB * 4);
+  add(G * NBH * 8 * 2);
+  add(NB * 8 * 2);
+  add(sizeof(OuterCtl));
+  add(nn * G * (4 + G) * 8);
+  add(kMaxBlocks * 8);
+  DevArena A;
+  A.size = bytes;
+  CK(cudaMalloc((void**)&A.base, bytes));
+  h->adj_base = A.base;
+  h->d_AT = (double*)A.take(G * 7 * NB * 8);
+  if (mixed) h->d_AT32 = (float*)A.take(G * 7 * NB * 4);
+  for (int t = 0; t < 2; ++t) h->d_psi[t] = (double*)A.take(G * NBH * 8) + h->plane;
+  for (int t = 0; t < 2; ++t) h->d_fsa[t] = (double*)A.take(NB * 8);
+  h->d_ctla = (OuterCtl*)A.take(sizeof(OuterCtl));
+  h->d_sens = (double*)A.take(nn * G * (4 + G) * 8);
+  h->d_spart = (double*)A.take(kMaxBlocks * 8);
+  if (A.used > A.size) return fail(h, ADP_ERR_CUDA, "internal: adjoint arena overflow");
+  CK(cudaMemsetAsync(A.base, 0, A.size, h->st));   // halos and inactive positions stay 0
+  CK(cudaStreamSynchronize(h->st));
+  return ADP_OK;
+}
+
+adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* rep) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!h->fwd_ok)
+    return fail(h, ADP_ERR_STATE, "adp_adjoint_sens: needs a converged forward adp_outer on the current cross sections");
+  adp_status s = adj_alloc(h);
+  if (s != ADP_OK) return s;
+  CK(cudaEventRecord(h->e0, h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const OuterCtl fwd = *h->h_ctl;
+  // A^T of the converged forward matrix (dn frozen)
+  CK(launch_transpose(box_geom(h), h->ng, h->d_A, h->d_AT, h->d_AT32, h->st));
+  OuterParams P = outer_params(h, 1);
+  P.A = h->d_AT;
+  P.A32 = h->d_AT32;
+  for (int t = 0; t < 2; ++t) {
+    P.phi[t] = h->d_psi[t];
+    P.fs[t] = h->d_fsa[t];
+  }
+  P.ctl = h->d_ctla;
+  P.do_nodal = 0;
+  if (tol > 0) P.serc = P.ferc = tol;
+  CK(launch_init_flux(P, h->st));
+  OuterCtl c;
+  std::memset(&c, 0, sizeof c);
+  c.Ke = 1.0;
+  c.need_prologue = 1;
+  c.err_node = -1;
+  *h->h_ctl = c;
+  CK(cudaMemcpyAsync(h->d_ctla, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
+  int blocks, threads;
+  launch_shape(h, blocks, threads);
+  adp_status result = ADP_OK;
+  for (int guard = 0; guard < 4 * h->o.nout + 8; ++guard) {
+    CK(cudaMemsetAsync(&h->d_ctla->bar_count, 0, sizeof(unsigned), h->st));
+    CK(launch_outer(P, blocks, threads, h->st));
+    CK(cudaMemcpyAsync(h->h_ctl, h->d_ctla, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    c = *h->h_ctl;
+    if (c.status) { result = ctl_error(h, c); break; }
+    if (c.converged) break;
+    if (c.max_reached) {
+      result = fail(h, ADP_ERR_MAXOUTER, "adp_adjoint_sens: the adjoint solve reached nout outers without convergence");
+      break;
+    }
+  }
+  if (result == ADP_OK && !c.converged)
+    result = fail(h, ADP_ERR_MAXOUTER, "adp_adjoint_sens: the adjoint solve did not converge");
+  if (result == ADP_OK) {
+    SensParams S;
+    S.G = box_geom(h);
+    S.ng = h->ng;
+    S.nnod = h->nnod;
+    S.NBH = h->NBH;
+    S.keff = fwd.Ke;
+    S.act = h->d_act;
+    S.phi = h->d_phi[fwd.cur];
+    S.psi = h->d_psi[c.cur];
+    S.D = h->d_D;
+    S.nuf = h->d_nuf;
+    S.chin = h->d_chin;
+    CK(launch_sens(S, h->d_spart, h->d_sens, h->st));
+  }
+  CK(cudaEventRecord(h->e1, h->st));
+  CK(cudaEventSynchronize(h->e1));
+  float total_ms = 0.f;
+  cudaEventElapsedTime(&total_ms, h->e0, h->e1);
+  h->tm.adjoint_ms += total_ms;
+  h->tm.adjoint_outers += c.p;
+  if (rep) {
+    rep->outers = c.p;
+    rep->converged = c.converged;
+    rep->nodal_updates = 0;
+    rep->keff = c.Ke;
+    rep->ser = c.ser;
+    rep->fer = c.fer;
+    rep->ndmax = 0.0;
+    rep->im = rep->jm = rep->km = 0;
+    rep->device_ms = total_ms;
+    int n = std::min(std::min(c.p, rep->trace_cap), h->o.nout);
+    if (n > 0) {
+      if (rep->trace_k) CK(cudaMemcpy(rep->trace_k, h->d_tr_k, n * 8, cudaMemcpyDeviceToHost));
+      if (rep->trace_ser) CK(cudaMemcpy(rep->trace_ser, h->d_tr_ser, n * 8, cudaMemcpyDeviceToHost));
+      if (rep->trace_fer) CK(cudaMemcpy(rep->trace_fer, h->d_tr_fer, n * 8, cudaMemcpyDeviceToHost));
+      if (rep->trace_flags) CK(cudaMemcpy(rep->trace_flags, h->d_tr_flags, n * 4, cudaMemcpyDeviceToHost));
+      if (rep->trace_ndmax) CK(cudaMemcpy(rep->trace_ndmax, h->d_tr_ndmax, n * 8, cudaMemcpyDeviceToHost));
+    }
+  }
+  if (result != ADP_OK) return result;
+  const int nn = h->nnod, G = h->ng;
+  if (dkdp) CK(cudaMemcpy(dkdp, h->d_sens, (size_t)nn * G * (4 + G) * 8, cudaMemcpyDeviceToHost));
+  if (psi) {
+    std::vector<double> box((size_t)G * h->NBH);
+    CK(cudaMemcpy(box.data(), h->d_psi[c.cur] - h->plane, box.size() * 8, cudaMemcpyDeviceToHost));
+    for (int g = 0; g < G; ++g)
+      for (int n = 0; n < nn; ++n) psi[(size_t)g * nn + n] = box[(size_t)g * h->NBH + h->plane + h->node2box[n]];
+  }
   return ADP_OK;
 }
 

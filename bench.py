@@ -140,6 +140,44 @@ def cpu_baseline_single(text):
                       f"({est:.1f} s)"}
 
 
+# ------------------------------------------------ dk/dSigma leg ----
+def adjoint_leg(flush, steps=3):
+    """Forward solve + discrete adjoint + contraction on the 34x34x22-node
+    two-group full core (seed 0), mixed precision and FP64; gradients/s
+    counts D, siga, nuf per group and the 1->2 scattering per node."""
+    import torch
+
+    from adpres_gb300 import deck, synth
+    from adpres_gb300.core import Core
+
+    dk = deck.parse(synth.full_core_3d(0))
+    out = {"workload": "full_core_3d seed 0: 34x34 radial nodes x 22 planes, 2 groups, SANM",
+           "params_per_solve": int(dk.nnod * (3 * dk.ng + dk.ng * (dk.ng - 1) // 2))}
+    for prec in ("mixed", "fp64"):
+        c = Core.from_deck(dk, precision=prec)
+
+        def run():
+            c.reset()
+            r = c.outer(trace=False)
+            c.adjoint_sens()
+            return r.device_ms, c.last_adjoint_ms
+
+        for _ in range(2):
+            run()
+        fwd, adj = [], []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            f, a = run()
+            fwd.append(f)
+            adj.append(a)
+        t = (sum(fwd) + sum(adj)) / steps / 1e3
+        out[prec] = {"grads_per_s": out["params_per_solve"] / t, "ms_per_solve": t * 1e3,
+                     "forward_ms": sum(fwd) / steps, "adjoint_ms": sum(adj) / steps}
+        c.close()
+    return out
+
+
 # ------------------------------------------------------------ our arm ----
 def run_ours(args):
     import numpy as np
@@ -238,6 +276,8 @@ def run_ours(args):
     perr = np.abs(p_mixed[m] - p64[m]) / p64[m]
     core64.close()
 
+    adjoint = adjoint_leg(flush)
+
     # e2e through the C ABI from host buffers
     e2e_steps = max(2, min(args.steps, 5))
     h2d = (dk.ng * 5 + dk.ng * dk.ng + 6 * dk.ng) * dk.nnod * 8 + dk.nnod * 4
@@ -276,6 +316,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
                      "launches": launches},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "adjoint": adjoint,
         "gpu_launches": gpu_launches,
         "clocks": ck,
         "cpu_baseline": cpu,

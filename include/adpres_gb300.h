@@ -49,7 +49,11 @@ typedef enum adp_status {
   ADP_ERR_STATE = 12        /* call made in the wrong order                    */
 } adp_status;
 
-typedef enum adp_mode { ADP_FORWARD = 0, ADP_ADJOINT = 1 } adp_mode;
+/* ADP_FROZEN_DN may be or-ed into the mode of adp_outer: the outers then
+ * keep the nodal coupling coefficients dn at their current values (no nodal
+ * update, ndmax taken as 0).  It has no counterpart in the reference; it
+ * gives the CMFD eigenvalue at fixed dn that adp_adjoint_sens differentiates. */
+typedef enum adp_mode { ADP_FORWARD = 0, ADP_ADJOINT = 1, ADP_FROZEN_DN = 4 } adp_mode;
 typedef enum adp_kern { ADP_KERN_FDM = 0, ADP_KERN_PNM = 1, ADP_KERN_SANM = 2 } adp_kern;
 typedef enum adp_precision { ADP_FP64 = 0, ADP_MIXED = 1 } adp_precision;
 
@@ -115,6 +119,8 @@ typedef struct adp_timers {
   long outers;              /* outer iterations performed                      */
   long bicg_rows;           /* BiCGSTAB row-iterations (rows x nin x groups x outers) */
   int grid_blocks, block_threads;
+  double adjoint_ms;        /* adp_adjoint_sens: transpose, adjoint solve, contraction */
+  long adjoint_outers;
 } adp_timers;
 
 /* -- handle life cycle ---------------------------------------------------- */
@@ -200,6 +206,25 @@ adp_status adp_power(adp_handle* h, double* p);
  * Errors: message through adp_last_error(NULL). */
 adp_status adp_power_noalloc(int nnod, int ng, const double* f0, const double* sigf, const double* vdel, double* p,
                              void* stream);
+
+/* Discrete adjoint and dk/dSigma; no counterpart in the reference (its
+ * outer_ad, mod_cmfd.f90:602-699, solves the physical adjoint with its own
+ * adjoint nodal update and the untransposed matrix).  Needs a converged
+ * forward adp_outer on the current cross sections.  With dn frozen at the
+ * forward solution the CMFD problem is M phi = (1/k) F phi; this call
+ * solves M^T psi = (1/k) F^T psi with the persistent kernel on the
+ * transposed stencil (source weights and group sweep of outer_ad), starting
+ * from psi = 1, until ser < tol and fer < tol (tol <= 0: the handle's serc
+ * and ferc), then
+ *   dk/dp = k^2 psi^T ((1/k) dF/dp - dM/dp) phi / (psi^T F phi)
+ * for every node parameter.  dkdp (nnod, ng, 4 + ng), node index fastest:
+ * [:,g,1] dk/dD_g, [:,g,2] dk/dsiga_g, [:,g,3] dk/dnuf_g, [:,g,4]
+ * dk/dsigtr_g (= -3 D_g^2 dk/dD_g, the chain rule of D = 1/(3 sigtr)),
+ * [:,g,4+h] dk/dsigs(g->h) (through sigr and the scattering source; 0 for
+ * h = g).  psi (nnod, ng) receives the adjoint flux (unnormalised); either
+ * output may be NULL.  report (may be NULL) describes the adjoint solve
+ * (keff is its eigenvalue).  The forward state is left unchanged. */
+adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* report);
 
 /* Device timers of the handle. */
 adp_status adp_get_timers(const adp_handle* h, adp_timers* t);

@@ -1722,6 +1722,8 @@ int ora_set_double(void* h, const char* name, double v) {
   std::string s(name);
   if (s == "Ke") { o->Ke = v; return 0; }
   if (s == "ndmax") { o->ndmax = v; return 0; }
+  if (s == "serc") { o->serc = v; return 0; }
+  if (s == "ferc") { o->ferc = v; return 0; }
   return -1;
 }
 
