@@ -13,7 +13,7 @@ module adpres_gb300_bind
   implicit none
 
   integer(c_int), parameter :: ADP_OK = 0
-  integer(c_int), parameter :: ADP_FORWARD = 0, ADP_ADJOINT = 1
+  integer(c_int), parameter :: ADP_FORWARD = 0, ADP_ADJOINT = 1, ADP_FROZEN_DN = 4
   integer(c_int), parameter :: ADP_KERN_FDM = 0, ADP_KERN_PNM = 1, ADP_KERN_SANM = 2
   integer(c_int), parameter :: ADP_FP64 = 0, ADP_MIXED = 1
 
@@ -105,6 +105,15 @@ module adpres_gb300_bind
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: h
       real(c_double), intent(out) :: p(*)
+    end function
+
+    ! dkdp(nnod, ng, 4+ng) and psi(nnod, ng); pass c_null_ptr-free arrays
+    integer(c_int) function adp_adjoint_sens(h, tol, dkdp, psi, rep) bind(C, name="adp_adjoint_sens")
+      import :: c_int, c_ptr, c_double, adp_report
+      type(c_ptr), value :: h
+      real(c_double), value :: tol
+      real(c_double), intent(out) :: dkdp(*), psi(*)
+      type(adp_report), intent(inout) :: rep
     end function
   end interface
 
