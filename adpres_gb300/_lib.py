@@ -68,6 +68,18 @@ class AdpTimers(ctypes.Structure):
                 ("block_threads", ctypes.c_int), ("adjoint_ms", ctypes.c_double), ("adjoint_outers", ctypes.c_long)]
 
 
+class AdpBatchConfig(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int), ("max_team", ctypes.c_int), ("grain", ctypes.c_double),
+                ("blocks_per_sm", ctypes.c_int), ("use_graph", ctypes.c_int)]
+
+
+class AdpBatchResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("converged", ctypes.c_int), ("outers", ctypes.c_int),
+                ("nodal_updates", ctypes.c_int), ("keff", ctypes.c_double), ("ser", ctypes.c_double),
+                ("fer", ctypes.c_double), ("ndmax", ctypes.c_double), ("device_ms", ctypes.c_double),
+                ("team", ctypes.c_int)]
+
+
 # Every entry point declared in include/adpres_gb300.h, with its ctypes signature.
 SIGNATURES = {
     "adp_create": (ctypes.c_int, [ctypes.POINTER(AdpGeom), ctypes.POINTER(AdpOpts), ctypes.POINTER(ctypes.c_void_p)]),
@@ -85,6 +97,21 @@ SIGNATURES = {
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "adp_adjoint_sens": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _dp, _dp, ctypes.POINTER(AdpReport)]),
     "adp_get_timers": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpTimers)]),
+    "adp_batch_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(AdpGeom), ctypes.POINTER(AdpOpts),
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "adp_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "adp_batch_last_error": (ctypes.c_size_t, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    "adp_batch_set_xs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _ip,
+                                        _dp, _dp]),
+    "adp_batch_set_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpBatchConfig)]),
+    "adp_batch_get_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpBatchConfig)]),
+    "adp_batch_solve": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpBatchResult),
+                                       ctypes.POINTER(ctypes.c_double)]),
+    "adp_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpBatchConfig),
+                                          ctypes.POINTER(ctypes.c_double)]),
+    "adp_batch_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "adp_batch_power": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
+    "adp_batch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _ip, _dp]),
     "adp_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }
 

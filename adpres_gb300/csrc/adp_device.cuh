@@ -106,44 +106,47 @@ __device__ __forceinline__ void set_status(OuterCtl* C, int code) {
   atomicCAS(&C->status, 0, code);
 }
 
-// Grid-wide barrier for a cooperative launch (all blocks co-resident).
-// One 32-bit word: block 0 adds 2^31 - (nblocks - 1), every other block
-// adds 1, so the top bit flips exactly when the last block arrives and the
-// low bits return to zero; each block waits until the top bit differs from
-// the value its own add returned.  The word must be 0 at launch.  The wait
-// is bounded: after kBarrierTimeoutNs the block records ADP_ERR_TIMEOUT and
-// returns false, so a fault elsewhere can never leave the kernel spinning.
+// Barrier of a team of co-resident blocks (the whole grid of a cooperative
+// launch, or the blocks that share one core of a batch).  One 32-bit word
+// per team: the block of rank 0 adds 2^31 - (nblocks - 1), every other
+// block adds 1, so the top bit flips exactly when the last block arrives
+// and the low bits return to zero; each block waits until the top bit
+// differs from the value its own add returned.  The word must be 0 when the
+// team first uses it.  The wait is bounded: after kBarrierTimeoutNs the
+// block records ADP_ERR_TIMEOUT and returns false, so a fault elsewhere can
+// never leave the kernel spinning.  Called by lane 0 of one warp.
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
-__device__ __forceinline__ bool grid_barrier(OuterCtl* C, unsigned nblocks) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned add = (blockIdx.x == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
-    __threadfence();
-    const unsigned old = atomicAdd(&C->bar_count, add);
-    if (((old + add) ^ old) & 0x80000000u) {
-      // this block completed the barrier
-    } else {
-      unsigned long long t0 = 0;
-      unsigned spins = 0;
-      while (!((ld_acquire_gpu(&C->bar_count) ^ old) & 0x80000000u)) {
-        if ((++spins & 63u) == 0) {
-          const unsigned long long t = globaltimer_ns();
-          if (t0 == 0) t0 = t;
-          else if (t - t0 > kBarrierTimeoutNs) {
-            set_status(C, ADP_ERR_TIMEOUT);
-            ok = 0;
-            break;
-          }
+__device__ __forceinline__ int team_arrive_wait(OuterCtl* C, unsigned nblocks, unsigned rank) {
+  int ok = 1;
+  const unsigned add = (rank == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
+  __threadfence();
+  const unsigned old = atomicAdd(&C->bar_count, add);
+  if (!(((old + add) ^ old) & 0x80000000u)) {
+    unsigned long long t0 = 0;
+    unsigned spins = 0;
+    while (!((ld_acquire_gpu(&C->bar_count) ^ old) & 0x80000000u)) {
+      if ((++spins & 63u) == 0) {
+        const unsigned long long t = globaltimer_ns();
+        if (t0 == 0) t0 = t;
+        else if (t - t0 > kBarrierTimeoutNs) {
+          set_status(C, ADP_ERR_TIMEOUT);
+          ok = 0;
+          break;
         }
       }
     }
-    __threadfence();
-    if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
-    s_ok = ok;
   }
+  __threadfence();
+  if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
+  return ok;
+}
+
+__device__ __forceinline__ bool team_barrier(OuterCtl* C, unsigned nblocks, unsigned rank) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (nblocks == 1) return true;
+  if (threadIdx.x == 0) s_ok = team_arrive_wait(C, nblocks, rank);
   __syncthreads();
   return s_ok != 0;
 }
@@ -233,15 +236,16 @@ __device__ __forceinline__ void warp_all_n(double (&x)[NQ]) {
   }
 }
 
-// Block reduction, grid barrier and totals in one step, with two block-wide
+// Block reduction, team barrier and totals in one step, with two block-wide
 // synchronisations: every warp reduces its values; after the first
-// __syncthreads warp 0 forms the block partials, lane 0 publishes them and
-// waits at the grid barrier, and warp 0 then sums every block's partials
-// (same order in every block) into shared memory for the whole block.
-// Returns false when the barrier wait ran out of time.
+// __syncthreads warp 0 forms the block partials, lane 0 publishes them in
+// slot[q * kMaxBlocks + rank] and waits at the team barrier, and warp 0
+// then sums every block's partials (same order in every block) into shared
+// memory for the whole block.  Returns false when the barrier wait ran out
+// of time.
 template <int NQ, unsigned MAXMASK>
-__device__ __forceinline__ bool grid_reduce(OuterCtl* C, unsigned nblocks, double* slot, const double (&v)[NQ],
-                                            double (&tot)[NQ]) {
+__device__ __forceinline__ bool grid_reduce(OuterCtl* C, unsigned nblocks, unsigned rank, double* slot,
+                                            const double (&v)[NQ], double (&tot)[NQ]) {
   __shared__ double sw[NQ][32];
   __shared__ double st[NQ];
   __shared__ int s_ok;
@@ -259,36 +263,24 @@ __device__ __forceinline__ bool grid_reduce(OuterCtl* C, unsigned nblocks, doubl
 #pragma unroll
     for (int q = 0; q < NQ; ++q) x[q] = lane < nw ? sw[q][lane] : 0.0;   // sums and maxima of |.| start at 0
     warp_all_n<NQ, MAXMASK>(x);
-    if (lane == 0) {
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) slot[q * kMaxBlocks + blockIdx.x] = x[q];
-    }
     int ok = 1;
-    if (lane == 0) {
-      const unsigned add = (blockIdx.x == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
-      __threadfence();
-      const unsigned old = atomicAdd(&C->bar_count, add);
-      if (!(((old + add) ^ old) & 0x80000000u)) {
-        unsigned long long t0 = 0;
-        unsigned spins = 0;
-        while (!((ld_acquire_gpu(&C->bar_count) ^ old) & 0x80000000u)) {
-          if ((++spins & 63u) == 0) {
-            const unsigned long long t = globaltimer_ns();
-            if (t0 == 0) t0 = t;
-            else if (t - t0 > kBarrierTimeoutNs) {
-              set_status(C, ADP_ERR_TIMEOUT);
-              ok = 0;
-              break;
-            }
-          }
-        }
+    if (nblocks == 1) {
+      // a team of one block: its partials are the totals (the same values
+      // the general path below would form from one partial)
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) st[q] = x[q];
       }
-      __threadfence();
-      if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
+    } else {
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) slot[q * kMaxBlocks + rank] = x[q];
+      }
+      if (lane == 0) ok = team_arrive_wait(C, nblocks, rank);
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      __syncwarp();
     }
-    ok = __shfl_sync(0xffffffffu, ok, 0);
-    __syncwarp();
-    if (ok) {
+    if (ok && nblocks > 1) {
       const int nblk = (int)nblocks;
 #pragma unroll
       for (int q = 0; q < NQ; ++q) x[q] = 0.0;

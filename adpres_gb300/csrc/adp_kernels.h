@@ -105,6 +105,28 @@ struct SensParams {
   const double* chin;
 };
 
+// One core of a batch (batch.cu): the parameter blocks of its handle plus the
+// inputs of the in-kernel cross-section update and power edit.
+struct BatchInst {
+  OuterParams op;
+  NodalParams np;
+  AssembleParams ap;          // with_coupling = 1 (start of the solve)
+  AssembleParams ap0;         // with_coupling = 0 (after a nodal update)
+  const double* sigtr;        // [ng][NB]
+  const double* siga;
+  const double* sigf;
+  double* pbox;               // [NB] normalised node power
+  unsigned long long* t_ns;   // [2] globaltimer at the start and the end of the solve
+  int kern;                   // adp_kern
+  int nnod;
+};
+
+// One entry of a block's task list: core `inst`, solved by a team of `size`
+// blocks in which this block has rank `rank`.
+struct BatchTask {
+  int inst, rank, size, pad;
+};
+
 // Launchers (return the launch error, if any)
 cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st);
 cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st);
@@ -119,5 +141,12 @@ cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, c
                            cudaStream_t st);
 cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, cudaStream_t st);
 cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st);
+// batched solve (batch_k_*.cu): a cooperative launch of `blocks` blocks
+cudaError_t launch_batch(bool mixed, int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,
+                         const int* task_begin, cudaStream_t st);
+int batch_max_blocks_per_sm(bool mixed, int ng, int threads);
+bool batch_supported(int ng, int threads);
+cudaError_t launch_batch_init(const BatchInst* insts, int n, cudaStream_t st);
+cudaError_t launch_batch_gather(const BatchInst* insts, int n, OuterCtl* out, cudaStream_t st);
 
 }  // namespace adp

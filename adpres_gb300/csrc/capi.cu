@@ -14,6 +14,8 @@
 
 #include "../../include/adpres_gb300.h"
 #include "adp_kernels.h"
+#include "handle.h"
+#include "host_geom.h"
 
 using namespace adp;
 
@@ -22,15 +24,6 @@ namespace {
 std::mutex g_err_mu;
 std::string g_create_err;
 
-struct DevArena {
-  char* base = nullptr;
-  size_t size = 0, used = 0;
-  void* take(size_t bytes) {
-    size_t off = (used + 255) & ~(size_t)255;
-    used = off + bytes;
-    return base + off;
-  }
-};
 
 }  // namespace
 
@@ -42,64 +35,6 @@ void set_global_error(const std::string& msg) {
 }
 }  // namespace adp
 
-struct adp_handle {
-  std::string err;
-  int dev = 0;
-  cudaStream_t st = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
-  // geometry
-  int nxx = 0, nyy = 0, nzz = 0, nnod = 0, NB = 0, plane = 0, ng = 0;
-  long long NBH = 0;
-  std::vector<int> node2box;
-  std::vector<unsigned char> nbm;
-  std::vector<int> ysmin, ysmax, xsmin, xsmax;
-  std::vector<double> xdel, ydel, zdel, vdel;
-  int bcf[6] = {0, 0, 0, 0, 0, 0};
-  adp_opts o{};
-  int nmat = 0;
-  // device memory
-  DevArena ar;
-  unsigned char* d_nbm = nullptr;
-  double *d_xdel = nullptr, *d_ydel = nullptr, *d_zdel = nullptr, *d_vdel = nullptr;
-  int *d_act = nullptr, *d_evbase = nullptr;
-  double *d_D = nullptr, *d_sigr = nullptr, *d_nuf = nullptr, *d_sigf = nullptr, *d_chin = nullptr;
-  double *d_sigs = nullptr, *d_dc = nullptr, *d_sigtr = nullptr, *d_siga = nullptr;
-  double *d_df = nullptr, *d_dn = nullptr, *d_A = nullptr;
-  float* d_A32 = nullptr;
-  double* d_phi[2] = {nullptr, nullptr};
-  double* d_fs[2] = {nullptr, nullptr};
-  double *d_r = nullptr, *d_rs = nullptr, *d_s = nullptr, *d_t = nullptr;
-  double* d_pv[2] = {nullptr, nullptr};
-  double* d_vv[2] = {nullptr, nullptr};
-  float *d_r32 = nullptr, *d_rs32 = nullptr, *d_s32 = nullptr, *d_t32 = nullptr;
-  float* d_pv32[2] = {nullptr, nullptr};
-  float* d_vv32[2] = {nullptr, nullptr};
-  double* d_red = nullptr;
-  OuterCtl* d_ctl = nullptr;
-  OuterCtl* h_ctl = nullptr;   // pinned mirror
-  double *d_tr_k = nullptr, *d_tr_ser = nullptr, *d_tr_fer = nullptr, *d_tr_ndmax = nullptr;
-  int* d_tr_flags = nullptr;
-  double *d_sanm = nullptr, *d_S = nullptr, *d_a2 = nullptr, *d_a4 = nullptr, *d_L1 = nullptr, *d_Bc = nullptr;
-  double* d_ndval = nullptr;
-  long long* d_ndkey = nullptr;
-  int* d_ndloc = nullptr;
-  double* d_pbox = nullptr;
-  // discrete adjoint (adp_adjoint_sens), allocated on its first call
-  char* adj_base = nullptr;
-  double* d_AT = nullptr;
-  float* d_AT32 = nullptr;
-  double* d_psi[2] = {nullptr, nullptr};
-  double* d_fsa[2] = {nullptr, nullptr};
-  OuterCtl* d_ctla = nullptr;
-  double *d_sens = nullptr, *d_spart = nullptr;
-  // state
-  bool xs_set = false;
-  bool fwd_ok = false;        // the flux is a converged forward solution of the current XS
-  bool started[2] = {false, false};
-  int launch_blocks = 0, launch_threads = 0;
-  int sms = 0;
-  adp_timers tm{};
-};
 
 namespace {
 
@@ -119,6 +54,20 @@ adp_status fail(adp_handle* h, adp_status s, const std::string& msg) {
       return fail(h, ADP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
   } while (0)
 
+
+// Upload a node-major Fortran array a(nnod, ng[, m]) into the box layout
+// [ng][m][NB] (or [ng][NB]); inactive box positions get 0.
+template <class T>
+void to_box(const adp_handle* h, const T* src, int ncomp, std::vector<T>& out) {
+  const int nn = h->nnod, NB = h->NB;
+  out.assign((size_t)ncomp * NB, T(0));
+  for (int c = 0; c < ncomp; ++c)
+    for (int n = 0; n < nn; ++n) out[(size_t)c * NB + h->node2box[n]] = src[(size_t)c * nn + n];
+}
+
+}  // namespace
+
+namespace adp {
 BoxGeom box_geom(const adp_handle* h) {
   BoxGeom G;
   G.nxx = h->nxx;
@@ -135,18 +84,136 @@ BoxGeom box_geom(const adp_handle* h) {
   for (int f = 0; f < 6; ++f) G.bcf[f] = h->bcf[f];
   return G;
 }
+}  // namespace adp
 
-// Upload a node-major Fortran array a(nnod, ng[, m]) into the box layout
-// [ng][m][NB] (or [ng][NB]); inactive box positions get 0.
-template <class T>
-void to_box(const adp_handle* h, const T* src, int ncomp, std::vector<T>& out) {
-  const int nn = h->nnod, NB = h->NB;
-  out.assign((size_t)ncomp * NB, T(0));
-  for (int c = 0; c < ncomp; ++c)
-    for (int n = 0; n < nn; ++n) out[(size_t)c * NB + h->node2box[n]] = src[(size_t)c * nn + n];
+namespace adp {
+
+static adp_status gfail(std::string& err, adp_status st, const char* msg) {
+  err = msg;
+  return st;
 }
 
-}  // namespace
+// Geometry of one core from the reference's sdata view (adp_geom): box
+// sizes, the ragged outline from plane 1 (mod_io.f90:1071-1110), the node
+// order check (misc, :1317-1330), neighbour masks, volumes and the sweep
+// order of the nodal update.  Shared by adp_create and adp_batch_create.
+adp_status build_geometry(const adp_geom& g, HostGeom& H, std::string& err) {
+  if (g.nxx < 1 || g.nyy < 1 || g.nzz < 2 || g.nnod < 1 || !g.ix || !g.iy || !g.iz || !g.xdel || !g.ydel || !g.zdel)
+    return gfail(err, ADP_ERR_INPUT, "bad geometry sizes or null arrays");
+  int bcs[6] = {g.east, g.west, g.north, g.south, g.bottom, g.top};
+  for (int b : bcs)
+    if (b < 0 || b > 2) return gfail(err, ADP_ERR_INPUT, "boundary conditions must be 0, 1 or 2");
+  long long nb64 = (long long)g.nxx * g.nyy * g.nzz;
+  if (nb64 > 400000000LL) return gfail(err, ADP_ERR_INPUT, "box too large");
+
+  H.nxx = g.nxx;
+  H.nyy = g.nyy;
+  H.nzz = g.nzz;
+  H.nnod = g.nnod;
+  H.NB = (int)nb64;
+  H.plane = g.nxx * g.nyy;
+  H.NBH = (long long)H.NB + 2LL * H.plane;
+  // face order X+ X- Y+ Y- Z+ Z- : east west north south top bottom
+  H.bcf[FXP] = g.east;
+  H.bcf[FXM] = g.west;
+  H.bcf[FYP] = g.north;
+  H.bcf[FYM] = g.south;
+  H.bcf[FZP] = g.top;
+  H.bcf[FZM] = g.bottom;
+  H.xdel.assign(g.xdel, g.xdel + g.nxx);
+  H.ydel.assign(g.ydel, g.ydel + g.nyy);
+  H.zdel.assign(g.zdel, g.zdel + g.nzz);
+  for (double d : H.xdel) if (!(d > 0)) return gfail(err, ADP_ERR_INPUT, "node sizes must be > 0");
+  for (double d : H.ydel) if (!(d > 0)) return gfail(err, ADP_ERR_INPUT, "node sizes must be > 0");
+  for (double d : H.zdel) if (!(d > 0)) return gfail(err, ADP_ERR_INPUT, "node sizes must be > 0");
+
+  // Outline from the plane iz == 1 (mod_io.f90:1071-1110).
+  const int nxx = g.nxx, nyy = g.nyy, nzz = g.nzz;
+  H.ysmin.assign(nyy, nxx);
+  H.ysmax.assign(nyy, -1);
+  H.xsmin.assign(nxx, nyy);
+  H.xsmax.assign(nxx, -1);
+  for (int n = 0; n < g.nnod; ++n) {
+    int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1;
+    if (i < 0 || i >= nxx || j < 0 || j >= nyy || k < 0 || k >= nzz) return gfail(err, ADP_ERR_INPUT, "node index out of the box");
+    if (k == 0) {
+      H.ysmin[j] = std::min(H.ysmin[j], i);
+      H.ysmax[j] = std::max(H.ysmax[j], i);
+      H.xsmin[i] = std::min(H.xsmin[i], j);
+      H.xsmax[i] = std::max(H.xsmax[i], j);
+    }
+  }
+  // The node order must be the reference's (misc, mod_io.f90:1317-1330).
+  {
+    int n = 0;
+    std::vector<unsigned char> on((size_t)nxx * nyy, 0);
+    for (int k = 0; k < nzz; ++k)
+      for (int j = 0; j < nyy; ++j)
+        for (int i = H.ysmin[j]; i <= H.ysmax[j]; ++i) {
+          if (n >= g.nnod || g.ix[n] - 1 != i || g.iy[n] - 1 != j || g.iz[n] - 1 != k) return gfail(err, ADP_ERR_INPUT, "nodes are not in the reference order (k, j, i over the plane-1 outline)");
+          if (k == 0) on[(size_t)j * nxx + i] = 1;
+          ++n;
+        }
+    if (n != g.nnod) return gfail(err, ADP_ERR_INPUT, "node count does not match the outline");
+    // Column and row outlines must agree (the reference's zero-material
+    // check, mod_io.f90:1112-1132), and every line needs two nodes
+    // (the two-node sweeps read a neighbour at every line end).
+    for (int i = 0; i < nxx; ++i) {
+      if (H.xsmax[i] - H.xsmin[i] < 1) return gfail(err, ADP_ERR_INPUT, "a y column holds fewer than two nodes");
+      for (int j = H.xsmin[i]; j <= H.xsmax[i]; ++j)
+        if (!on[(size_t)j * nxx + i]) return gfail(err, ADP_ERR_INPUT, "outline has a hole inside the core");
+    }
+    for (int j = 0; j < nyy; ++j)
+      if (H.ysmax[j] - H.ysmin[j] < 1) return gfail(err, ADP_ERR_INPUT, "an x row holds fewer than two nodes");
+  }
+  H.node2box.resize(g.nnod);
+  H.nbm.assign(H.NB, 0);
+  H.vdel.assign(H.NB, 0.0);
+  for (int n = 0; n < g.nnod; ++n) {
+    int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1;
+    int b = i + nxx * (j + nyy * k);
+    H.node2box[n] = b;
+    unsigned m = NB_ACTIVE;
+    if (i != H.ysmax[j]) m |= 1u << FXP;
+    if (i != H.ysmin[j]) m |= 1u << FXM;
+    if (j != H.xsmax[i]) m |= 1u << FYP;
+    if (j != H.xsmin[i]) m |= 1u << FYM;
+    if (k != nzz - 1) m |= 1u << FZP;
+    if (k != 0) m |= 1u << FZM;
+    H.nbm[b] = (unsigned char)m;
+    H.vdel[b] = H.xdel[i] * H.ydel[j] * H.zdel[k];
+  }
+  // Sweep-order index of each node's minus face, per direction
+  // (mod_nodal.f90:53-125: x lines over (k,j), y lines over (k,i), z lines
+  // over the plane-1 columns in node order).
+  std::vector<int>& evbase = H.evbase;
+  evbase.assign((size_t)3 * H.NB, 0);
+  {
+    std::vector<long long> prefx(nyy), prefy(nxx);
+    long long Tx = 0, Ty = 0;
+    for (int j = 0; j < nyy; ++j) { prefx[j] = Tx; Tx += H.ysmax[j] - H.ysmin[j] + 2; }
+    for (int i = 0; i < nxx; ++i) { prefy[i] = Ty; Ty += H.xsmax[i] - H.xsmin[i] + 2; }
+    long long base_y = Tx * nzz, base_z = base_y + Ty * nzz;
+    std::vector<int> col((size_t)nxx * nyy, -1);
+    int c = 0;
+    for (int j = 0; j < nyy; ++j)
+      for (int i = H.ysmin[j]; i <= H.ysmax[j]; ++i) col[(size_t)j * nxx + i] = c++;
+    long long total = base_z + (long long)c * (nzz + 1);
+    if (total * kMaxGroups > 0x7fffffffffffLL) return gfail(err, ADP_ERR_INPUT, "too many faces");
+    if (total > 0x7fffffffLL) return gfail(err, ADP_ERR_INPUT, "too many faces");
+    for (int n = 0; n < g.nnod; ++n) {
+      int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1, b = H.node2box[n];
+      evbase[b] = (int)(k * Tx + prefx[j] + (i - H.ysmin[j]));
+      evbase[(size_t)H.NB + b] = (int)(base_y + k * Ty + prefy[i] + (j - H.xsmin[i]));
+      evbase[(size_t)2 * H.NB + b] = (int)(base_z + (long long)col[(size_t)j * nxx + i] * (nzz + 1) + k);
+    }
+  }
+
+  H.nnod = g.nnod;
+  return ADP_OK;
+}
+
+}  // namespace adp
 
 extern "C" {
 
@@ -190,134 +257,37 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
     return fail(nullptr, ADP_ERR_UNSUPPORTED, "adp_create: groups must be 1..8");
   if (opts->kern < 0 || opts->kern > 2 || opts->precision < 0 || opts->precision > 1)
     return fail(nullptr, ADP_ERR_INPUT, "adp_create: bad kern or precision");
-  int bcs[6] = {g.east, g.west, g.north, g.south, g.bottom, g.top};
-  for (int b : bcs)
-    if (b < 0 || b > 2) return fail(nullptr, ADP_ERR_INPUT, "adp_create: boundary conditions must be 0, 1 or 2");
-  long long nb64 = (long long)g.nxx * g.nyy * g.nzz;
-  if (nb64 > 400000000LL) return fail(nullptr, ADP_ERR_INPUT, "adp_create: box too large");
-
   h = new adp_handle();
-  h->nxx = g.nxx;
-  h->nyy = g.nyy;
-  h->nzz = g.nzz;
-  h->nnod = g.nnod;
+  {
+    adp::HostGeom H;
+    std::string gerr;
+    adp_status gs = adp::build_geometry(g, H, gerr);
+    if (gs != ADP_OK) {
+      adp_destroy(h);
+      return fail(nullptr, gs, "adp_create: " + gerr);
+    }
+    h->nxx = H.nxx;
+    h->nyy = H.nyy;
+    h->nzz = H.nzz;
+    h->nnod = H.nnod;
+    h->NB = H.NB;
+    h->plane = H.plane;
+    h->NBH = H.NBH;
+    for (int f = 0; f < 6; ++f) h->bcf[f] = H.bcf[f];
+    h->xdel = std::move(H.xdel);
+    h->ydel = std::move(H.ydel);
+    h->zdel = std::move(H.zdel);
+    h->vdel = std::move(H.vdel);
+    h->ysmin = std::move(H.ysmin);
+    h->ysmax = std::move(H.ysmax);
+    h->xsmin = std::move(H.xsmin);
+    h->xsmax = std::move(H.xsmax);
+    h->node2box = std::move(H.node2box);
+    h->nbm = std::move(H.nbm);
+    h->evbase_host = std::move(H.evbase);
+  }
   h->ng = opts->ng;
-  h->NB = (int)nb64;
-  h->plane = g.nxx * g.nyy;
-  h->NBH = (long long)h->NB + 2LL * h->plane;
-  // face order X+ X- Y+ Y- Z+ Z- : east west north south top bottom
-  h->bcf[FXP] = g.east;
-  h->bcf[FXM] = g.west;
-  h->bcf[FYP] = g.north;
-  h->bcf[FYM] = g.south;
-  h->bcf[FZP] = g.top;
-  h->bcf[FZM] = g.bottom;
-  h->xdel.assign(g.xdel, g.xdel + g.nxx);
-  h->ydel.assign(g.ydel, g.ydel + g.nyy);
-  h->zdel.assign(g.zdel, g.zdel + g.nzz);
-  for (double d : h->xdel) if (!(d > 0)) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: node sizes must be > 0"); }
-  for (double d : h->ydel) if (!(d > 0)) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: node sizes must be > 0"); }
-  for (double d : h->zdel) if (!(d > 0)) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: node sizes must be > 0"); }
-
-  // Outline from the plane iz == 1 (mod_io.f90:1071-1110).
-  const int nxx = g.nxx, nyy = g.nyy, nzz = g.nzz;
-  h->ysmin.assign(nyy, nxx);
-  h->ysmax.assign(nyy, -1);
-  h->xsmin.assign(nxx, nyy);
-  h->xsmax.assign(nxx, -1);
-  for (int n = 0; n < g.nnod; ++n) {
-    int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1;
-    if (i < 0 || i >= nxx || j < 0 || j >= nyy || k < 0 || k >= nzz) {
-      adp_destroy(h);
-      return fail(nullptr, ADP_ERR_INPUT, "adp_create: node index out of the box");
-    }
-    if (k == 0) {
-      h->ysmin[j] = std::min(h->ysmin[j], i);
-      h->ysmax[j] = std::max(h->ysmax[j], i);
-      h->xsmin[i] = std::min(h->xsmin[i], j);
-      h->xsmax[i] = std::max(h->xsmax[i], j);
-    }
-  }
-  // The node order must be the reference's (misc, mod_io.f90:1317-1330).
-  {
-    int n = 0;
-    std::vector<unsigned char> on((size_t)nxx * nyy, 0);
-    for (int k = 0; k < nzz; ++k)
-      for (int j = 0; j < nyy; ++j)
-        for (int i = h->ysmin[j]; i <= h->ysmax[j]; ++i) {
-          if (n >= g.nnod || g.ix[n] - 1 != i || g.iy[n] - 1 != j || g.iz[n] - 1 != k) {
-            adp_destroy(h);
-            return fail(nullptr, ADP_ERR_INPUT, "adp_create: nodes are not in the reference order (k, j, i over the plane-1 outline)");
-          }
-          if (k == 0) on[(size_t)j * nxx + i] = 1;
-          ++n;
-        }
-    if (n != g.nnod) {
-      adp_destroy(h);
-      return fail(nullptr, ADP_ERR_INPUT, "adp_create: node count does not match the outline");
-    }
-    // Column and row outlines must agree (the reference's zero-material
-    // check, mod_io.f90:1112-1132), and every line needs two nodes
-    // (the two-node sweeps read a neighbour at every line end).
-    for (int i = 0; i < nxx; ++i) {
-      if (h->xsmax[i] - h->xsmin[i] < 1) {
-        adp_destroy(h);
-        return fail(nullptr, ADP_ERR_INPUT, "adp_create: a y column holds fewer than two nodes");
-      }
-      for (int j = h->xsmin[i]; j <= h->xsmax[i]; ++j)
-        if (!on[(size_t)j * nxx + i]) {
-          adp_destroy(h);
-          return fail(nullptr, ADP_ERR_INPUT, "adp_create: outline has a hole inside the core");
-        }
-    }
-    for (int j = 0; j < nyy; ++j)
-      if (h->ysmax[j] - h->ysmin[j] < 1) {
-        adp_destroy(h);
-        return fail(nullptr, ADP_ERR_INPUT, "adp_create: an x row holds fewer than two nodes");
-      }
-  }
-  h->node2box.resize(g.nnod);
-  h->nbm.assign(h->NB, 0);
-  h->vdel.assign(h->NB, 0.0);
-  for (int n = 0; n < g.nnod; ++n) {
-    int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1;
-    int b = i + nxx * (j + nyy * k);
-    h->node2box[n] = b;
-    unsigned m = NB_ACTIVE;
-    if (i != h->ysmax[j]) m |= 1u << FXP;
-    if (i != h->ysmin[j]) m |= 1u << FXM;
-    if (j != h->xsmax[i]) m |= 1u << FYP;
-    if (j != h->xsmin[i]) m |= 1u << FYM;
-    if (k != nzz - 1) m |= 1u << FZP;
-    if (k != 0) m |= 1u << FZM;
-    h->nbm[b] = (unsigned char)m;
-    h->vdel[b] = h->xdel[i] * h->ydel[j] * h->zdel[k];
-  }
-  // Sweep-order index of each node's minus face, per direction
-  // (mod_nodal.f90:53-125: x lines over (k,j), y lines over (k,i), z lines
-  // over the plane-1 columns in node order).
-  std::vector<int> evbase((size_t)3 * h->NB, 0);
-  {
-    std::vector<long long> prefx(nyy), prefy(nxx);
-    long long Tx = 0, Ty = 0;
-    for (int j = 0; j < nyy; ++j) { prefx[j] = Tx; Tx += h->ysmax[j] - h->ysmin[j] + 2; }
-    for (int i = 0; i < nxx; ++i) { prefy[i] = Ty; Ty += h->xsmax[i] - h->xsmin[i] + 2; }
-    long long base_y = Tx * nzz, base_z = base_y + Ty * nzz;
-    std::vector<int> col((size_t)nxx * nyy, -1);
-    int c = 0;
-    for (int j = 0; j < nyy; ++j)
-      for (int i = h->ysmin[j]; i <= h->ysmax[j]; ++i) col[(size_t)j * nxx + i] = c++;
-    long long total = base_z + (long long)c * (nzz + 1);
-    if (total * kMaxGroups > 0x7fffffffffffLL) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: too many faces"); }
-    if (total > 0x7fffffffLL) { adp_destroy(h); return fail(nullptr, ADP_ERR_INPUT, "adp_create: too many faces"); }
-    for (int n = 0; n < g.nnod; ++n) {
-      int i = g.ix[n] - 1, j = g.iy[n] - 1, k = g.iz[n] - 1, b = h->node2box[n];
-      evbase[b] = (int)(k * Tx + prefx[j] + (i - h->ysmin[j]));
-      evbase[(size_t)h->NB + b] = (int)(base_y + k * Ty + prefy[i] + (j - h->xsmin[i]));
-      evbase[(size_t)2 * h->NB + b] = (int)(base_z + (long long)col[(size_t)j * nxx + i] * (nzz + 1) + k);
-    }
-  }
-
+  const int nxx = h->nxx, nyy = h->nyy, nzz = h->nzz;
   // Options with the reference defaults.
   h->o = *opts;
   if (h->o.nin < 1) h->o.nin = 2;
@@ -432,7 +402,7 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
       (ce = cudaMemcpyAsync(h->d_zdel, h->zdel.data(), nzz * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(h->d_vdel, h->vdel.data(), NB * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(h->d_act, h->node2box.data(), nn * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
-      (ce = cudaMemcpyAsync(h->d_evbase, evbase.data(), 3 * NB * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess) {
+      (ce = cudaMemcpyAsync(h->d_evbase, h->evbase_host.data(), 3 * NB * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess) {
     adp_destroy(h);
     return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
   }
@@ -504,7 +474,9 @@ static adp_status upload_xs_common(adp_handle* h, int nmat, const double* nuf, c
   return ADP_OK;
 }
 
-static NodalParams nodal_params(adp_handle* h, int cmode) {
+}  // extern "C"
+
+NodalParams adp::nodal_params(adp_handle* h, int cmode) {
   NodalParams P;
   std::memset(&P, 0, sizeof P);
   P.G = box_geom(h);
@@ -542,6 +514,8 @@ static NodalParams nodal_params(adp_handle* h, int cmode) {
   P.tr_flags = h->d_tr_flags;
   return P;
 }
+
+extern "C" {
 
 static adp_status after_xs(adp_handle* h) {
   if (h->o.kern == ADP_KERN_SANM) {
@@ -631,7 +605,9 @@ adp_status adp_xs_updt(adp_handle* h, int nmat, const double* xsigtr, const doub
   return adp_xs_updt_nodes(h, nmat, st.data(), sa.data(), nf.data(), sf.data(), chi, mat, ss.data(), dc);
 }
 
-static OuterParams outer_params(adp_handle* h, int adj) {
+}  // extern "C"
+
+OuterParams adp::outer_params(adp_handle* h, int adj) {
   OuterParams P;
   std::memset(&P, 0, sizeof P);
   P.G = box_geom(h);
@@ -675,6 +651,8 @@ static OuterParams outer_params(adp_handle* h, int adj) {
   P.tr_ndmax = h->d_tr_ndmax;
   return P;
 }
+
+extern "C" {
 
 // Launch shape of the persistent kernel: at most one 512-thread block per SM
 // (more co-resident blocks only add barrier participants), and a block

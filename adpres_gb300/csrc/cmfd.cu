@@ -11,13 +11,12 @@
 #include <math.h>
 
 #include "adp_kernels.h"
+#include "cmfd_items.cuh"
+#include "outer_body.cuh"
 
 namespace adp {
 
 constexpr int kOuterThreads = 512;
-
-__device__ __forceinline__ double fmav(double a, double b, double c) { return fma(a, b, c); }
-__device__ __forceinline__ float fmav(float a, float b, float c) { return fmaf(a, b, c); }
 
 // ---------------------------------------------------------------------------
 // matrix_setup (mod_cmfd.f90:217-304) with coup_coef (:11-137) when requested.
@@ -25,61 +24,7 @@ __device__ __forceinline__ float fmav(float a, float b, float c) { return fmaf(a
 // Row slots in reference column order: [z-, y-, x-, diag, x+, y+, z+].
 // ---------------------------------------------------------------------------
 __global__ void k_assemble(AssembleParams P) {
-  const BoxGeom& G = P.G;
-  const int NB = G.NB;
-  const long long total = (long long)NB * P.ng;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
-       q += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(q / NB), b = (int)(q - (long long)g * NB);
-    const unsigned m = G.nbm[b];
-    double* df = P.df + (size_t)g * 6 * NB;
-    const double* dn = P.dn + (size_t)g * 6 * NB;
-    double* A = P.A + (size_t)g * 7 * NB;
-    if (!(m & NB_ACTIVE)) {
-      for (int c = 0; c < 7; ++c) {
-        A[(size_t)c * NB + b] = 0.0;
-        if (P.A32) P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = 0.0f;
-      }
-      continue;
-    }
-    const int i = b % G.nxx, j = (b / G.nxx) % G.nyy, k = b / G.plane;
-    const double h[3] = {G.xdel[i], G.ydel[j], G.zdel[k]};
-    if (P.with_coupling) {
-      const double alb = 1.e30;
-      const double Dn = P.D[(size_t)g * NB + b];
-      for (int f = 0; f < 6; ++f) {
-        const int u = f >> 1;
-        double v;
-        if (m & (1u << f)) {
-          const int nb = b + face_off(G, f);
-          const double d2 = P.D[(size_t)g * NB + nb];
-          const double hn = hdir(G, u, nb);
-          v = 2.0 * Dn * d2 / (Dn * hn + d2 * h[u]);
-        } else {
-          const int bc = G.bcf[f];
-          if (bc == 0) v = 2.0 * alb * Dn / (2.0 * Dn + alb * h[u]);
-          else if (bc == 1) v = Dn / (2.0 * Dn + 0.5 * h[u]);
-          else v = 0.0;
-        }
-        df[(size_t)f * NB + b] = v;
-      }
-    }
-    double F[6], N[6];
-    for (int f = 0; f < 6; ++f) { F[f] = df[(size_t)f * NB + b]; N[f] = dn[(size_t)f * NB + b]; }
-    double a[7];
-    a[0] = (m & (1u << FZM)) ? -(F[FZM] - N[FZM]) / h[2] : 0.0;
-    a[1] = (m & (1u << FYM)) ? -(F[FYM] - N[FYM]) / h[1] : 0.0;
-    a[2] = (m & (1u << FXM)) ? -(F[FXM] - N[FXM]) / h[0] : 0.0;
-    a[3] = (F[FXP] + F[FXM] - N[FXP] + N[FXM]) / h[0] + (F[FYP] + F[FYM] - N[FYP] + N[FYM]) / h[1] +
-           (F[FZP] + F[FZM] - N[FZP] + N[FZM]) / h[2] + P.sigr[(size_t)g * NB + b];
-    a[4] = (m & (1u << FXP)) ? -(F[FXP] + N[FXP]) / h[0] : 0.0;
-    a[5] = (m & (1u << FYP)) ? -(F[FYP] + N[FYP]) / h[1] : 0.0;
-    a[6] = (m & (1u << FZP)) ? -(F[FZP] + N[FZP]) / h[2] : 0.0;
-    for (int c = 0; c < 7; ++c) {
-      A[(size_t)c * NB + b] = a[c];
-      if (P.A32) P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)a[c];
-    }
-  }
+  assemble_items(P, blockIdx.x * (long long)blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x);
 }
 
 cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st) {
@@ -92,21 +37,7 @@ cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st) {
 
 // First-call start of outer()/outer_ad(): f0 = 1, Ke = 1, fs0 = FSrc(f0)
 // (mod_cmfd.f90:448-454, :635-641).
-__global__ void k_init_flux(OuterParams P) {
-  const BoxGeom& G = P.G;
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < G.NB; b += gridDim.x * blockDim.x) {
-    const bool act = G.nbm[b] & NB_ACTIVE;
-    double fs = 0.0;
-    for (int g = 0; g < P.ng; ++g) {
-      const double x = act ? 1.0 : 0.0;
-      P.phi[0][(size_t)g * P.NBH + b] = x;
-      P.phi[1][(size_t)g * P.NBH + b] = x;
-      fs = fs + x * P.wfis[(size_t)g * G.NB + b];
-    }
-    P.fs[0][b] = fs;
-    P.fs[1][b] = fs;
-  }
-}
+__global__ void k_init_flux(OuterParams P) { init_flux_items(P, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x); }
 
 cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
   int blocks = (P.G.NB + 255) / 256;
@@ -115,363 +46,9 @@ cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// The persistent outer-iteration kernel.
-//
-// One cooperative launch runs outer iterations until one needs a nodal
-// update (p mod nupd == 0), converges, reaches nout, or fails.  Every block
-// owns the box rows tid, tid + nthreads, ... in every phase, so values a
-// thread wrote in one phase are read back by the same thread without a
-// barrier; neighbour reads and global dot products are separated by
-// grid_barrier.  Per group solve (bicg, mod_cmfd.f90:1203-1243):
-//   P0: b = TSrc, r = b - A x, rs = r, partial (rs,r)              | barrier
-//   per step i = 1..nin:
-//   A : (i > 1: the previous step's x += alpha p + omega s and
-//       r = s - omega t, r recomputed at neighbours), beta,
-//       p = r + beta (p - omega v) (neighbours recomputed), v = A p,
-//       partial (rs,v)                                               | barrier
-//   B : alpha, s = r - alpha v (neighbours recomputed), t = A s,
-//       partials (t,t), (t,s) and, before another step, (rs,s), (rs,t),
-//       whence (rs, r_next) = (rs,s) - omega (rs,t)                  | barrier
-//   C (last step only, no barrier): x += alpha p + omega s, RelEg.
-// Two grid barriers per BiCGSTAB step instead of three: the (rs,r)
-// reduction of bicg (mod_cmfd.f90:1230) is formed algebraically from
-// phase-B partials, so the r/x update joins the next step's phase A.
-// After the last group: FSrc, |fs - fs0c|^2, Integrate, RelE, RelEg
-// (barrier), extrapolation every nac outers (barrier), k update and the
-// convergence test, all in the same order as mod_cmfd.f90:479-495.
-//
-// MIXED: P0 is computed in FP64 with the FP64 matrix (the defect of the
-// current flux); the nin Krylov steps for the correction run with the FP32
-// matrix copy and FP32 vectors; each thread sums its rows' products in FP32
-// and the block and grid sums are FP64; the flux x stays FP64 and receives
-// FP32 increments.  Both forms avoid FP64 division in per-row work (the
-// source uses 1/k computed once per outer; RelE/RelEg divide only when a
-// candidate beats the running maximum).
-// ---------------------------------------------------------------------------
-template <bool MIXED>
-struct KV { using T = double; };
-template <>
-struct KV<true> { using T = float; };
-
 template <bool MIXED>
 __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
-  using T = typename KV<MIXED>::T;
-  OuterCtl* C = P.ctl;
-  const BoxGeom& G = P.G;
-  const int NB = G.NB, nxx = G.nxx, plane = G.plane, ng = P.ng;
-  const int nthr = gridDim.x * blockDim.x;
-  const int tid0 = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned nblk = gridDim.x;
-  const long long NBH = P.NBH;
-
-  __shared__ int s_stop;
-  if (threadIdx.x == 0) s_stop = (C->status || C->converged || C->max_reached || C->nodal_due) ? 1 : 0;
-  __syncthreads();
-  if (s_stop) return;
-
-  double Ke = C->Ke, f = C->f, e1 = C->e1;
-  const double ndmax = C->ndmax;
-  int p = C->p, ptot = C->p_total, cur = C->cur;
-  int epoch = 0;
-  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
-#define RED(e) (P.red + ((e) & 1) * kRedQ * kMaxBlocks)
-
-  const T* Ab = MIXED ? (const T*)P.A32 : (const T*)P.A;
-  T* r = MIXED ? (T*)P.r32 : (T*)P.r;
-  T* rs = MIXED ? (T*)P.rs32 : (T*)P.rs;
-  T* s = MIXED ? (T*)P.s32 : (T*)P.s;
-  T* t = MIXED ? (T*)P.t32 : (T*)P.t;
-  T* pv[2] = {MIXED ? (T*)P.pv32[0] : (T*)P.pv[0], MIXED ? (T*)P.pv32[1] : (T*)P.pv[1]};
-  T* vv[2] = {MIXED ? (T*)P.vv32[0] : (T*)P.vv[0], MIXED ? (T*)P.vv32[1] : (T*)P.vv[1]};
-
-  if (C->need_prologue) {
-    // f = Integrate(fs0); errn = 1; e1 = Integrate(errn)  (mod_cmfd.f90:457-459)
-    double acc[2] = {0.0, 0.0};
-    const double* fsc = P.fs[cur];
-    for (int b = tid0; b < NB; b += nthr) {
-      acc[0] = fma(G.vdel[b], fsc[b], acc[0]);
-      acc[1] += G.vdel[b];
-    }
-    double tot[2];
-    if (!grid_reduce<2, 0u>(C, nblk, RED(epoch), acc, tot)) return;
-    ++epoch;
-    f = tot[0];
-    e1 = tot[1];
-  }
-
-  while (true) {
-    ++p;
-    ++ptot;
-    const int old = cur, nw = cur ^ 1;
-    const double* phiO = P.phi[old];
-    double* phiN = P.phi[nw];
-    const double* fsO = P.fs[old];
-    double* fsN = P.fs[nw];
-    const double invKe = 1.0 / Ke;
-    double fer_acc = 0.0;
-
-    for (int gi = 0; gi < ng; ++gi) {
-      const int g = P.adj ? ng - 1 - gi : gi;
-      const T* Ag = Ab + (size_t)g * 7 * NB;
-      const double* A64 = P.A + (size_t)g * 7 * NB;
-      const double* xO = phiO + (size_t)g * NBH;
-      double* xN = phiN + (size_t)g * NBH;
-      const double* wsrc = P.wsrc + (size_t)g * NB;
-
-      // ---- P0: source and initial residual (TSrc + r = b - A x) --------
-      double tot1[1];
-      {
-        T accT = T(0);
-        for (int b = tid0; b < NB; b += nthr) {
-          double s0 = 0.0;
-          for (int h = 0; h < ng; ++h) {
-            if (h == g) continue;
-            const bool solved = P.adj ? (h > g) : (h < g);
-            const double ph = (solved ? phiN : phiO)[(size_t)h * NBH + b];
-            const double sg = P.adj ? P.sigs[((size_t)g * ng + h) * NB + b] : P.sigs[((size_t)h * ng + g) * NB + b];
-            s0 = fma(sg, ph, s0);
-          }
-          const double bs = wsrc[b] * fsO[b] * invKe + s0;
-          double ax = A64[b] * xO[b - plane];
-          ax = fma(A64[(size_t)NB + b], xO[b - nxx], ax);
-          ax = fma(A64[(size_t)2 * NB + b], xO[b - 1], ax);
-          ax = fma(A64[(size_t)3 * NB + b], xO[b], ax);
-          ax = fma(A64[(size_t)4 * NB + b], xO[b + 1], ax);
-          ax = fma(A64[(size_t)5 * NB + b], xO[b + nxx], ax);
-          ax = fma(A64[(size_t)6 * NB + b], xO[b + plane], ax);
-          const double rr = bs - ax;
-          const T rt = (T)rr;
-          r[b] = rt;
-          rs[b] = rt;
-          accT = fmav(rt, rt, accT);
-        }
-        double acc[1] = {(double)accT};
-        if (!grid_reduce<1, 0u>(C, nblk, RED(epoch), acc, tot1)) return;
-      }
-      ++epoch;
-      double rsr = tot1[0];
-      double rho = 1.0, alpha = 1.0, omega = 1.0;
-
-      for (int it = 0; it < P.nin; ++it) {
-        const bool last = (it == P.nin - 1);
-        const double rho_prev = rho;
-        rho = rsr;
-        if (rho == 0.0 || omega == 0.0) {
-          if (lead) set_status(C, ADP_ERR_BREAKDOWN);
-          return;
-        }
-        const double beta = (rho / rho_prev) * (alpha / omega);
-        T* pN = pv[it & 1];
-        const T* pO = pv[(it & 1) ^ 1];
-        T* vN = vv[it & 1];
-        const T* vO = vv[(it & 1) ^ 1];
-        const T tb = (T)beta, tom = (T)omega, tap = (T)alpha;
-        // ---- phase A: (previous step's x and r), p and v = A p -----------
-        {
-          T accT = T(0);
-          if (it == 0) {
-            for (int b = tid0; b < NB; b += nthr) {
-              const T pb = r[b];
-              T v = Ag[b] * r[b - plane];
-              v = fmav(Ag[(size_t)NB + b], r[b - nxx], v);
-              v = fmav(Ag[(size_t)2 * NB + b], r[b - 1], v);
-              v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-              v = fmav(Ag[(size_t)4 * NB + b], r[b + 1], v);
-              v = fmav(Ag[(size_t)5 * NB + b], r[b + nxx], v);
-              v = fmav(Ag[(size_t)6 * NB + b], r[b + plane], v);
-              pN[b] = pb;
-              vN[b] = v;
-              accT = fmav(rs[b], v, accT);
-            }
-          } else {
-            const double* xc = (it == 1) ? xO : xN;
-            for (int b = tid0; b < NB; b += nthr) {
-              auto rf = [&](int m) -> T { return fmav(-tom, t[m], s[m]); };
-              auto pf = [&](int m) -> T { return fmav(tb, fmav(-tom, vO[m], pO[m]), rf(m)); };
-              const T rb = rf(b);
-              r[b] = rb;
-              if (MIXED) {
-                const T dx = fmav(tom, s[b], tap * pO[b]);
-                xN[b] = xc[b] + (double)dx;
-              } else {
-                xN[b] = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
-              }
-              const T pb = fmav(tb, fmav(-tom, vO[b], pO[b]), rb);
-              T v = Ag[b] * pf(b - plane);
-              v = fmav(Ag[(size_t)NB + b], pf(b - nxx), v);
-              v = fmav(Ag[(size_t)2 * NB + b], pf(b - 1), v);
-              v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-              v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
-              v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
-              v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
-              pN[b] = pb;
-              vN[b] = v;
-              accT = fmav(rs[b], v, accT);
-            }
-          }
-          double acc[1] = {(double)accT};
-          if (!grid_reduce<1, 0u>(C, nblk, RED(epoch), acc, tot1)) return;
-        }
-        ++epoch;
-        if (tot1[0] == 0.0) {
-          if (lead) set_status(C, ADP_ERR_BREAKDOWN);
-          return;
-        }
-        alpha = rho / tot1[0];
-        const T ta = (T)alpha;
-        // ---- phase B: s and t = A s; (t,t), (t,s) and, for the next step,
-        //      (rs,s), (rs,t): (rs, s - omega t) = (rs,s) - omega (rs,t) ------
-        double tot4[4];
-        {
-          T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
-          for (int b = tid0; b < NB; b += nthr) {
-            auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
-            const T sb = sf(b);
-            T tt = Ag[b] * sf(b - plane);
-            tt = fmav(Ag[(size_t)NB + b], sf(b - nxx), tt);
-            tt = fmav(Ag[(size_t)2 * NB + b], sf(b - 1), tt);
-            tt = fmav(Ag[(size_t)3 * NB + b], sb, tt);
-            tt = fmav(Ag[(size_t)4 * NB + b], sf(b + 1), tt);
-            tt = fmav(Ag[(size_t)5 * NB + b], sf(b + nxx), tt);
-            tt = fmav(Ag[(size_t)6 * NB + b], sf(b + plane), tt);
-            s[b] = sb;
-            t[b] = tt;
-            acc0 = fmav(tt, tt, acc0);
-            acc1 = fmav(tt, sb, acc1);
-            if (!last) {
-              const T rb = rs[b];
-              acc2 = fmav(rb, sb, acc2);
-              acc3 = fmav(rb, tt, acc3);
-            }
-          }
-          if (last) {
-            double acc[2] = {(double)acc0, (double)acc1}, tot2[2];
-            if (!grid_reduce<2, 0u>(C, nblk, RED(epoch), acc, tot2)) return;
-            tot4[0] = tot2[0];
-            tot4[1] = tot2[1];
-          } else {
-            double acc[4] = {(double)acc0, (double)acc1, (double)acc2, (double)acc3};
-            if (!grid_reduce<4, 0u>(C, nblk, RED(epoch), acc, tot4)) return;
-          }
-        }
-        ++epoch;
-        if (tot4[0] == 0.0) {
-          if (lead) set_status(C, ADP_ERR_BREAKDOWN);
-          return;
-        }
-        omega = tot4[1] / tot4[0];
-        if (!last) {
-          rsr = tot4[2] - omega * tot4[3];
-        } else {
-          // ---- phase C of the last step: x, and RelEg's running maximum.
-          // No barrier follows: the next group's P0 (or the fission source)
-          // reads only this thread's own rows of x.
-          const T to = (T)omega;
-          const double* xc = (it == 0) ? xO : xN;
-          for (int b = tid0; b < NB; b += nthr) {
-            double xn;
-            if (MIXED) {
-              // FP32 increment of the correction, accumulated into the FP64 flux
-              const T dx = fmav(to, s[b], ta * pN[b]);
-              xn = xc[b] + (double)dx;
-            } else {
-              xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
-            }
-            xN[b] = xn;
-            // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
-            const double ax = fabs(xn), d = fabs(xn - xO[b]);
-            if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
-          }
-        }
-      }
-    }
-
-    // ---- fission source, norms and eigenvalue ------------------------------
-    const bool extrap = (p % P.nac) == 0;
-    double tot4[4];
-    {
-      double acc[4] = {0.0, 0.0, 0.0, fer_acc};
-      for (int b = tid0; b < NB; b += nthr) {
-        double fs = 0.0;
-        for (int g = 0; g < ng; ++g) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
-        fsN[b] = fs;
-        const double en = fs - fsO[b];
-        acc[0] = fma(en, en, acc[0]);
-        if (!extrap) {
-          acc[1] = fma(G.vdel[b], fs, acc[1]);
-          // RelE (mod_cmfd.f90:1143-1168)
-          const double af = fabs(fs), d = fabs(en);
-          if (af > 1.e-10 && d > acc[2] * af) acc[2] = fmax(acc[2], d / af);
-        }
-      }
-      if (!grid_reduce<4, 0xCu>(C, nblk, RED(epoch), acc, tot4)) return;
-      ++epoch;
-    }
-    const double e2 = sqrt(tot4[0]);
-    double fsum = tot4[1], ser = tot4[2];
-    const double fer = tot4[3];
-    if (extrap) {
-      // fiss_extrp (mod_cmfd.f90:308-335)
-      const double domiR = e2 / e1;
-      const double c = domiR / (1.0 - domiR);
-      double acc[2] = {0.0, 0.0};
-      for (int b = tid0; b < NB; b += nthr) {
-        const double fo = fsO[b];
-        double fs = fsN[b];
-        fs = fma(c, fs - fo, fs);
-        fsN[b] = fs;
-        acc[0] = fma(G.vdel[b], fs, acc[0]);
-        const double af = fabs(fs), d = fabs(fs - fo);
-        if (af > 1.e-10 && d > acc[1] * af) acc[1] = fmax(acc[1], d / af);
-      }
-      double tot[2];
-      if (!grid_reduce<2, 0x2u>(C, nblk, RED(epoch), acc, tot)) return;
-      ++epoch;
-      fsum = tot[0];
-      ser = tot[1];
-    }
-    e1 = e2;
-    const double Keo = Ke;
-    Ke = Keo * fsum / f;
-    f = fsum;
-    cur = nw;
-
-    const bool nodal = P.do_nodal && (p % P.nupd) == 0;
-    const bool bad = !isfinite(Ke) || !isfinite(fsum);
-    const bool conv = !nodal && ser < P.serc && fer < P.ferc && ndmax < kF1em2;
-    const bool maxr = !nodal && !conv && p >= P.nout;
-    if (lead) {
-      const int q = p - 1;
-      if (q < P.nout) {
-        P.tr_k[q] = Ke;
-        P.tr_ser[q] = ser;
-        P.tr_fer[q] = fer;
-        P.tr_flags[q] = extrap ? 1 : 0;
-        P.tr_ndmax[q] = ndmax;
-      }
-    }
-    if (bad || nodal || conv || maxr) {
-      if (lead) {
-        C->Ke = Ke;
-        C->f = f;
-        C->e1 = e1;
-        C->ser = ser;
-        C->fer = fer;
-        C->p = p;
-        C->p_total = ptot;
-        C->cur = cur;
-        C->nodal_due = nodal ? 1 : 0;
-        C->converged = conv ? 1 : 0;
-        C->max_reached = maxr ? 1 : 0;
-        C->need_prologue = 0;
-        if (bad) set_status(C, ADP_ERR_NAN);
-        __threadfence();
-      }
-      return;
-    }
-  }
-#undef RED
+  outer_body<MIXED>(P, blockIdx.x, gridDim.x);
 }
 
 int outer_max_blocks_per_sm(int threads, int mixed) {
@@ -534,27 +111,8 @@ cudaError_t launch_power(const BoxGeom& G, int ng, long long NBH, const double* 
 // ---------------------------------------------------------------------------
 __global__ void k_xs_updt(BoxGeom G, int ng, const int* act, int nnod, const double* sigtr, const double* siga,
                           const double* sigs, double* D, double* sigr, OuterCtl* C) {
-  const int NB = G.NB;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnod * ng; q += gridDim.x * blockDim.x) {
-    const int g = q / nnod, n = q - g * nnod, b = act[n];
-    const double st = sigtr[(size_t)g * NB + b];
-    if (st < kF1em5) {
-      set_status(C, ADP_ERR_BADXS);
-      atomicCAS(&C->err_node, -1, b);
-      continue;
-    }
-    const double d = 1.0 / (3.0 * st);
-    double dum = 0.;
-    for (int h = 0; h < ng; ++h)
-      if (h != g) dum = dum + sigs[((size_t)g * ng + h) * NB + b];
-    const double sr = siga[(size_t)g * NB + b] + dum;
-    D[(size_t)g * NB + b] = d;
-    sigr[(size_t)g * NB + b] = sr;
-    if (d < (double)1.e-20f || sr < 0.) {
-      set_status(C, ADP_ERR_BADXS);
-      atomicCAS(&C->err_node, -1, b);
-    }
-  }
+  xs_updt_items(G, ng, act, nnod, sigtr, siga, sigs, D, sigr, C, blockIdx.x * blockDim.x + threadIdx.x,
+                gridDim.x * blockDim.x);
 }
 
 cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, const double* sigtr,

@@ -1,0 +1,93 @@
+// The single-core solver handle (device state of one core), shared by the
+// C ABI (capi.cu) and the batch (batch.cu), which owns one handle per core.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/adpres_gb300.h"
+#include "adp_kernels.h"
+
+namespace adp {
+
+// Bump allocator over one device allocation (256-byte aligned pieces).
+struct DevArena {
+  char* base = nullptr;
+  size_t size = 0, used = 0;
+  void* take(size_t bytes) {
+    size_t off = (used + 255) & ~(size_t)255;
+    used = off + bytes;
+    return base + off;
+  }
+};
+
+}  // namespace adp
+
+struct adp_handle {
+  std::string err;
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+  // geometry
+  int nxx = 0, nyy = 0, nzz = 0, nnod = 0, NB = 0, plane = 0, ng = 0;
+  long long NBH = 0;
+  std::vector<int> node2box;
+  std::vector<unsigned char> nbm;
+  std::vector<int> ysmin, ysmax, xsmin, xsmax, evbase_host;
+  std::vector<double> xdel, ydel, zdel, vdel;
+  int bcf[6] = {0, 0, 0, 0, 0, 0};
+  adp_opts o{};
+  int nmat = 0;
+  // device memory
+  adp::DevArena ar;
+  unsigned char* d_nbm = nullptr;
+  double *d_xdel = nullptr, *d_ydel = nullptr, *d_zdel = nullptr, *d_vdel = nullptr;
+  int *d_act = nullptr, *d_evbase = nullptr;
+  double *d_D = nullptr, *d_sigr = nullptr, *d_nuf = nullptr, *d_sigf = nullptr, *d_chin = nullptr;
+  double *d_sigs = nullptr, *d_dc = nullptr, *d_sigtr = nullptr, *d_siga = nullptr;
+  double *d_df = nullptr, *d_dn = nullptr, *d_A = nullptr;
+  float* d_A32 = nullptr;
+  double* d_phi[2] = {nullptr, nullptr};
+  double* d_fs[2] = {nullptr, nullptr};
+  double *d_r = nullptr, *d_rs = nullptr, *d_s = nullptr, *d_t = nullptr;
+  double* d_pv[2] = {nullptr, nullptr};
+  double* d_vv[2] = {nullptr, nullptr};
+  float *d_r32 = nullptr, *d_rs32 = nullptr, *d_s32 = nullptr, *d_t32 = nullptr;
+  float* d_pv32[2] = {nullptr, nullptr};
+  float* d_vv32[2] = {nullptr, nullptr};
+  double* d_red = nullptr;
+  adp::OuterCtl* d_ctl = nullptr;
+  adp::OuterCtl* h_ctl = nullptr;   // pinned mirror
+  double *d_tr_k = nullptr, *d_tr_ser = nullptr, *d_tr_fer = nullptr, *d_tr_ndmax = nullptr;
+  int* d_tr_flags = nullptr;
+  double *d_sanm = nullptr, *d_S = nullptr, *d_a2 = nullptr, *d_a4 = nullptr, *d_L1 = nullptr, *d_Bc = nullptr;
+  double* d_ndval = nullptr;
+  long long* d_ndkey = nullptr;
+  int* d_ndloc = nullptr;
+  double* d_pbox = nullptr;
+  // discrete adjoint (adp_adjoint_sens), allocated on its first call
+  char* adj_base = nullptr;
+  double* d_AT = nullptr;
+  float* d_AT32 = nullptr;
+  double* d_psi[2] = {nullptr, nullptr};
+  double* d_fsa[2] = {nullptr, nullptr};
+  adp::OuterCtl* d_ctla = nullptr;
+  double *d_sens = nullptr, *d_spart = nullptr;
+  // state
+  bool xs_set = false;
+  bool fwd_ok = false;        // the flux is a converged forward solution of the current XS
+  bool started[2] = {false, false};
+  int launch_blocks = 0, launch_threads = 0;
+  int sms = 0;
+  adp_timers tm{};
+};
+
+
+namespace adp {
+void set_global_error(const std::string& msg);
+BoxGeom box_geom(const adp_handle* h);
+OuterParams outer_params(adp_handle* h, int adj);
+NodalParams nodal_params(adp_handle* h, int cmode);
+}  // namespace adp

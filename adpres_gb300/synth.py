@@ -13,8 +13,9 @@ and the CPU oracle.
                    reflector, 3 fuel types, rodded top 40% in 8 assemblies.
   core_4g          17x17 assemblies with 4x4 nodes, 80 planes of 5 cm,
                    4 groups with down-scatter only.
-  batch_member     a 2-group core with a drawn radial size (20..68 nodes)
-                   and axial size (10..40 nodes), cross sections perturbed by
+  batch_member     a 2-group core with a drawn radial grid (20..68 nodes),
+                   axial size (10..40 nodes) and a cylindrical outline (fuel
+                   inside, one reflector ring), cross sections perturbed by
                    1% lognormal factors per material value.
   small_core       a small ragged core with optional ADFs, any boundary
                    conditions and 1-4 groups (parity tests).
@@ -193,8 +194,15 @@ def _split_nodes(n, max_asm=33):
     return div
 
 
-def batch_member(seed, index):
-    """One member of the batched workload: drawn radial/axial size, 1% lognormal XS perturbation."""
+def batch_member(seed, index, zref=True, zsize=10.0, nupd=100):
+    """One member of the batched workload: drawn radial/axial size, 1% lognormal XS perturbation.
+
+    zref: the first and last axial nodes are reflector (as in the 3D full
+    core); zsize: axial node height in cm.  nupd: nodal update interval.
+    The default interval ceil((nxx+nyy+nzz)/2.5) starts the nodal updates
+    before the CMFD flux of these larger cores has settled, and the
+    reference's two-node iteration then diverges on about one core in five
+    (ndmax > 1e3, mod_nodal.f90:131-142); 100 outers avoid that."""
     rng = np.random.default_rng([3000 + seed, index])
     nr = int(rng.integers(20, 69))
     nzn = int(rng.integers(10, 41))
@@ -211,13 +219,23 @@ def batch_member(seed, index):
     mats = [_mat2(**pert(REFL2))] + [_mat2(**pert(f)) for f in fuels]
     div = _split_nodes(nr)
     nx = len(div)
-    fuel = _circle_outline(nx, 0.42 * nx)
+    # cylindrical outline: fuel inside the circle, one ring of reflector
+    # assemblies, no nodes beyond (a square box with thick reflector corners
+    # drives the reference's two-node iteration unstable on the larger cores)
+    rad = 0.5 * nx
+    fuel = _circle_outline(nx, rad - 1.0)
+    core = _circle_outline(nx, rad + 0.25)
     types = rng.integers(0, 3, size=(nx, nx))
-    pl = np.where(fuel, 2 + types, 1)
+    pl = np.where(fuel, 2 + types, np.where(core, 1, 0))
     size = [10.0 * d for d in div]
-    it = [2000, 2, "1.0e-5", "1.0e-5", 5, _nupd(nr, nr, nzn), 30, 20]
-    return _deck(f"BATCH{index}", 2, mats, nx, nx, nzn, size, div, size, div, [10.0] * nzn, [1] * nzn,
-                 [pl], [1] * nzn, (1, 1, 1, 1, 1, 1), iter_=it)
+    it = [2000, 2, "1.0e-5", "1.0e-5", 5, nupd, 30, 20]
+    planars = [pl]
+    zpln = [1] * nzn
+    if zref:
+        planars.append(np.where(pl > 0, 1, 0))
+        zpln[0] = zpln[-1] = 2
+    return _deck(f"BATCH{index}", 2, mats, nx, nx, nzn, size, div, size, div, [zsize] * nzn, [1] * nzn,
+                 planars, zpln, (1, 1, 1, 1, 1, 1), iter_=it)
 
 
 def small_core(seed=0, ng=2, kern="SANM", nx=4, ny=4, nz=3, xdiv=2, ydiv=2, zdiv=1, ragged=True, adf=False,

@@ -178,6 +178,93 @@ def adjoint_leg(flush, steps=3):
     return out
 
 
+# ------------------------------------------------- batched solves leg ----
+def _batch_oracle_member(args):
+    seed, i = args
+    import oracle
+    from adpres_gb300 import synth
+    o = oracle.Oracle(text=synth.batch_member(seed, i))
+    t0 = time.perf_counter()
+    o.run()
+    return time.perf_counter() - t0
+
+
+def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
+    """256 independent two-group cores (radial 20..68, axial 10..40 nodes,
+    config-1 cross sections with 1% lognormal perturbations) in one
+    persistent launch replayed from a CUDA graph, mixed precision, schedule
+    from the autotuner (cached per batch shape).  Members are those of the
+    seeded draw that the reference algorithm converges on
+    (tests/golden/batch_members.json).  Per-instance |dk| against individual
+    single-core FP64 solves; CPU baseline: the oracle on a sample of members,
+    one process per host core."""
+    import multiprocessing as mp
+
+    import numpy as np
+    import torch
+
+    from adpres_gb300 import deck, synth
+    from adpres_gb300.batch import Batch
+    from adpres_gb300.core import Core
+
+    with open(os.path.join(ROOT, "tests", "golden", "batch_members.json")) as f:
+        acc = json.load(f)
+    seed, idx = acc["seed"], acc["accepted"][:ncores]
+    texts = [synth.batch_member(seed, i) for i in idx]
+    decks = [deck.parse(t) for t in texts]
+    nodes = int(sum(len(d.ix) for d in decks))
+    t0 = time.perf_counter()
+    b = Batch(decks, precision="mixed")
+    t_create = time.perf_counter() - t0
+    cache = os.path.join(os.path.expanduser("~"), ".cache", "adpres_gb300", "batch_tune.json")
+    t0 = time.perf_counter()
+    cfg, tune_ms, hit = b.autotune(cache)
+    t_tune = time.perf_counter() - t0
+    for _ in range(warmup):
+        b.solve()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        res, m = b.solve()
+        ms.append(m)
+    t = sum(ms) / len(ms) / 1e3
+    conv = sum(r["converged"] for r in res)
+    # individual FP64 single-core solves
+    dks = []
+    t0 = time.perf_counter()
+    for i in range(min(fp64_check, len(decks))):
+        c = Core.from_deck(decks[i], precision="fp64")
+        r = c.outer(trace=False)
+        dks.append(abs(res[i]["keff"] - r.keff) / r.keff * 1e5)
+        c.close()
+    t_fp64 = time.perf_counter() - t0
+    b.close()
+    # CPU baseline: the oracle on a sample, all host cores
+    nproc = os.cpu_count() or 1
+    sample = [(seed, i) for i in idx[:nproc]]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(nproc) as pool:
+        tcpu = pool.map(_batch_oracle_member, sample)
+    wall = time.perf_counter() - t0
+    cpu_rate = len(sample) / wall
+    return {
+        "workload": f"{len(decks)} two-group cores, radial 20..68, axial 10..40 nodes, {nodes} nodes in all "
+                    "(seeded draw, members the reference converges on), SANM, mixed precision",
+        "value": len(decks) / t, "unit": "solves/s", "ms_per_batch": t * 1e3, "steps": steps, "warmup": warmup,
+        "converged": conv, "config": cfg, "tuned_from_cache": hit, "tune_s": t_tune, "create_s": t_create,
+        "outers_mean": float(np.mean([r["outers"] for r in res])),
+        "teams": sorted({r["team"] for r in res}),
+        "dk_pcm_vs_fp64_single": {"max": float(max(dks)), "rms": float(np.sqrt(np.mean(np.square(dks)))),
+                                  "checked": len(dks), "fp64_single_s": t_fp64},
+        "cpu_baseline": {"value": cpu_rate, "unit": "solves/s", "cores": nproc, "kind": "port",
+                         "sample": f"oracle full solves of the first {len(sample)} members, one process per host core, "
+                                   f"wall {wall:.1f} s (mean {np.mean(tcpu):.1f} s per member)"},
+        "l2_flush": "256 MiB written between steps",
+    }
+
+
 # ------------------------------------------------------------ our arm ----
 def run_ours(args):
     import numpy as np
@@ -277,6 +364,7 @@ def run_ours(args):
     core64.close()
 
     adjoint = adjoint_leg(flush)
+    batched = batch_leg(flush) if not args.no_batch else None
 
     # e2e through the C ABI from host buffers
     e2e_steps = max(2, min(args.steps, 5))
@@ -317,6 +405,7 @@ def run_ours(args):
                      "launches": launches},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "adjoint": adjoint,
+        "batched": batched,
         "gpu_launches": gpu_launches,
         "clocks": ck,
         "cpu_baseline": cpu,
@@ -376,6 +465,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-solves leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         log("warm-up raised to 3 steps")

@@ -226,6 +226,62 @@ adp_status adp_power_noalloc(int nnod, int ng, const double* f0, const double* s
  * (keff is its eigenvalue).  The forward state is left unchanged. */
 adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* report);
 
+/* -- batched solves ------------------------------------------------------ */
+
+/* Many independent cores solved together; no counterpart in the reference,
+ * whose process solves one core (control::forward, mod_control.f90:11-47).
+ * A batch owns one handle per core (adp_batch_core gives it, for
+ * adp_get_state and friends) and solves all cores in one persistent
+ * cooperative launch captured in a CUDA graph: per core XS_updt, the
+ * first-call start, outer iterations with nodal updates and PowDis, each
+ * core on a team of thread blocks that synchronise only among themselves.
+ * All cores share ng (1..4), kern and precision. */
+typedef struct adp_batch adp_batch;
+
+/* Launch shape and schedule: threads per block (256 or 512), the largest
+ * team of blocks on one core, grain (cores are split into teams so that a
+ * team member's share is about 1/grain of a block's average load),
+ * blocks per SM, and whether the solve is replayed from a captured graph. */
+typedef struct adp_batch_config {
+  int threads;
+  int max_team;
+  double grain;
+  int blocks_per_sm;
+  int use_graph;
+} adp_batch_config;
+
+typedef struct adp_batch_result {
+  int status;               /* adp_status of the core                          */
+  int converged, outers, nodal_updates;
+  double keff, ser, fer, ndmax;
+  double device_ms;         /* device time of the core's team (global timer)   */
+  int team;                 /* blocks that solved it                           */
+} adp_batch_result;
+
+adp_status adp_batch_create(int n, const adp_geom* geoms, const adp_opts* opts, adp_batch** out);
+adp_status adp_batch_destroy(adp_batch* b);
+size_t adp_batch_last_error(const adp_batch* b, char* buf, size_t len);
+/* Node-wise cross sections of core i, as adp_xs_updt_nodes. */
+adp_status adp_batch_set_xs(adp_batch* b, int i, int nmat, const double* sigtr, const double* siga, const double* nuf,
+                            const double* sigf, const double* chi, const int* mat, const double* sigs,
+                            const double* dc);
+adp_status adp_batch_set_config(adp_batch* b, const adp_batch_config* c);
+adp_status adp_batch_get_config(const adp_batch* b, adp_batch_config* c);
+/* Solve every core from a fresh start; res has n entries (may be NULL);
+ * device_ms is the whole launch (CUDA events).  Returns the first failing
+ * core's status, or ADP_OK. */
+adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_ms);
+/* Time the batch over block size, max_team and grain (schedules built from
+ * the measured per-core times of one solve) and keep the fastest. */
+adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best, double* best_ms);
+adp_status adp_batch_core(adp_batch* b, int i, adp_handle** h);
+/* Per-outer trace of core i from the last adp_batch_solve (as the trace of
+ * adp_report; any array may be NULL); returns the number of entries written
+ * (at most cap), or -1 on bad arguments. */
+int adp_batch_trace(adp_batch* b, int i, int cap, double* k, double* ser, double* fer, int* flags, double* ndmax);
+/* Normalised node power of core i after adp_batch_solve (nnod entries). */
+adp_status adp_batch_power(adp_batch* b, int i, double* p);
+
 /* Device timers of the handle. */
 adp_status adp_get_timers(const adp_handle* h, adp_timers* t);
 

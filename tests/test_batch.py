@@ -1,0 +1,165 @@
+"""Batched solves (adp_batch_*) against single-core solves and the oracle.
+
+Each core of a batch is solved by a team of thread blocks inside one
+persistent launch; its result must be the single-core path's result on the
+same inputs: FP64 batch vs FP64 single core within 0.1 pcm and 1e-6 in
+nodal power (the team's reductions group the partial sums differently, so
+bits may differ), mixed batch vs FP64 within 1 pcm and 0.1%.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from adpres_gb300 import deck, synth
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+def _accepted():
+    """Members of the batched workload the reference converges on, with the
+    oracle's (k, outers) (tests/golden/make_batch_members.py)."""
+    with open(os.path.join(GOLDEN, "batch_members.json")) as f:
+        return json.load(f)
+
+
+def pcm(a, b):
+    return abs(a - b) / abs(b) * 1e5
+
+
+def max_rel(a, b):
+    m = np.abs(b) > 0
+    return float(np.max(np.abs(a[m] - b[m]) / np.abs(b[m])))
+
+
+def _single(text, precision="fp64"):
+    from adpres_gb300.core import Core
+    c = Core.from_deck(deck.parse(text), precision=precision)
+    rep = c.outer(trace=False)
+    return rep, c.power()
+
+
+@pytest.fixture(scope="module")
+def members():
+    acc = _accepted()
+    return [synth.batch_member(acc["seed"], i) for i in acc["accepted"][:6]]
+
+
+def test_batch_matches_oracle_on_workload_members():
+    """FP64 batch of six workload members against the oracle's k (0.1 pcm)."""
+    from adpres_gb300.batch import Batch
+    acc = _accepted()
+    idx = acc["accepted"][:6]
+    b = Batch([deck.parse(synth.batch_member(acc["seed"], i)) for i in idx], precision="fp64")
+    res, _ = b.solve()
+    for r, i in zip(res, idx):
+        k_ora, outers_ora = acc["oracle"][str(i)]
+        assert r["converged"] == 1
+        assert pcm(r["keff"], k_ora) <= 0.1, (i, r["keff"], k_ora)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_single_core_solves(members, precision):
+    from adpres_gb300.batch import Batch
+    b = Batch([deck.parse(t) for t in members], precision=precision)
+    res, ms = b.solve()
+    assert ms > 0
+    for i, t in enumerate(members):
+        r64, p64 = _single(t, "fp64")
+        assert res[i]["status"] == 0 and res[i]["converged"] == 1
+        tol_k, tol_p = (0.1, 1e-6) if precision == "fp64" else (1.0, 1e-3)
+        assert pcm(res[i]["keff"], r64.keff) <= tol_k, (i, res[i], r64.keff)
+        assert max_rel(b.power(i), p64) <= tol_p
+        f0, k = b.state(i)
+        assert k == res[i]["keff"]
+
+
+def test_batch_matches_oracle_small_cores():
+    """Four small ragged cores (two with ADFs) in one FP64 batch against the
+    oracle: same outer count, |dk| <= 0.1 pcm, power <= 1e-6."""
+    from adpres_gb300.batch import Batch
+    texts = [synth.small_core(seed=s, ng=2, adf=(s % 2 == 1), bc=(1, 2, 1, 2, 1, 1)) for s in range(20, 24)]
+    b = Batch([deck.parse(t) for t in texts], precision="fp64")
+    res, _ = b.solve()
+    for i, t in enumerate(texts):
+        o = oracle.Oracle(text=t)
+        o.run()
+        assert res[i]["outers"] == o.geti("outers")
+        assert pcm(res[i]["keff"], o.getd("Ke")) <= 0.1
+        assert max_rel(b.power(i), o.powdis()) <= 1e-6
+
+
+@pytest.mark.parametrize("kern", ["FDM", "PNM"])
+def test_batch_other_kernels(kern):
+    from adpres_gb300.batch import Batch
+    texts = [synth.small_core(seed=s, ng=2, kern=kern, bc=(1, 1, 1, 1, 2, 1)) for s in range(30, 33)]
+    b = Batch([deck.parse(t) for t in texts], precision="fp64")
+    res, _ = b.solve()
+    for i, t in enumerate(texts):
+        r, p = _single(t)
+        assert res[i]["converged"] == 1
+        assert pcm(res[i]["keff"], r.keff) <= 0.1
+        assert max_rel(b.power(i), p) <= 1e-6
+
+
+def test_team_sizes_give_the_same_answer(members):
+    """A core solved by one block or by a team of blocks converges to the
+    same eigenvalue (the partial sums are grouped differently)."""
+    from adpres_gb300.batch import Batch
+    b = Batch([deck.parse(t) for t in members[:4]], precision="fp64")
+    b.set_config(max_team=1)
+    r1, _ = b.solve()
+    b.set_config(max_team=16, grain=4.0)
+    r2, _ = b.solve()
+    assert any(r["team"] > 1 for r in r2)
+    for a, c in zip(r1, r2):
+        assert pcm(a["keff"], c["keff"]) <= 0.01
+
+
+def test_graph_and_direct_launch_agree(members):
+    from adpres_gb300.batch import Batch
+    b = Batch([deck.parse(t) for t in members[:3]], precision="mixed")
+    b.set_config(use_graph=1)
+    rg, _ = b.solve()
+    rg2, _ = b.solve()
+    b.set_config(use_graph=0)
+    rd, _ = b.solve()
+    for a, c, d in zip(rg, rg2, rd):
+        assert a["keff"] == c["keff"] == d["keff"]
+        assert a["outers"] == c["outers"] == d["outers"]
+
+
+def test_autotune_and_cache(members, tmp_path):
+    from adpres_gb300.batch import Batch
+    decks = [deck.parse(t) for t in members]
+    b = Batch(decks, precision="mixed")
+    cache = str(tmp_path / "tune.json")
+    cfg, ms, hit = b.autotune(cache)
+    assert not hit and ms > 0 and cfg["threads"] in (256, 512)
+    res, _ = b.solve()
+    assert all(r["converged"] == 1 for r in res)
+    b2 = Batch(decks, precision="mixed")
+    cfg2, ms2, hit2 = b2.autotune(cache)
+    assert hit2 and cfg2 == cfg
+    assert b2.config()["threads"] == cfg["threads"]
+
+
+def test_bad_cross_section_is_reported_per_core():
+    from adpres_gb300._lib import AdpError, ADP_ERR_BADXS
+    from adpres_gb300.batch import Batch, node_tables
+    texts = [synth.small_core(seed=s, ng=2) for s in (40, 41)]
+    decks = [deck.parse(t) for t in texts]
+    b = Batch(decks, precision="fp64")
+    t = node_tables(decks[1])
+    bad = t["sigtr"].copy()
+    bad[3, 1] = 1e-7
+    with pytest.raises(AdpError) as e:
+        b.set_xs(1, bad, t["siga"], t["nuf"], t["sigf"], decks[1].chi, decks[1].mat, t["sigs"], decks[1].dc)
+    assert e.value.status == ADP_ERR_BADXS
+    # the batch stays usable once good cross sections are back
+    b.set_xs(1, t["sigtr"], t["siga"], t["nuf"], t["sigf"], decks[1].chi, decks[1].mat, t["sigs"], decks[1].dc)
+    res, _ = b.solve()
+    assert all(r["converged"] == 1 for r in res)
