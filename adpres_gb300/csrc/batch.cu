@@ -444,8 +444,8 @@ adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best_out, double* 
   adp_batch_config best = base;
   double best_t = 1e300;
   const int threads[2] = {256, 512};
-  const int teams[5] = {1, 2, 4, 8, 16};
-  const double grains[2] = {1.0, 2.0};
+  const int teams[3] = {2, 8, 32};
+  const double grains[2] = {1.0, 4.0};
   const std::vector<double> meas = b->measured;
   for (int th : threads) {
     if (batch_max_blocks_per_sm(b->mixed, b->ng, th) < 1) continue;

@@ -271,8 +271,9 @@ adp_status adp_batch_get_config(const adp_batch* b, adp_batch_config* c);
  * device_ms is the whole launch (CUDA events).  Returns the first failing
  * core's status, or ADP_OK. */
 adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_ms);
-/* Time the batch over block size, max_team and grain (schedules built from
- * the measured per-core times of one solve) and keep the fastest. */
+/* Time the batch over block size {256, 512} x max_team {2, 8, 32} x grain
+ * {1, 4} (schedules built from the measured per-core times of one solve)
+ * and keep the fastest: 13 solves of the whole batch. */
 adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best, double* best_ms);
 adp_status adp_batch_core(adp_batch* b, int i, adp_handle** h);
 /* Per-outer trace of core i from the last adp_batch_solve (as the trace of
