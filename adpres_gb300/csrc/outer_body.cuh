@@ -21,6 +21,31 @@ __device__ __forceinline__ T vld(const T* p) {
   return *(const volatile T*)p;
 }
 
+// The rows b, b + nthr, b + 2 nthr, ... of one thread, R at a time: `ld`
+// computes a row's results from loads only, `ex` stores them and adds to
+// the thread's partial sums, in the original row order.  Issuing the loads
+// of R rows before any store lets them overlap (a store may alias a later
+// row's loads for all the compiler knows), without changing any value or
+// the order of any sum.
+template <int R, class Ld, class Ex>
+__device__ __forceinline__ void rows_batched(int b, int nthr, int NB, Ld&& ld, Ex&& ex) {
+  using Row = decltype(ld(0));
+  for (; b + (R - 1) * nthr < NB; b += R * nthr) {
+    Row v[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) v[u] = ld(b + u * nthr);
+#pragma unroll
+    for (int u = 0; u < R; ++u) ex(b + u * nthr, v[u]);
+  }
+  for (; b < NB; b += nthr) ex(b, ld(b));
+}
+
+// Rows in flight per thread in the row loops.
+template <bool MIXED>
+struct RowsInFlight { static constexpr int R = 2; };
+template <>
+struct RowsInFlight<true> { static constexpr int R = 4; };
+
 // ---------------------------------------------------------------------------
 // The persistent outer-iteration loop.
 //
@@ -130,29 +155,34 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       double tot1[1];
       {
         T accT = T(0);
-        for (int b = tid0; b < NB; b += nthr) {
-          double s0 = 0.0;
-          for (int h = 0; h < ng; ++h) {
-            if (h == g) continue;
-            const bool solved = P.adj ? (h > g) : (h < g);
-            const double ph = (solved ? phiN : phiO)[(size_t)h * NBH + b];
-            const double sg = P.adj ? P.sigs[((size_t)g * ng + h) * NB + b] : P.sigs[((size_t)h * ng + g) * NB + b];
-            s0 = fma(sg, ph, s0);
-          }
-          const double bs = wsrc[b] * fsO[b] * invKe + s0;
-          double ax = A64[b] * xO[b - plane];
-          ax = fma(A64[(size_t)NB + b], xO[b - nxx], ax);
-          ax = fma(A64[(size_t)2 * NB + b], xO[b - 1], ax);
-          ax = fma(A64[(size_t)3 * NB + b], xO[b], ax);
-          ax = fma(A64[(size_t)4 * NB + b], xO[b + 1], ax);
-          ax = fma(A64[(size_t)5 * NB + b], xO[b + nxx], ax);
-          ax = fma(A64[(size_t)6 * NB + b], xO[b + plane], ax);
-          const double rr = bs - ax;
-          const T rt = (T)rr;
-          r[b] = rt;
-          rs[b] = rt;
-          accT = fmav(rt, rt, accT);
-        }
+        rows_batched<RowsInFlight<MIXED>::R>(
+            tid0, nthr, NB,
+            [&](int b) -> T {
+              double s0 = 0.0;
+              for (int h = 0; h < ng; ++h) {
+                if (h == g) continue;
+                const bool solved = P.adj ? (h > g) : (h < g);
+                const double ph = (solved ? phiN : phiO)[(size_t)h * NBH + b];
+                const double sg =
+                    P.adj ? P.sigs[((size_t)g * ng + h) * NB + b] : P.sigs[((size_t)h * ng + g) * NB + b];
+                s0 = fma(sg, ph, s0);
+              }
+              const double bs = wsrc[b] * fsO[b] * invKe + s0;
+              double ax = A64[b] * xO[b - plane];
+              ax = fma(A64[(size_t)NB + b], xO[b - nxx], ax);
+              ax = fma(A64[(size_t)2 * NB + b], xO[b - 1], ax);
+              ax = fma(A64[(size_t)3 * NB + b], xO[b], ax);
+              ax = fma(A64[(size_t)4 * NB + b], xO[b + 1], ax);
+              ax = fma(A64[(size_t)5 * NB + b], xO[b + nxx], ax);
+              ax = fma(A64[(size_t)6 * NB + b], xO[b + plane], ax);
+              const double rr = bs - ax;
+              return (T)rr;
+            },
+            [&](int b, T rt) {
+              r[b] = rt;
+              rs[b] = rt;
+              accT = fmav(rt, rt, accT);
+            });
         double acc[1] = {(double)accT};
         if (!grid_reduce<1, 0u>(C, nblk, rank, RED(epoch), acc, tot1)) return;
       }
@@ -178,44 +208,58 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
         {
           T accT = T(0);
           if (it == 0) {
-            for (int b = tid0; b < NB; b += nthr) {
-              const T pb = r[b];
-              T v = Ag[b] * r[b - plane];
-              v = fmav(Ag[(size_t)NB + b], r[b - nxx], v);
-              v = fmav(Ag[(size_t)2 * NB + b], r[b - 1], v);
-              v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-              v = fmav(Ag[(size_t)4 * NB + b], r[b + 1], v);
-              v = fmav(Ag[(size_t)5 * NB + b], r[b + nxx], v);
-              v = fmav(Ag[(size_t)6 * NB + b], r[b + plane], v);
-              pN[b] = pb;
-              vN[b] = v;
-              accT = fmav(rs[b], v, accT);
-            }
+            struct RowA0 { T pb, v, rsb; };
+            rows_batched<RowsInFlight<MIXED>::R>(
+                tid0, nthr, NB,
+                [&](int b) -> RowA0 {
+                  const T pb = r[b];
+                  T v = Ag[b] * r[b - plane];
+                  v = fmav(Ag[(size_t)NB + b], r[b - nxx], v);
+                  v = fmav(Ag[(size_t)2 * NB + b], r[b - 1], v);
+                  v = fmav(Ag[(size_t)3 * NB + b], pb, v);
+                  v = fmav(Ag[(size_t)4 * NB + b], r[b + 1], v);
+                  v = fmav(Ag[(size_t)5 * NB + b], r[b + nxx], v);
+                  v = fmav(Ag[(size_t)6 * NB + b], r[b + plane], v);
+                  return RowA0{pb, v, rs[b]};
+                },
+                [&](int b, const RowA0& q) {
+                  pN[b] = q.pb;
+                  vN[b] = q.v;
+                  accT = fmav(q.rsb, q.v, accT);
+                });
           } else {
             const double* xc = (it == 1) ? xO : xN;
-            for (int b = tid0; b < NB; b += nthr) {
-              auto rf = [&](int m) -> T { return fmav(-tom, t[m], s[m]); };
-              auto pf = [&](int m) -> T { return fmav(tb, fmav(-tom, vO[m], pO[m]), rf(m)); };
-              const T rb = rf(b);
-              r[b] = rb;
-              if (MIXED) {
-                const T dx = fmav(tom, s[b], tap * pO[b]);
-                xN[b] = xc[b] + (double)dx;
-              } else {
-                xN[b] = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
-              }
-              const T pb = fmav(tb, fmav(-tom, vO[b], pO[b]), rb);
-              T v = Ag[b] * pf(b - plane);
-              v = fmav(Ag[(size_t)NB + b], pf(b - nxx), v);
-              v = fmav(Ag[(size_t)2 * NB + b], pf(b - 1), v);
-              v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-              v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
-              v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
-              v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
-              pN[b] = pb;
-              vN[b] = v;
-              accT = fmav(rs[b], v, accT);
-            }
+            struct RowA { T rb, pb, v, rsb; double xn; };
+            rows_batched<RowsInFlight<MIXED>::R>(
+                tid0, nthr, NB,
+                [&](int b) -> RowA {
+                  auto rf = [&](int m) -> T { return fmav(-tom, t[m], s[m]); };
+                  auto pf = [&](int m) -> T { return fmav(tb, fmav(-tom, vO[m], pO[m]), rf(m)); };
+                  const T rb = rf(b);
+                  double xn;
+                  if (MIXED) {
+                    const T dx = fmav(tom, s[b], tap * pO[b]);
+                    xn = xc[b] + (double)dx;
+                  } else {
+                    xn = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
+                  }
+                  const T pb = fmav(tb, fmav(-tom, vO[b], pO[b]), rb);
+                  T v = Ag[b] * pf(b - plane);
+                  v = fmav(Ag[(size_t)NB + b], pf(b - nxx), v);
+                  v = fmav(Ag[(size_t)2 * NB + b], pf(b - 1), v);
+                  v = fmav(Ag[(size_t)3 * NB + b], pb, v);
+                  v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
+                  v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
+                  v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
+                  return RowA{rb, pb, v, rs[b], xn};
+                },
+                [&](int b, const RowA& q) {
+                  r[b] = q.rb;
+                  xN[b] = q.xn;
+                  pN[b] = q.pb;
+                  vN[b] = q.v;
+                  accT = fmav(q.rsb, q.v, accT);
+                });
           }
           double acc[1] = {(double)accT};
           if (!grid_reduce<1, 0u>(C, nblk, rank, RED(epoch), acc, tot1)) return;
@@ -232,26 +276,31 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
         double tot4[4];
         {
           T acc0 = T(0), acc1 = T(0), acc2 = T(0), acc3 = T(0);
-          for (int b = tid0; b < NB; b += nthr) {
-            auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
-            const T sb = sf(b);
-            T tt = Ag[b] * sf(b - plane);
-            tt = fmav(Ag[(size_t)NB + b], sf(b - nxx), tt);
-            tt = fmav(Ag[(size_t)2 * NB + b], sf(b - 1), tt);
-            tt = fmav(Ag[(size_t)3 * NB + b], sb, tt);
-            tt = fmav(Ag[(size_t)4 * NB + b], sf(b + 1), tt);
-            tt = fmav(Ag[(size_t)5 * NB + b], sf(b + nxx), tt);
-            tt = fmav(Ag[(size_t)6 * NB + b], sf(b + plane), tt);
-            s[b] = sb;
-            t[b] = tt;
-            acc0 = fmav(tt, tt, acc0);
-            acc1 = fmav(tt, sb, acc1);
-            if (!last) {
-              const T rb = rs[b];
-              acc2 = fmav(rb, sb, acc2);
-              acc3 = fmav(rb, tt, acc3);
-            }
-          }
+          struct RowB { T sb, tt, rsb; };
+          rows_batched<RowsInFlight<MIXED>::R>(
+              tid0, nthr, NB,
+              [&](int b) -> RowB {
+                auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
+                const T sb = sf(b);
+                T tt = Ag[b] * sf(b - plane);
+                tt = fmav(Ag[(size_t)NB + b], sf(b - nxx), tt);
+                tt = fmav(Ag[(size_t)2 * NB + b], sf(b - 1), tt);
+                tt = fmav(Ag[(size_t)3 * NB + b], sb, tt);
+                tt = fmav(Ag[(size_t)4 * NB + b], sf(b + 1), tt);
+                tt = fmav(Ag[(size_t)5 * NB + b], sf(b + nxx), tt);
+                tt = fmav(Ag[(size_t)6 * NB + b], sf(b + plane), tt);
+                return RowB{sb, tt, last ? T(0) : rs[b]};
+              },
+              [&](int b, const RowB& q) {
+                s[b] = q.sb;
+                t[b] = q.tt;
+                acc0 = fmav(q.tt, q.tt, acc0);
+                acc1 = fmav(q.tt, q.sb, acc1);
+                if (!last) {
+                  acc2 = fmav(q.rsb, q.sb, acc2);
+                  acc3 = fmav(q.rsb, q.tt, acc3);
+                }
+              });
           if (last) {
             double acc[2] = {(double)acc0, (double)acc1}, tot2[2];
             if (!grid_reduce<2, 0u>(C, nblk, rank, RED(epoch), acc, tot2)) return;
@@ -276,20 +325,26 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           // reads only this thread's own rows of x.
           const T to = (T)omega;
           const double* xc = (it == 0) ? xO : xN;
-          for (int b = tid0; b < NB; b += nthr) {
-            double xn;
-            if (MIXED) {
-              // FP32 increment of the correction, accumulated into the FP64 flux
-              const T dx = fmav(to, s[b], ta * pN[b]);
-              xn = xc[b] + (double)dx;
-            } else {
-              xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
-            }
-            xN[b] = xn;
-            // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
-            const double ax = fabs(xn), d = fabs(xn - xO[b]);
-            if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
-          }
+          struct RowC { double xn, xo; };
+          rows_batched<RowsInFlight<MIXED>::R>(
+              tid0, nthr, NB,
+              [&](int b) -> RowC {
+                double xn;
+                if (MIXED) {
+                  // FP32 increment of the correction, accumulated into the FP64 flux
+                  const T dx = fmav(to, s[b], ta * pN[b]);
+                  xn = xc[b] + (double)dx;
+                } else {
+                  xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
+                }
+                return RowC{xn, xO[b]};
+              },
+              [&](int b, const RowC& q) {
+                xN[b] = q.xn;
+                // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
+                const double ax = fabs(q.xn), d = fabs(q.xn - q.xo);
+                if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
+              });
         }
       }
     }
@@ -299,19 +354,25 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     double tot4[4];
     {
       double acc[4] = {0.0, 0.0, 0.0, fer_acc};
-      for (int b = tid0; b < NB; b += nthr) {
-        double fs = 0.0;
-        for (int g = 0; g < ng; ++g) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
-        fsN[b] = fs;
-        const double en = fs - fsO[b];
-        acc[0] = fma(en, en, acc[0]);
-        if (!extrap) {
-          acc[1] = fma(G.vdel[b], fs, acc[1]);
-          // RelE (mod_cmfd.f90:1143-1168)
-          const double af = fabs(fs), d = fabs(en);
-          if (af > 1.e-10 && d > acc[2] * af) acc[2] = fmax(acc[2], d / af);
-        }
-      }
+      struct RowF { double fs, fo, vd; };
+      rows_batched<RowsInFlight<MIXED>::R>(
+          tid0, nthr, NB,
+          [&](int b) -> RowF {
+            double fs = 0.0;
+            for (int g = 0; g < ng; ++g) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
+            return RowF{fs, fsO[b], G.vdel[b]};
+          },
+          [&](int b, const RowF& q) {
+            fsN[b] = q.fs;
+            const double en = q.fs - q.fo;
+            acc[0] = fma(en, en, acc[0]);
+            if (!extrap) {
+              acc[1] = fma(q.vd, q.fs, acc[1]);
+              // RelE (mod_cmfd.f90:1143-1168)
+              const double af = fabs(q.fs), d = fabs(en);
+              if (af > 1.e-10 && d > acc[2] * af) acc[2] = fmax(acc[2], d / af);
+            }
+          });
       if (!grid_reduce<4, 0xCu>(C, nblk, rank, RED(epoch), acc, tot4)) return;
       ++epoch;
     }
