@@ -24,7 +24,7 @@ namespace adp {
 // A^T in the same 7-slot layout: the coefficient of x[b + off_c] in row b of
 // A^T is the coefficient of x[b] in row b + off_c of A, i.e. that row's
 // opposite slot.
-__global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, float* AT32) {
+__global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, float* AT32, float* AT32lo) {
   const int NB = G.NB;
   const long long total = (long long)NB * ng;
   const int off[7] = {-G.plane, -G.nxx, -1, 0, 1, G.nxx, G.plane};
@@ -39,16 +39,21 @@ __global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, floa
       if (c == 3) v = Ag[(size_t)3 * NB + b];
       else if ((m & NB_ACTIVE) && (m & (1u << face[c]))) v = Ag[(size_t)(6 - c) * NB + b + off[c]];
       AT[(size_t)g * 7 * NB + (size_t)c * NB + b] = v;
-      if (AT32) AT32[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)v;
+      if (AT32) {
+        const float hi = (float)v;
+        AT32[(size_t)g * 7 * NB + (size_t)c * NB + b] = hi;
+        if (AT32lo) AT32lo[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)(v - (double)hi);
+      }
     }
   }
 }
 
-cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, cudaStream_t st) {
+cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, float* AT32lo,
+                             cudaStream_t st) {
   long long total = (long long)G.NB * ng;
   int blocks = (int)((total + 255) / 256);
   if (blocks > 65535 * 4) blocks = 65535 * 4;
-  k_transpose<<<blocks, 256, 0, st>>>(G, ng, A, AT, AT32);
+  k_transpose<<<blocks, 256, 0, st>>>(G, ng, A, AT, AT32, AT32lo);
   return cudaGetLastError();
 }
 

@@ -39,6 +39,21 @@ struct OuterParams {
   float* s32;
   float* t32;
   double* red;                // [2][kRedQ][kMaxBlocks]
+  // Double-float (hi + lo FP32 pairs) state of the mixed path: the defect
+  // correction and the flux and fission-source updates run on these.
+  const float* A32lo;         // [ng][7][NB] A - A32
+  float* xh[2];               // flux [ng][NBH] (halo offset applied)
+  float* xl[2];
+  float* fsh[2];              // fission source [NB]
+  float* fsl[2];
+  const float* wsrc_h;        // [ng][NB]
+  const float* wsrc_l;
+  const float* wfis_h;
+  const float* wfis_l;
+  const float* sigs_h;        // [ng][ng][NB]
+  const float* sigs_l;
+  const float* vdel_h;        // [NB]
+  const float* vdel_l;
   OuterCtl* ctl;
   double* tr_k;
   double* tr_ser;
@@ -89,6 +104,7 @@ struct AssembleParams {
   const double* dn;
   double* A;
   float* A32;
+  float* A32lo;               // A - A32 (mixed path), may be null
 };
 
 // Contraction of forward and adjoint fluxes into dk/dSigma (adjoint.cu).
@@ -139,7 +155,10 @@ cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st);
 cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, const double* sigtr,
                            const double* siga, const double* sigs, double* D, double* sigr, OuterCtl* ctl,
                            cudaStream_t st);
-cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, cudaStream_t st);
+cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, float* AT32lo,
+                             cudaStream_t st);
+// x = hi + lo with hi = (float)x (double-float copies of the mixed path)
+cudaError_t launch_split(const double* x, float* hi, float* lo, long long n, cudaStream_t st);
 cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st);
 // batched solve (batch_k_*.cu): a cooperative launch of `blocks` blocks
 cudaError_t launch_batch(bool mixed, int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,

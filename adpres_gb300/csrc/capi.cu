@@ -329,6 +329,14 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
   add(NB * 8 * 2);                  // fs
   add(NBH * 8 * 8);                 // Krylov FP64
   if (mixed) add(NBH * 4 * 8);      // Krylov FP32
+  if (mixed) {                      // double-float state: A lo, flux, fission source, XS copies
+    add(G * 7 * NB * 4);
+    for (int q = 0; q < 4; ++q) add(G * NBH * 4);
+    for (int q = 0; q < 4; ++q) add(NB * 4);
+    for (int q = 0; q < 4; ++q) add(G * NB * 4);
+    for (int q = 0; q < 2; ++q) add(G * G * NB * 4);
+    for (int q = 0; q < 2; ++q) add(NB * 4);
+  }
   add(2 * kRedQ * kMaxBlocks * 8);
   add(sizeof(OuterCtl));
   add(nout * 8 * 4 + nout * 4);
@@ -374,6 +382,25 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
     for (int q = 0; q < 8; ++q) *kq[q] = kf + (size_t)q * NBH + h->plane;
   }
   h->d_red = (double*)A.take(2 * kRedQ * kMaxBlocks * 8);
+  if (mixed) {
+    h->d_A32lo = (float*)A.take(G * 7 * NB * 4);
+    for (int t = 0; t < 2; ++t) {
+      h->d_xh[t] = (float*)A.take(G * NBH * 4) + h->plane;
+      h->d_xl[t] = (float*)A.take(G * NBH * 4) + h->plane;
+    }
+    for (int t = 0; t < 2; ++t) {
+      h->d_fsh[t] = (float*)A.take(NB * 4);
+      h->d_fsl[t] = (float*)A.take(NB * 4);
+    }
+    h->d_chin_h = (float*)A.take(G * NB * 4);
+    h->d_chin_l = (float*)A.take(G * NB * 4);
+    h->d_nuf_h = (float*)A.take(G * NB * 4);
+    h->d_nuf_l = (float*)A.take(G * NB * 4);
+    h->d_sigs_h = (float*)A.take(G * G * NB * 4);
+    h->d_sigs_l = (float*)A.take(G * G * NB * 4);
+    h->d_vdel_h = (float*)A.take(NB * 4);
+    h->d_vdel_l = (float*)A.take(NB * 4);
+  }
   h->d_ctl = (OuterCtl*)A.take(sizeof(OuterCtl));
   h->d_tr_k = (double*)A.take(nout * 8);
   h->d_tr_ser = (double*)A.take(nout * 8);
@@ -403,6 +430,10 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
       (ce = cudaMemcpyAsync(h->d_vdel, h->vdel.data(), NB * 8, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(h->d_act, h->node2box.data(), nn * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess ||
       (ce = cudaMemcpyAsync(h->d_evbase, h->evbase_host.data(), 3 * NB * 4, cudaMemcpyHostToDevice, h->st)) != cudaSuccess) {
+    adp_destroy(h);
+    return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
+  }
+  if (mixed && (ce = launch_split(h->d_vdel, h->d_vdel_h, h->d_vdel_l, (long long)NB, h->st)) != cudaSuccess) {
     adp_destroy(h);
     return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
   }
@@ -518,6 +549,12 @@ NodalParams adp::nodal_params(adp_handle* h, int cmode) {
 extern "C" {
 
 static adp_status after_xs(adp_handle* h) {
+  if (h->o.precision == ADP_MIXED) {
+    const long long gn = (long long)h->ng * h->NB;
+    CK(launch_split(h->d_chin, h->d_chin_h, h->d_chin_l, gn, h->st));
+    CK(launch_split(h->d_nuf, h->d_nuf_h, h->d_nuf_l, gn, h->st));
+    CK(launch_split(h->d_sigs, h->d_sigs_h, h->d_sigs_l, gn * h->ng, h->st));
+  }
   if (h->o.kern == ADP_KERN_SANM) {
     // get_ABEFGH depends on sigr, D and the node sizes only
     NodalParams P = nodal_params(h, 1);
@@ -643,6 +680,21 @@ OuterParams adp::outer_params(adp_handle* h, int adj) {
   P.s32 = h->d_s32;
   P.t32 = h->d_t32;
   P.red = h->d_red;
+  P.A32lo = h->d_A32lo;
+  for (int t = 0; t < 2; ++t) {
+    P.xh[t] = h->d_xh[t];
+    P.xl[t] = h->d_xl[t];
+    P.fsh[t] = h->d_fsh[t];
+    P.fsl[t] = h->d_fsl[t];
+  }
+  P.wsrc_h = adj ? h->d_nuf_h : h->d_chin_h;
+  P.wsrc_l = adj ? h->d_nuf_l : h->d_chin_l;
+  P.wfis_h = adj ? h->d_chin_h : h->d_nuf_h;
+  P.wfis_l = adj ? h->d_chin_l : h->d_nuf_l;
+  P.sigs_h = h->d_sigs_h;
+  P.sigs_l = h->d_sigs_l;
+  P.vdel_h = h->d_vdel_h;
+  P.vdel_l = h->d_vdel_l;
   P.ctl = h->d_ctl;
   P.tr_k = h->d_tr_k;
   P.tr_ser = h->d_tr_ser;
@@ -724,6 +776,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   AP.dn = h->d_dn;
   AP.A = h->d_A;
   AP.A32 = h->d_A32;
+  AP.A32lo = h->d_A32lo;
   CK(launch_assemble(AP, h->st));
   OuterParams P = outer_params(h, adj);
   // first-call start (mod_cmfd.f90:448-454 / :635-641)
@@ -946,7 +999,7 @@ static adp_status adj_alloc(adp_handle* h) {
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += ((b + 255) & ~(size_t)255) + 256; };
   add(G * 7 * NB * 8);
-  if (mixed) add(G * 7 * NB * 4);
+  if (mixed) add(G * 7 * NB * 4 * 2);
   add(G * NBH * 8 * 2);
   add(NB * 8 * 2);
   add(sizeof(OuterCtl));
@@ -957,7 +1010,10 @@ static adp_status adj_alloc(adp_handle* h) {
   CK(cudaMalloc((void**)&A.base, bytes));
   h->adj_base = A.base;
   h->d_AT = (double*)A.take(G * 7 * NB * 8);
-  if (mixed) h->d_AT32 = (float*)A.take(G * 7 * NB * 4);
+  if (mixed) {
+    h->d_AT32 = (float*)A.take(G * 7 * NB * 4);
+    h->d_AT32lo = (float*)A.take(G * 7 * NB * 4);
+  }
   for (int t = 0; t < 2; ++t) h->d_psi[t] = (double*)A.take(G * NBH * 8) + h->plane;
   for (int t = 0; t < 2; ++t) h->d_fsa[t] = (double*)A.take(NB * 8);
   h->d_ctla = (OuterCtl*)A.take(sizeof(OuterCtl));
@@ -981,10 +1037,11 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
   CK(cudaStreamSynchronize(h->st));
   const OuterCtl fwd = *h->h_ctl;
   // A^T of the converged forward matrix (dn frozen)
-  CK(launch_transpose(box_geom(h), h->ng, h->d_A, h->d_AT, h->d_AT32, h->st));
+  CK(launch_transpose(box_geom(h), h->ng, h->d_A, h->d_AT, h->d_AT32, h->d_AT32lo, h->st));
   OuterParams P = outer_params(h, 1);
   P.A = h->d_AT;
   P.A32 = h->d_AT32;
+  P.A32lo = h->d_AT32lo;
   for (int t = 0; t < 2; ++t) {
     P.phi[t] = h->d_psi[t];
     P.fs[t] = h->d_fsa[t];

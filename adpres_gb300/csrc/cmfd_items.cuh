@@ -31,6 +31,7 @@ __device__ __forceinline__ void assemble_items(const AssembleParams& P, long lon
       for (int c = 0; c < 7; ++c) {
         A[(size_t)c * NB + b] = 0.0;
         if (P.A32) P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = 0.0f;
+        if (P.A32lo) P.A32lo[(size_t)g * 7 * NB + (size_t)c * NB + b] = 0.0f;
       }
       continue;
     }
@@ -69,7 +70,11 @@ __device__ __forceinline__ void assemble_items(const AssembleParams& P, long lon
     a[6] = (m & (1u << FZP)) ? -(F[FZP] + N[FZP]) / h[2] : 0.0;
     for (int c = 0; c < 7; ++c) {
       A[(size_t)c * NB + b] = a[c];
-      if (P.A32) P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)a[c];
+      if (P.A32) {
+        const float hi = (float)a[c];
+        P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = hi;
+        if (P.A32lo) P.A32lo[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)(a[c] - (double)hi);
+      }
     }
   }
 }

@@ -9,6 +9,7 @@
 #include <math.h>
 
 #include "adp_kernels.h"
+#include "ff.cuh"
 
 namespace adp {
 
@@ -44,7 +45,7 @@ __device__ __forceinline__ void rows_batched(int b, int nthr, int NB, Ld&& ld, E
 template <bool MIXED>
 struct RowsInFlight { static constexpr int R = 2; };
 template <>
-struct RowsInFlight<true> { static constexpr int R = 4; };
+struct RowsInFlight<true> { static constexpr int R = 2; };
 
 // ---------------------------------------------------------------------------
 // The persistent outer-iteration loop.
@@ -132,6 +133,24 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     e1 = tot[1];
   }
 
+  if constexpr (MIXED) {
+    // The FP64 flux and fission source are authoritative between launches;
+    // split the current ones into double-floats (own rows), then wait for
+    // the neighbours' rows before the first stencil.
+    const double* ph = P.phi[cur];
+    for (int b = tid0; b < NB; b += nthr) {
+      for (int g = 0; g < ng; ++g) {
+        const ff v = ff_from_double(ph[(size_t)g * NBH + b]);
+        P.xh[cur][(size_t)g * NBH + b] = v.hi;
+        P.xl[cur][(size_t)g * NBH + b] = v.lo;
+      }
+      const ff v = ff_from_double(P.fs[cur][b]);
+      P.fsh[cur][b] = v.hi;
+      P.fsl[cur][b] = v.lo;
+    }
+    if (!team_barrier(C, nblk, rank)) return;
+  }
+
   while (true) {
     ++p;
     ++ptot;
@@ -141,7 +160,9 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     const double* fsO = P.fs[old];
     double* fsN = P.fs[nw];
     const double invKe = 1.0 / Ke;
+    const ff invKe_ff = ff_from_double(invKe);
     double fer_acc = 0.0;
+    float fer_f = 0.f;
 
     for (int gi = 0; gi < ng; ++gi) {
       const int g = P.adj ? ng - 1 - gi : gi;
@@ -153,7 +174,42 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
 
       // ---- P0: source and initial residual (TSrc + r = b - A x) --------
       double tot1[1];
-      {
+      if constexpr (MIXED) {
+        // Defect of the current flux in double-float: one compensated dot
+        // product over the source and the seven matrix terms (A = A32 + lo).
+        const float* xOh = P.xh[old] + (size_t)g * NBH;
+        const float* xOl = P.xl[old] + (size_t)g * NBH;
+        const float* Alo = P.A32lo + (size_t)g * 7 * NB;
+        T accT = T(0);
+        rows_batched<RowsInFlight<MIXED>::R>(
+            tid0, nthr, NB,
+            [&](int b) -> T {
+              Dot2 d;
+              d.add(ff_mul(ff{P.wsrc_h[(size_t)g * NB + b], P.wsrc_l[(size_t)g * NB + b]},
+                           ff{P.fsh[old][b], P.fsl[old][b]}),
+                    invKe_ff);
+              for (int h = 0; h < ng; ++h) {
+                if (h == g) continue;
+                const bool solved = P.adj ? (h > g) : (h < g);
+                const int buf = solved ? nw : old;
+                const size_t ix = (size_t)h * NBH + b;
+                const size_t is = P.adj ? ((size_t)g * ng + h) * NB + b : ((size_t)h * ng + g) * NB + b;
+                d.add(ff{P.sigs_h[is], P.sigs_l[is]}, ff{P.xh[buf][ix], P.xl[buf][ix]});
+              }
+              const int off[7] = {-plane, -nxx, -1, 0, 1, nxx, plane};
+#pragma unroll
+              for (int c = 0; c < 7; ++c)
+                d.sub(ff{Ag[(size_t)c * NB + b], Alo[(size_t)c * NB + b]}, ff{xOh[b + off[c]], xOl[b + off[c]]});
+              return d.value().hi;
+            },
+            [&](int b, T rt) {
+              r[b] = rt;
+              rs[b] = rt;
+              accT = fmav(rt, rt, accT);
+            });
+        double acc[1] = {(double)accT};
+        if (!grid_reduce<1, 0u>(C, nblk, rank, RED(epoch), acc, tot1)) return;
+      } else {
         T accT = T(0);
         rows_batched<RowsInFlight<MIXED>::R>(
             tid0, nthr, NB,
@@ -229,17 +285,23 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 });
           } else {
             const double* xc = (it == 1) ? xO : xN;
-            struct RowA { T rb, pb, v, rsb; double xn; };
+            const float* xch = MIXED ? ((it == 1) ? P.xh[old] : P.xh[nw]) + (size_t)g * NBH : nullptr;
+            const float* xcl = MIXED ? ((it == 1) ? P.xl[old] : P.xl[nw]) + (size_t)g * NBH : nullptr;
+            float* xNh = MIXED ? P.xh[nw] + (size_t)g * NBH : nullptr;
+            float* xNl = MIXED ? P.xl[nw] + (size_t)g * NBH : nullptr;
+            struct RowA { T rb, pb, v, rsb; double xn; ff xf; };
             rows_batched<RowsInFlight<MIXED>::R>(
                 tid0, nthr, NB,
                 [&](int b) -> RowA {
                   auto rf = [&](int m) -> T { return fmav(-tom, t[m], s[m]); };
                   auto pf = [&](int m) -> T { return fmav(tb, fmav(-tom, vO[m], pO[m]), rf(m)); };
                   const T rb = rf(b);
-                  double xn;
-                  if (MIXED) {
+                  double xn = 0.0;
+                  ff xf{0.f, 0.f};
+                  if constexpr (MIXED) {
+                    // FP32 increment of the correction, added to the double-float flux
                     const T dx = fmav(tom, s[b], tap * pO[b]);
-                    xn = xc[b] + (double)dx;
+                    xf = ff_add_f(ff{xch[b], xcl[b]}, dx);
                   } else {
                     xn = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
                   }
@@ -251,11 +313,16 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                   v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
                   v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
                   v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
-                  return RowA{rb, pb, v, rs[b], xn};
+                  return RowA{rb, pb, v, rs[b], xn, xf};
                 },
                 [&](int b, const RowA& q) {
                   r[b] = q.rb;
-                  xN[b] = q.xn;
+                  if constexpr (MIXED) {
+                    xNh[b] = q.xf.hi;
+                    xNl[b] = q.xf.lo;
+                  } else {
+                    xN[b] = q.xn;
+                  }
                   pN[b] = q.pb;
                   vN[b] = q.v;
                   accT = fmav(q.rsb, q.v, accT);
@@ -325,18 +392,35 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           // reads only this thread's own rows of x.
           const T to = (T)omega;
           const double* xc = (it == 0) ? xO : xN;
+          if constexpr (MIXED) {
+            const float* xch = ((it == 0) ? P.xh[old] : P.xh[nw]) + (size_t)g * NBH;
+            const float* xcl = ((it == 0) ? P.xl[old] : P.xl[nw]) + (size_t)g * NBH;
+            const float* xOh = P.xh[old] + (size_t)g * NBH;
+            const float* xOl = P.xl[old] + (size_t)g * NBH;
+            float* xNh = P.xh[nw] + (size_t)g * NBH;
+            float* xNl = P.xl[nw] + (size_t)g * NBH;
+            struct RowCm { ff xn; float d; };
+            rows_batched<RowsInFlight<MIXED>::R>(
+                tid0, nthr, NB,
+                [&](int b) -> RowCm {
+                  // FP32 increment of the correction, added to the double-float flux
+                  const T dx = fmav(to, s[b], ta * pN[b]);
+                  const ff xn = ff_add_f(ff{xch[b], xcl[b]}, dx);
+                  return RowCm{xn, ff_diff(xn, ff{xOh[b], xOl[b]})};
+                },
+                [&](int b, const RowCm& q) {
+                  xNh[b] = q.xn.hi;
+                  xNl[b] = q.xn.lo;
+                  // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
+                  const float ax = fabsf(q.xn.hi), d = fabsf(q.d);
+                  if (ax > 1.e-10f && d > fer_f * ax) fer_f = fmaxf(fer_f, d / ax);
+                });
+          } else {
           struct RowC { double xn, xo; };
           rows_batched<RowsInFlight<MIXED>::R>(
               tid0, nthr, NB,
               [&](int b) -> RowC {
-                double xn;
-                if (MIXED) {
-                  // FP32 increment of the correction, accumulated into the FP64 flux
-                  const T dx = fmav(to, s[b], ta * pN[b]);
-                  xn = xc[b] + (double)dx;
-                } else {
-                  xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
-                }
+                const double xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
                 return RowC{xn, xO[b]};
               },
               [&](int b, const RowC& q) {
@@ -345,6 +429,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 const double ax = fabs(q.xn), d = fabs(q.xn - q.xo);
                 if (ax > 1.e-10 && d > fer_acc * ax) fer_acc = fmax(fer_acc, d / ax);
               });
+          }
         }
       }
     }
@@ -352,7 +437,37 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     // ---- fission source, norms and eigenvalue ------------------------------
     const bool extrap = (p % P.nac) == 0;
     double tot4[4];
-    {
+    if constexpr (MIXED) {
+      // fission source in double-float (Dot2 over the groups), Integrate
+      // as a compensated per-thread sum, norms of the change in FP32
+      float e2f = 0.f, serf = 0.f;
+      Dot2 dint;
+      struct RowFm { ff fs, fo, vd; };
+      rows_batched<RowsInFlight<MIXED>::R>(
+          tid0, nthr, NB,
+          [&](int b) -> RowFm {
+            Dot2 d;
+            for (int g = 0; g < ng; ++g)
+              d.add(ff{P.xh[nw][(size_t)g * NBH + b], P.xl[nw][(size_t)g * NBH + b]},
+                    ff{P.wfis_h[(size_t)g * NB + b], P.wfis_l[(size_t)g * NB + b]});
+            return RowFm{d.value(), ff{P.fsh[old][b], P.fsl[old][b]}, ff{P.vdel_h[b], P.vdel_l[b]}};
+          },
+          [&](int b, const RowFm& q) {
+            P.fsh[nw][b] = q.fs.hi;
+            P.fsl[nw][b] = q.fs.lo;
+            const float en = ff_diff(q.fs, q.fo);
+            e2f = fmaf(en, en, e2f);
+            if (!extrap) {
+              dint.add(q.vd, q.fs);
+              // RelE (mod_cmfd.f90:1143-1168)
+              const float af = fabsf(q.fs.hi), d = fabsf(en);
+              if (af > 1.e-10f && d > serf * af) serf = fmaxf(serf, d / af);
+            }
+          });
+      double acc[4] = {(double)e2f, ff_to_double(dint.value()), (double)serf, (double)fer_f};
+      if (!grid_reduce<4, 0xCu>(C, nblk, rank, RED(epoch), acc, tot4)) return;
+      ++epoch;
+    } else {
       double acc[4] = {0.0, 0.0, 0.0, fer_acc};
       struct RowF { double fs, fo, vd; };
       rows_batched<RowsInFlight<MIXED>::R>(
@@ -384,6 +499,23 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       const double domiR = e2 / e1;
       const double c = domiR / (1.0 - domiR);
       double acc[2] = {0.0, 0.0};
+      if constexpr (MIXED) {
+        const ff cf = ff_from_double(c);
+        float serf = 0.f;
+        Dot2 dint;
+        for (int b = tid0; b < NB; b += nthr) {
+          const ff fo{P.fsh[old][b], P.fsl[old][b]};
+          ff fs{P.fsh[nw][b], P.fsl[nw][b]};
+          fs = ff_add(fs, ff_mul(cf, ff_add(fs, ff{-fo.hi, -fo.lo})));
+          P.fsh[nw][b] = fs.hi;
+          P.fsl[nw][b] = fs.lo;
+          dint.add(ff{P.vdel_h[b], P.vdel_l[b]}, fs);
+          const float af = fabsf(fs.hi), d = fabsf(ff_diff(fs, fo));
+          if (af > 1.e-10f && d > serf * af) serf = fmaxf(serf, d / af);
+        }
+        acc[0] = ff_to_double(dint.value());
+        acc[1] = (double)serf;
+      } else
       for (int b = tid0; b < NB; b += nthr) {
         const double fo = fsO[b];
         double fs = fsN[b];
@@ -420,6 +552,14 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       }
     }
     if (bad || nodal || conv || maxr) {
+      if constexpr (MIXED) {
+        // back to the FP64 flux and fission source for the host and the nodal update
+        for (int b = tid0; b < NB; b += nthr) {
+          for (int g = 0; g < ng; ++g)
+            P.phi[cur][(size_t)g * NBH + b] = ff_to_double(ff{P.xh[cur][(size_t)g * NBH + b], P.xl[cur][(size_t)g * NBH + b]});
+          P.fs[cur][b] = ff_to_double(ff{P.fsh[cur][b], P.fsl[cur][b]});
+        }
+      }
       if (lead) {
         C->Ke = Ke;
         C->f = f;
