@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "../../include/adpres_gb300.h"
+#include "ff.cuh"
 
 namespace adp {
 
@@ -117,11 +118,17 @@ __device__ __forceinline__ void set_status(OuterCtl* C, int code) {
 // never leave the kernel spinning.  Called by lane 0 of one warp.
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
+// The arrival is an acquire-release add (it publishes this block's writes,
+// which the block's other threads ordered before it with __syncthreads,
+// and the last arrival acquires everyone else's) and the wait an acquire
+// load; the add's read-modify-write chain carries every arriving block's
+// release to the acquire that sees the flip, so no separate fence is
+// needed.  A block that gave up never arrives again, so every later wait
+// of the team runs out of time too and the kernel ends.
 __device__ __forceinline__ int team_arrive_wait(OuterCtl* C, unsigned nblocks, unsigned rank) {
   int ok = 1;
   const unsigned add = (rank == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
-  __threadfence();
-  const unsigned old = atomicAdd(&C->bar_count, add);
+  const unsigned old = atom_add_acqrel_gpu(&C->bar_count, add);
   if (!(((old + add) ^ old) & 0x80000000u)) {
     unsigned long long t0 = 0;
     unsigned spins = 0;
@@ -137,8 +144,6 @@ __device__ __forceinline__ int team_arrive_wait(OuterCtl* C, unsigned nblocks, u
       }
     }
   }
-  __threadfence();
-  if (ok && *((volatile int*)&C->status) == ADP_ERR_TIMEOUT) ok = 0;
   return ok;
 }
 
@@ -305,6 +310,90 @@ __device__ __forceinline__ bool grid_reduce(OuterCtl* C, unsigned nblocks, unsig
       }
     }
     if (lane == 0) s_ok = ok;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) tot[q] = st[q];
+  return s_ok != 0;
+}
+
+// The same fused block reduction, team barrier and totals in double-float
+// arithmetic (FP32 pairs, error-free sums) for the mixed path: the values,
+// the warp and block sums and the partials in memory are double-floats, so
+// no FP64 instruction runs except the final conversion of each total.
+// The partial slots of `slot` hold one (hi, lo) pair per block.  MAXMASK
+// quantities are maxima of non-negative values carried in hi.
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ void warp_all_ff(ff (&x)[NQ]) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const ff y{__shfl_xor_sync(0xffffffffu, x[q].hi, o), __shfl_xor_sync(0xffffffffu, x[q].lo, o)};
+      x[q] = ((MAXMASK >> q) & 1u) ? (y.hi > x[q].hi ? y : x[q]) : ff_add(x[q], y);
+    }
+  }
+}
+
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ bool grid_reduce_ff(OuterCtl* C, unsigned nblocks, unsigned rank, double* slot_d,
+                                               const ff (&v)[NQ], double (&tot)[NQ]) {
+  __shared__ ff sw[NQ][32];
+  __shared__ double st[NQ];
+  __shared__ int s_ok;
+  float2* slot = reinterpret_cast<float2*>(slot_d);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  ff x[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) x[q] = v[q];
+  warp_all_ff<NQ, MAXMASK>(x);
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) sw[q][w] = x[q];
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) x[q] = lane < nw ? sw[q][lane] : ff{0.f, 0.f};
+    warp_all_ff<NQ, MAXMASK>(x);
+    int ok = 1;
+    if (nblocks > 1) {
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) slot[q * kMaxBlocks + rank] = make_float2(x[q].hi, x[q].lo);
+        ok = team_arrive_wait(C, nblocks, rank);
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      __syncwarp();
+      if (ok) {
+        const int nblk = (int)nblocks;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) x[q] = ff{0.f, 0.f};
+        for (int base = 0; base < nblk; base += 256) {
+          float2 y[NQ][8];
+#pragma unroll
+          for (int q = 0; q < NQ; ++q)
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const int i = base + lane + 32 * k;
+              y[q][k] = (i < nblk) ? __ldcg(slot + q * kMaxBlocks + i) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+              const ff yy{y[q][k].x, y[q][k].y};
+              x[q] = ((MAXMASK >> q) & 1u) ? (yy.hi > x[q].hi ? yy : x[q]) : ff_add(x[q], yy);
+            }
+        }
+        warp_all_ff<NQ, MAXMASK>(x);
+      }
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) st[q] = ff_to_double(x[q]);
+      s_ok = ok;
+    }
   }
   __syncthreads();
 #pragma unroll

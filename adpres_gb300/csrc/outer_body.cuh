@@ -41,6 +41,15 @@ __device__ __forceinline__ void rows_batched(int b, int nthr, int NB, Ld&& ld, E
   for (; b < NB; b += nthr) ex(b, ld(b));
 }
 
+// Team reduction of per-thread partials: in double-float for the mixed
+// path (no FP64 instruction per warp), in FP64 for the FP64 path.
+template <bool MIXED, int NQ, unsigned MASK>
+__device__ __forceinline__ bool team_reduce(OuterCtl* C, unsigned nblk, unsigned rank, double* slot,
+                                            const double (&vd)[NQ], const ff (&vf)[NQ], double (&tot)[NQ]) {
+  if constexpr (MIXED) return grid_reduce_ff<NQ, MASK>(C, nblk, rank, slot, vf, tot);
+  else return grid_reduce<NQ, MASK>(C, nblk, rank, slot, vd, tot);
+}
+
 // Rows in flight per thread in the row loops.
 template <bool MIXED>
 struct RowsInFlight { static constexpr int R = 2; };
@@ -103,6 +112,18 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
   __syncthreads();
   if (s_stop) return;
 
+  // Scalars shared by the whole block (alpha, beta, omega, k, ...) are formed
+  // by one thread and broadcast: on GB300 an FP64 instruction of a warp
+  // occupies the FP64 pipe for tens of cycles, so forming them in every
+  // warp would cost several microseconds per BiCGSTAB step.
+  // Slots: step start s_d[0..1], s_f[0..2], s_ib; after phase A s_d[0],
+  // s_f[0], s_ia; after phase B s_d[2..3], s_f[3], s_io (its readers may
+  // still be reading when the next step's start writes, hence its own
+  // slots); end of outer s_d[0..2], s_f[0..1].  Every other reuse of a slot
+  // is separated from its last read by a block-wide barrier.
+  __shared__ double s_d[4];
+  __shared__ float s_f[4];
+  __shared__ int s_ib, s_ia, s_io;
   double Ke = vld(&C->Ke), f = vld(&C->f), e1 = vld(&C->e1);
   const double ndmax = vld(&C->ndmax);
   int p = vld(&C->p), ptot = vld(&C->p_total), cur = vld(&C->cur);
@@ -159,8 +180,16 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     double* phiN = P.phi[nw];
     const double* fsO = P.fs[old];
     double* fsN = P.fs[nw];
-    const double invKe = 1.0 / Ke;
-    const ff invKe_ff = ff_from_double(invKe);
+    if (threadIdx.x == 0) {
+      const double ik = 1.0 / Ke;
+      const ff ikf = ff_from_double(ik);
+      s_d[0] = ik;
+      s_f[0] = ikf.hi;
+      s_f[1] = ikf.lo;
+    }
+    __syncthreads();
+    const double invKe = s_d[0];
+    const ff invKe_ff{s_f[0], s_f[1]};
     double fer_acc = 0.0;
     float fer_f = 0.f;
 
@@ -207,8 +236,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
               rs[b] = rt;
               accT = fmav(rt, rt, accT);
             });
-        double acc[1] = {(double)accT};
-        if (!grid_reduce<1, 0u>(C, nblk, rank, RED(epoch), acc, tot1)) return;
+        ff acc[1] = {ff{(float)accT, 0.f}};
+        if (!grid_reduce_ff<1, 0u>(C, nblk, rank, RED(epoch), acc, tot1)) return;
       } else {
         T accT = T(0);
         rows_batched<RowsInFlight<MIXED>::R>(
@@ -248,18 +277,30 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
 
       for (int it = 0; it < P.nin; ++it) {
         const bool last = (it == P.nin - 1);
-        const double rho_prev = rho;
-        rho = rsr;
-        if (rho == 0.0 || omega == 0.0) {
+        if (threadIdx.x == 0) {
+          const double rho_prev = rho, rho_n = rsr;
+          const int brk = (rho_n == 0.0 || omega == 0.0);
+          const double bt = brk ? 0.0 : (rho_n / rho_prev) * (alpha / omega);
+          s_d[0] = rho_n;
+          s_d[1] = bt;
+          s_f[0] = (float)bt;
+          s_f[1] = (float)omega;
+          s_f[2] = (float)alpha;
+          s_ib = brk;
+        }
+        __syncthreads();
+        rho = s_d[0];
+        const double beta = s_d[1];
+        if (s_ib) {
           if (lead) set_status(C, ADP_ERR_BREAKDOWN);
           return;
         }
-        const double beta = (rho / rho_prev) * (alpha / omega);
         T* pN = pv[it & 1];
         const T* pO = pv[(it & 1) ^ 1];
         T* vN = vv[it & 1];
         const T* vO = vv[(it & 1) ^ 1];
-        const T tb = (T)beta, tom = (T)omega, tap = (T)alpha;
+        const T tb = MIXED ? (T)s_f[0] : (T)beta, tom = MIXED ? (T)s_f[1] : (T)omega,
+                tap = MIXED ? (T)s_f[2] : (T)alpha;
         // ---- phase A: (previous step's x and r), p and v = A p -----------
         {
           T accT = T(0);
@@ -328,16 +369,25 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                   accT = fmav(q.rsb, q.v, accT);
                 });
           }
-          double acc[1] = {(double)accT};
-          if (!grid_reduce<1, 0u>(C, nblk, rank, RED(epoch), acc, tot1)) return;
+          const double accd[1] = {(double)accT};
+          const ff accf[1] = {ff{(float)accT, 0.f}};
+          if (!team_reduce<MIXED, 1, 0u>(C, nblk, rank, RED(epoch), accd, accf, tot1)) return;
         }
         ++epoch;
-        if (tot1[0] == 0.0) {
+        if (threadIdx.x == 0) {
+          const int brk = tot1[0] == 0.0;
+          const double al = brk ? 0.0 : rho / tot1[0];
+          s_d[0] = al;
+          s_f[0] = (float)al;
+          s_ia = brk;
+        }
+        __syncthreads();
+        if (s_ia) {
           if (lead) set_status(C, ADP_ERR_BREAKDOWN);
           return;
         }
-        alpha = rho / tot1[0];
-        const T ta = (T)alpha;
+        alpha = s_d[0];
+        const T ta = MIXED ? (T)s_f[0] : (T)alpha;
         // ---- phase B: s and t = A s; (t,t), (t,s) and, for the next step,
         //      (rs,s), (rs,t): (rs, s - omega t) = (rs,s) - omega (rs,t) ------
         double tot4[4];
@@ -369,28 +419,41 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 }
               });
           if (last) {
-            double acc[2] = {(double)acc0, (double)acc1}, tot2[2];
-            if (!grid_reduce<2, 0u>(C, nblk, rank, RED(epoch), acc, tot2)) return;
+            const double accd[2] = {(double)acc0, (double)acc1};
+            const ff accf[2] = {ff{(float)acc0, 0.f}, ff{(float)acc1, 0.f}};
+            double tot2[2];
+            if (!team_reduce<MIXED, 2, 0u>(C, nblk, rank, RED(epoch), accd, accf, tot2)) return;
             tot4[0] = tot2[0];
             tot4[1] = tot2[1];
           } else {
-            double acc[4] = {(double)acc0, (double)acc1, (double)acc2, (double)acc3};
-            if (!grid_reduce<4, 0u>(C, nblk, rank, RED(epoch), acc, tot4)) return;
+            const double accd[4] = {(double)acc0, (double)acc1, (double)acc2, (double)acc3};
+            const ff accf[4] = {ff{(float)acc0, 0.f}, ff{(float)acc1, 0.f}, ff{(float)acc2, 0.f},
+                                ff{(float)acc3, 0.f}};
+            if (!team_reduce<MIXED, 4, 0u>(C, nblk, rank, RED(epoch), accd, accf, tot4)) return;
           }
         }
         ++epoch;
-        if (tot4[0] == 0.0) {
+        if (threadIdx.x == 0) {
+          const int brk = tot4[0] == 0.0;
+          const double om = brk ? 0.0 : tot4[1] / tot4[0];
+          s_d[2] = om;
+          s_d[3] = last ? 0.0 : tot4[2] - om * tot4[3];
+          s_f[3] = (float)om;
+          s_io = brk;
+        }
+        __syncthreads();
+        if (s_io) {
           if (lead) set_status(C, ADP_ERR_BREAKDOWN);
           return;
         }
-        omega = tot4[1] / tot4[0];
+        omega = s_d[2];
         if (!last) {
-          rsr = tot4[2] - omega * tot4[3];
+          rsr = s_d[3];
         } else {
           // ---- phase C of the last step: x, and RelEg's running maximum.
           // No barrier follows: the next group's P0 (or the fission source)
           // reads only this thread's own rows of x.
-          const T to = (T)omega;
+          const T to = MIXED ? (T)s_f[3] : (T)omega;
           const double* xc = (it == 0) ? xO : xN;
           if constexpr (MIXED) {
             const float* xch = ((it == 0) ? P.xh[old] : P.xh[nw]) + (size_t)g * NBH;
@@ -464,8 +527,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
               if (af > 1.e-10f && d > serf * af) serf = fmaxf(serf, d / af);
             }
           });
-      double acc[4] = {(double)e2f, ff_to_double(dint.value()), (double)serf, (double)fer_f};
-      if (!grid_reduce<4, 0xCu>(C, nblk, rank, RED(epoch), acc, tot4)) return;
+      const ff acc[4] = {ff{e2f, 0.f}, dint.value(), ff{serf, 0.f}, ff{fer_f, 0.f}};
+      if (!grid_reduce_ff<4, 0xCu>(C, nblk, rank, RED(epoch), acc, tot4)) return;
       ++epoch;
     } else {
       double acc[4] = {0.0, 0.0, 0.0, fer_acc};
@@ -491,16 +554,29 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       if (!grid_reduce<4, 0xCu>(C, nblk, rank, RED(epoch), acc, tot4)) return;
       ++epoch;
     }
-    const double e2 = sqrt(tot4[0]);
+    if (threadIdx.x == 0) {
+      const double e2n = sqrt(tot4[0]);
+      s_d[0] = e2n;
+      if (extrap) {
+        // fiss_extrp (mod_cmfd.f90:308-335)
+        const double domiR = e2n / e1;
+        const double cn = domiR / (1.0 - domiR);
+        const ff cnf = ff_from_double(cn);
+        s_d[1] = cn;
+        s_f[0] = cnf.hi;
+        s_f[1] = cnf.lo;
+      }
+    }
+    __syncthreads();
+    const double e2 = s_d[0];
     double fsum = tot4[1], ser = tot4[2];
     const double fer = tot4[3];
     if (extrap) {
-      // fiss_extrp (mod_cmfd.f90:308-335)
-      const double domiR = e2 / e1;
-      const double c = domiR / (1.0 - domiR);
+      const double c = s_d[1];
       double acc[2] = {0.0, 0.0};
+      ff accf[2] = {ff{0.f, 0.f}, ff{0.f, 0.f}};
       if constexpr (MIXED) {
-        const ff cf = ff_from_double(c);
+        const ff cf{s_f[0], s_f[1]};
         float serf = 0.f;
         Dot2 dint;
         for (int b = tid0; b < NB; b += nthr) {
@@ -513,8 +589,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           const float af = fabsf(fs.hi), d = fabsf(ff_diff(fs, fo));
           if (af > 1.e-10f && d > serf * af) serf = fmaxf(serf, d / af);
         }
-        acc[0] = ff_to_double(dint.value());
-        acc[1] = (double)serf;
+        accf[0] = dint.value();
+        accf[1] = ff{serf, 0.f};
       } else
       for (int b = tid0; b < NB; b += nthr) {
         const double fo = fsO[b];
@@ -526,14 +602,15 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
         if (af > 1.e-10 && d > acc[1] * af) acc[1] = fmax(acc[1], d / af);
       }
       double tot[2];
-      if (!grid_reduce<2, 0x2u>(C, nblk, rank, RED(epoch), acc, tot)) return;
+      if (!team_reduce<MIXED, 2, 0x2u>(C, nblk, rank, RED(epoch), acc, accf, tot)) return;
       ++epoch;
       fsum = tot[0];
       ser = tot[1];
     }
     e1 = e2;
-    const double Keo = Ke;
-    Ke = Keo * fsum / f;
+    if (threadIdx.x == 0) s_d[2] = Ke * fsum / f;
+    __syncthreads();
+    Ke = s_d[2];
     f = fsum;
     cur = nw;
 

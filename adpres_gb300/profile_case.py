@@ -2,8 +2,12 @@
 solver in isolation (for example under ncu):
 
     python -m adpres_gb300.profile_case --config core_4g --planes 40 --precision mixed --solves 1
+    python -m adpres_gb300.profile_case --config batch --members 16 --precision mixed
+    python -m adpres_gb300.profile_case --config full_core_3d --adjoint
 
-Prints k, the outer count and the device time of each solve.
+Prints k, the outer count and the device time of each solve.  The batch
+case solves the first `members` cores of the batched workload; --adjoint
+adds the discrete adjoint and dk/dSigma after the forward solve.
 """
 from __future__ import annotations
 
@@ -15,12 +19,29 @@ from .core import Core
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", default="core_4g", choices=sorted(synth.CONFIGS))
+    ap.add_argument("--config", default="core_4g", choices=sorted(synth.CONFIGS) + ["batch"])
+    ap.add_argument("--members", type=int, default=16, help="cores of the batch case")
+    ap.add_argument("--adjoint", action="store_true", help="also run adp_adjoint_sens")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--planes", type=int, default=80, help="axial planes of core_4g (20, 40 or 80)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--solves", type=int, default=1)
     a = ap.parse_args()
+    if a.config == "batch":
+        import json
+        import os
+        from .batch import Batch
+        root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        with open(os.path.join(root, "tests", "golden", "batch_members.json")) as f:
+            acc = json.load(f)
+        decks = [deck.parse(synth.batch_member(acc["seed"], i)) for i in acc["accepted"][:a.members]]
+        b = Batch(decks, precision=a.precision)
+        for _ in range(a.solves):
+            res, ms = b.solve()
+            print(f"batch of {len(decks)} ({sum(len(d.ix) for d in decks)} nodes) {a.precision}: "
+                  f"device_ms={ms:.2f} outers={[r['outers'] for r in res]}", flush=True)
+        b.close()
+        return
     if a.config == "core_4g":
         text = synth.core_4g(a.seed, planes=a.planes)
     else:
@@ -32,6 +53,9 @@ def main():
             rep = c.outer(trace=False)
             print(f"{a.config} nodes={dk.nnod} groups={dk.ng} {a.precision}: k={rep.keff:.8f} "
                   f"outers={rep.outers} device_ms={rep.device_ms:.2f}", flush=True)
+            if a.adjoint:
+                _, _, arep = c.adjoint_sens()
+                print(f"  adjoint: k={arep.keff:.8f} outers={arep.outers} device_ms={arep.device_ms:.2f}", flush=True)
 
 
 if __name__ == "__main__":
