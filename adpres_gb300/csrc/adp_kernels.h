@@ -17,6 +17,7 @@ constexpr double kF1em5 = (double)1.e-5f;   // mod_data.f90:78-79
 struct OuterParams {
   BoxGeom G;
   int ng, nin, nac, nupd, nout, adj, do_nodal, mixed;
+  int smem_rows;              // > 0: rows per block of the matrix copy in shared memory
   double serc, ferc;
   long long NBH;              // group stride of halo'd arrays
   const double* A;            // [ng][7][NB] FP64 CMFD matrix
@@ -147,6 +148,9 @@ struct BatchTask {
 cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st);
 cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st);
 cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st);
+// Rows per block of the shared-memory matrix copy for this launch shape
+// (0 when it does not fit).
+int outer_smem_rows(int NB, int blocks, int threads, int mixed);
 int outer_max_blocks_per_sm(int threads, int mixed);
 cudaError_t launch_power(const BoxGeom& G, int ng, long long NBH, const double* phi, const double* sigf,
                          double* pbox, double* red, OuterCtl* ctl, cudaStream_t st);

@@ -809,6 +809,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   NodalParams NP = nodal_params(h, adj ? 0 : 1);
   int blocks, threads;
   launch_shape(h, blocks, threads);
+  P.smem_rows = outer_smem_rows(h->NB, blocks, threads, P.mixed);
   h->tm.grid_blocks = blocks;
   h->tm.block_threads = threads;
   adp_status result = ADP_OK;
@@ -1059,6 +1060,7 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
   CK(cudaMemcpyAsync(h->d_ctla, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
   int blocks, threads;
   launch_shape(h, blocks, threads);
+  P.smem_rows = outer_smem_rows(h->NB, blocks, threads, P.mixed);
   adp_status result = ADP_OK;
   for (int guard = 0; guard < 4 * h->o.nout + 8; ++guard) {
     CK(cudaMemsetAsync(&h->d_ctla->bar_count, 0, sizeof(unsigned), h->st));

@@ -63,23 +63,47 @@ cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <bool MIXED>
+template <bool MIXED, bool SMEMA>
 __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
-  outer_body<MIXED>(P, blockIdx.x, gridDim.x);
+  outer_body<MIXED, SMEMA>(P, blockIdx.x, gridDim.x);
 }
 
 int outer_max_blocks_per_sm(int threads, int mixed) {
   int nb = 0;
-  if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_outer<true>, threads, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_outer<false>, threads, 0);
+  if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_outer<true, false>, threads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_outer<false, false>, threads, 0);
   return nb;
 }
 
-cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st) {
+// Shared memory of the matrix copy: at most this much (the static shared
+// memory of the kernel is a few KB; 227 KB per block is the limit).
+constexpr size_t kSmemMatrixMax = 200 * 1024;
+
+int outer_smem_rows(int NB, int blocks, int threads, int mixed) {
+  const long long nthr = (long long)blocks * threads;
+  const long long rpt = (NB + nthr - 1) / nthr;   // rows per thread
+  const long long rows = rpt * threads;
+  const size_t bytes = (size_t)rows * 7 * (mixed ? sizeof(float) : sizeof(double));
+  return bytes <= kSmemMatrixMax ? (int)rows : 0;
+}
+
+template <bool MIXED, bool SMEMA>
+static cudaError_t launch_outer_t(const OuterParams& P, int blocks, int threads, cudaStream_t st) {
   void* args[] = {(void*)&P};
-  if (P.mixed)
-    return cudaLaunchCooperativeKernel((const void*)k_outer<true>, dim3(blocks), dim3(threads), args, 0, st);
-  return cudaLaunchCooperativeKernel((const void*)k_outer<false>, dim3(blocks), dim3(threads), args, 0, st);
+  size_t smem = 0;
+  if (SMEMA) {
+    smem = (size_t)P.smem_rows * 7 * (MIXED ? sizeof(float) : sizeof(double));
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_outer<MIXED, SMEMA>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaLaunchCooperativeKernel((const void*)k_outer<MIXED, SMEMA>, dim3(blocks), dim3(threads), args, smem, st);
+}
+
+cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st) {
+  if (P.smem_rows > 0)
+    return P.mixed ? launch_outer_t<true, true>(P, blocks, threads, st) : launch_outer_t<false, true>(P, blocks, threads, st);
+  return P.mixed ? launch_outer_t<true, false>(P, blocks, threads, st) : launch_outer_t<false, false>(P, blocks, threads, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -50,11 +50,17 @@ __device__ __forceinline__ bool team_reduce(OuterCtl* C, unsigned nblk, unsigned
   else return grid_reduce<NQ, MASK>(C, nblk, rank, slot, vd, tot);
 }
 
-// Rows in flight per thread in the row loops.
+// Rows in flight per thread in the row loops (compile-time tunable).
+#ifndef ADP_ROWS_FP64
+#define ADP_ROWS_FP64 2
+#endif
+#ifndef ADP_ROWS_MIXED
+#define ADP_ROWS_MIXED 2
+#endif
 template <bool MIXED>
-struct RowsInFlight { static constexpr int R = 2; };
+struct RowsInFlight { static constexpr int R = ADP_ROWS_FP64; };
 template <>
-struct RowsInFlight<true> { static constexpr int R = 2; };
+struct RowsInFlight<true> { static constexpr int R = ADP_ROWS_MIXED; };
 
 // ---------------------------------------------------------------------------
 // The persistent outer-iteration loop.
@@ -95,9 +101,17 @@ struct KV { using T = double; };
 template <>
 struct KV<true> { using T = float; };
 
-template <bool MIXED>
+// SMEMA: the block keeps its own rows' matrix coefficients of the group
+// being solved in dynamic shared memory (P.smem_rows rows per coefficient,
+// row k * nthreads + tid of the block at index k * blockDim.x + tid): P0
+// reads them from memory anyway and stores them, the 2 nin Krylov phases
+// that follow read them from there instead of L2 or HBM.
+template <bool MIXED, bool SMEMA = false>
 __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, unsigned nteam) {
   using T = typename KV<MIXED>::T;
+  extern __shared__ __align__(16) unsigned char adp_dyn_smem[];
+  T* const sA = reinterpret_cast<T*>(adp_dyn_smem);
+  const int SR = P.smem_rows;
   OuterCtl* C = P.ctl;
   const BoxGeom& G = P.G;
   const int NB = G.NB, nxx = G.nxx, plane = G.plane, ng = P.ng;
@@ -105,6 +119,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
   const int tid0 = rank * blockDim.x + threadIdx.x;
   const unsigned nblk = nteam;
   const long long NBH = P.NBH;
+  // shared-memory index of one of this thread's rows
+  auto jrow = [&](int b) -> int { return ((b - tid0) / nthr) * (int)blockDim.x + (int)threadIdx.x; };
 
   __shared__ int s_stop;
   if (threadIdx.x == 0)
@@ -226,9 +242,13 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 d.add(ff{P.sigs_h[is], P.sigs_l[is]}, ff{P.xh[buf][ix], P.xl[buf][ix]});
               }
               const int off[7] = {-plane, -nxx, -1, 0, 1, nxx, plane};
+              const int j = SMEMA ? jrow(b) : 0;
 #pragma unroll
-              for (int c = 0; c < 7; ++c)
-                d.sub(ff{Ag[(size_t)c * NB + b], Alo[(size_t)c * NB + b]}, ff{xOh[b + off[c]], xOl[b + off[c]]});
+              for (int c = 0; c < 7; ++c) {
+                const float ah = Ag[(size_t)c * NB + b];
+                if constexpr (SMEMA) sA[(size_t)c * SR + j] = ah;
+                d.sub(ff{ah, Alo[(size_t)c * NB + b]}, ff{xOh[b + off[c]], xOl[b + off[c]]});
+              }
               return d.value().hi;
             },
             [&](int b, T rt) {
@@ -253,13 +273,21 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 s0 = fma(sg, ph, s0);
               }
               const double bs = wsrc[b] * fsO[b] * invKe + s0;
-              double ax = A64[b] * xO[b - plane];
-              ax = fma(A64[(size_t)NB + b], xO[b - nxx], ax);
-              ax = fma(A64[(size_t)2 * NB + b], xO[b - 1], ax);
-              ax = fma(A64[(size_t)3 * NB + b], xO[b], ax);
-              ax = fma(A64[(size_t)4 * NB + b], xO[b + 1], ax);
-              ax = fma(A64[(size_t)5 * NB + b], xO[b + nxx], ax);
-              ax = fma(A64[(size_t)6 * NB + b], xO[b + plane], ax);
+              double a64[7];
+#pragma unroll
+              for (int c = 0; c < 7; ++c) a64[c] = A64[(size_t)c * NB + b];
+              if constexpr (SMEMA) {
+                const int j = jrow(b);
+#pragma unroll
+                for (int c = 0; c < 7; ++c) sA[(size_t)c * SR + j] = (T)a64[c];
+              }
+              double ax = a64[0] * xO[b - plane];
+              ax = fma(a64[1], xO[b - nxx], ax);
+              ax = fma(a64[2], xO[b - 1], ax);
+              ax = fma(a64[3], xO[b], ax);
+              ax = fma(a64[4], xO[b + 1], ax);
+              ax = fma(a64[5], xO[b + nxx], ax);
+              ax = fma(a64[6], xO[b + plane], ax);
               const double rr = bs - ax;
               return (T)rr;
             },
@@ -310,13 +338,15 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 tid0, nthr, NB,
                 [&](int b) -> RowA0 {
                   const T pb = r[b];
-                  T v = Ag[b] * r[b - plane];
-                  v = fmav(Ag[(size_t)NB + b], r[b - nxx], v);
-                  v = fmav(Ag[(size_t)2 * NB + b], r[b - 1], v);
-                  v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-                  v = fmav(Ag[(size_t)4 * NB + b], r[b + 1], v);
-                  v = fmav(Ag[(size_t)5 * NB + b], r[b + nxx], v);
-                  v = fmav(Ag[(size_t)6 * NB + b], r[b + plane], v);
+                  const int j = SMEMA ? jrow(b) : 0;
+                  auto AC = [&](int c) -> T { return SMEMA ? sA[(size_t)c * SR + j] : Ag[(size_t)c * NB + b]; };
+                  T v = AC(0) * r[b - plane];
+                  v = fmav(AC(1), r[b - nxx], v);
+                  v = fmav(AC(2), r[b - 1], v);
+                  v = fmav(AC(3), pb, v);
+                  v = fmav(AC(4), r[b + 1], v);
+                  v = fmav(AC(5), r[b + nxx], v);
+                  v = fmav(AC(6), r[b + plane], v);
                   return RowA0{pb, v, rs[b]};
                 },
                 [&](int b, const RowA0& q) {
@@ -347,13 +377,15 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                     xn = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
                   }
                   const T pb = fmav(tb, fmav(-tom, vO[b], pO[b]), rb);
-                  T v = Ag[b] * pf(b - plane);
-                  v = fmav(Ag[(size_t)NB + b], pf(b - nxx), v);
-                  v = fmav(Ag[(size_t)2 * NB + b], pf(b - 1), v);
-                  v = fmav(Ag[(size_t)3 * NB + b], pb, v);
-                  v = fmav(Ag[(size_t)4 * NB + b], pf(b + 1), v);
-                  v = fmav(Ag[(size_t)5 * NB + b], pf(b + nxx), v);
-                  v = fmav(Ag[(size_t)6 * NB + b], pf(b + plane), v);
+                  const int j = SMEMA ? jrow(b) : 0;
+                  auto AC = [&](int c) -> T { return SMEMA ? sA[(size_t)c * SR + j] : Ag[(size_t)c * NB + b]; };
+                  T v = AC(0) * pf(b - plane);
+                  v = fmav(AC(1), pf(b - nxx), v);
+                  v = fmav(AC(2), pf(b - 1), v);
+                  v = fmav(AC(3), pb, v);
+                  v = fmav(AC(4), pf(b + 1), v);
+                  v = fmav(AC(5), pf(b + nxx), v);
+                  v = fmav(AC(6), pf(b + plane), v);
                   return RowA{rb, pb, v, rs[b], xn, xf};
                 },
                 [&](int b, const RowA& q) {
@@ -399,13 +431,15 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
               [&](int b) -> RowB {
                 auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
                 const T sb = sf(b);
-                T tt = Ag[b] * sf(b - plane);
-                tt = fmav(Ag[(size_t)NB + b], sf(b - nxx), tt);
-                tt = fmav(Ag[(size_t)2 * NB + b], sf(b - 1), tt);
-                tt = fmav(Ag[(size_t)3 * NB + b], sb, tt);
-                tt = fmav(Ag[(size_t)4 * NB + b], sf(b + 1), tt);
-                tt = fmav(Ag[(size_t)5 * NB + b], sf(b + nxx), tt);
-                tt = fmav(Ag[(size_t)6 * NB + b], sf(b + plane), tt);
+                const int j = SMEMA ? jrow(b) : 0;
+                auto AC = [&](int c) -> T { return SMEMA ? sA[(size_t)c * SR + j] : Ag[(size_t)c * NB + b]; };
+                T tt = AC(0) * sf(b - plane);
+                tt = fmav(AC(1), sf(b - nxx), tt);
+                tt = fmav(AC(2), sf(b - 1), tt);
+                tt = fmav(AC(3), sb, tt);
+                tt = fmav(AC(4), sf(b + 1), tt);
+                tt = fmav(AC(5), sf(b + nxx), tt);
+                tt = fmav(AC(6), sf(b + plane), tt);
                 return RowB{sb, tt, last ? T(0) : rs[b]};
               },
               [&](int b, const RowB& q) {
