@@ -203,6 +203,38 @@ class Core:
     def set_launch(self, blocks=0, threads=0):
         self._check(self.L.adp_set_launch(self.h, int(blocks), int(threads)))
 
+    # -- output edits (mod_io.f90:3267-3644) ----------------------------------
+    def _divs(self, name, div):
+        if div is None:
+            div = getattr(self, "deck", None).extra[name]
+        return np.ascontiguousarray(div, dtype=np.int32)
+
+    def asmpow(self, xdiv=None, ydiv=None):
+        """AsmPow: (fasm (nx, ny), (imax, jmax)); divisions default to the deck's."""
+        xd, yd = self._divs("xdiv", xdiv), self._divs("ydiv", ydiv)
+        out = np.zeros(len(xd) * len(yd))
+        im, jm = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.adp_edit_asmpow(self.h, len(xd), len(yd), iptr(xd), iptr(yd), dptr(out), ctypes.byref(im),
+                                           ctypes.byref(jm)))
+        return out.reshape((len(xd), len(yd)), order="F"), (im.value, jm.value)
+
+    def axipow(self, zdiv=None):
+        """AxiPow: (faxi (nz,), kmax)."""
+        zd = self._divs("zdiv", zdiv)
+        out = np.zeros(len(zd))
+        km = ctypes.c_int()
+        self._check(self.L.adp_edit_axipow(self.h, len(zd), iptr(zd), dptr(out), ctypes.byref(km)))
+        return out, km.value
+
+    def asmflux(self, xdiv=None, ydiv=None, norm=1.0):
+        """AsmFlux: (fasm (nx, ny, ng), negative)."""
+        xd, yd = self._divs("xdiv", xdiv), self._divs("ydiv", ydiv)
+        out = np.zeros(len(xd) * len(yd) * self.ng)
+        neg = ctypes.c_int()
+        self._check(self.L.adp_edit_asmflux(self.h, len(xd), len(yd), iptr(xd), iptr(yd), float(norm), dptr(out),
+                                            ctypes.byref(neg)))
+        return out.reshape((len(xd), len(yd), self.ng), order="F"), bool(neg.value)
+
     # -- calculation modes (mod_control.f90:11-86) ---------------------------
     def forward(self):
         rep = self.outer(adjoint=False, popt=1)

@@ -76,6 +76,9 @@ struct adp_handle {
   long long* d_ndkey = nullptr;
   int* d_ndloc = nullptr;
   double* d_pbox = nullptr;
+  // output edits (adp_edit_*), allocated on first use
+  char* edit_base = nullptr;
+  size_t edit_size = 0;
   // discrete adjoint (adp_adjoint_sens), allocated on its first call
   char* adj_base = nullptr;
   double* d_AT = nullptr;

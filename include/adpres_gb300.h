@@ -226,6 +226,27 @@ adp_status adp_power_noalloc(int nnod, int ng, const double* f0, const double* s
  * (keff is its eigenvalue).  The forward state is left unchanged. */
 adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* report);
 
+/* -- output edits of control::forward (mod_control.f90:33-44) -------------- */
+
+/* AsmPow (mod_io.f90:3267-3403): PowDis of the current flux, axially
+ * averaged per node column (weights zdel), area-weighted per assembly of
+ * xdiv(nx) x ydiv(ny) columns, normalised so that the assemblies with
+ * power average 1.  fasm (nx, ny), i fastest; imax/jmax: the first maximum
+ * (1-based).  The node power never leaves the device. */
+adp_status adp_edit_asmpow(adp_handle* h, int nx, int ny, const int* xdiv, const int* ydiv, double* fasm, int* imax,
+                           int* jmax);
+/* AxiPow (mod_io.f90:3406-3498): PowDis summed over each axial region of
+ * zdiv(nz) planes and divided by the region's volume, normalised so that
+ * the regions with power average 1.  faxi (nz); kmax: the first maximum. */
+adp_status adp_edit_axipow(adp_handle* h, int nz, const int* zdiv, double* faxi, int* kmax);
+/* AsmFlux (mod_io.f90:3501-3644): per group, the flux axially averaged per
+ * column (weights: node volumes) and area-weighted per assembly; when
+ * norm > 0 scaled by norm / (sum of the positive assembly values) * norm
+ * (control::forward passes 1.0).  fasm (nx, ny, ng); negative = 1 when an
+ * assembly value is negative (the reference prints a warning). */
+adp_status adp_edit_asmflux(adp_handle* h, int nx, int ny, const int* xdiv, const int* ydiv, double norm, double* fasm,
+                            int* negative);
+
 /* -- batched solves ------------------------------------------------------ */
 
 /* Many independent cores solved together; no counterpart in the reference,

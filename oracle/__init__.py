@@ -105,6 +105,9 @@ def lib(variant: str = "plain"):
         L.ora_get_iarray.argtypes = [vp, cp, ipp]
         L.ora_get_trace.argtypes = [vp, ipp, dp, dp, dp, ipp, dp, ipp]
         L.ora_reset.argtypes = [vp]
+        L.ora_asmpow.argtypes = [vp, dp, dp, ipp, ipp]
+        L.ora_axipow.argtypes = [vp, dp, dp, ipp]
+        L.ora_asmflux.argtypes = [vp, dp, ctypes.c_double, dp, ipp]
         _libs[variant] = L
     return _libs[variant]
 
@@ -181,6 +184,34 @@ class Oracle:
         p = np.zeros(self.geti("nnod"))
         self._check(self.L.ora_powdis(self.h, _dp(p)))
         return p
+
+    # -- output edits of control::forward (mod_io.f90:3267-3644) ---------------
+    def asmpow(self, fn):
+        """AsmPow: (fasm (nx, ny), (imax, jmax)) of a node field such as PowDis."""
+        nx, ny = self.geti("nx"), self.geti("ny")
+        out = np.zeros(nx * ny)
+        im, jm = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.ora_asmpow(self.h, _dp(np.ascontiguousarray(fn, dtype=np.float64)), _dp(out),
+                                      ctypes.byref(im), ctypes.byref(jm)))
+        return out.reshape((nx, ny), order="F"), (im.value, jm.value)
+
+    def axipow(self, fn):
+        """AxiPow: (faxi (nz,), kmax)."""
+        out = np.zeros(self.geti("nz"))
+        km = ctypes.c_int()
+        self._check(self.L.ora_axipow(self.h, _dp(np.ascontiguousarray(fn, dtype=np.float64)), _dp(out),
+                                      ctypes.byref(km)))
+        return out, km.value
+
+    def asmflux(self, f=None, norm=1.0):
+        """AsmFlux of f (nnod, ng) (default: the oracle's f0): (fasm (nx, ny, ng), negative)."""
+        nx, ny, ng = self.geti("nx"), self.geti("ny"), self.geti("ng")
+        out = np.zeros(nx * ny * ng)
+        neg = ctypes.c_int()
+        fa = None if f is None else np.asfortranarray(f, dtype=np.float64).reshape(-1, order="F")
+        self._check(self.L.ora_asmflux(self.h, _dp(fa) if fa is not None else None, float(norm), _dp(out),
+                                       ctypes.byref(neg)))
+        return out.reshape((nx, ny, ng), order="F"), bool(neg.value)
 
     def matrix_setup(self, opt=1):
         self._check(self.L.ora_matrix_setup(self.h, opt))

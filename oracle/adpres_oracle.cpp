@@ -1528,6 +1528,144 @@ static void powdis(Ora& o, double* pw) {
   for (int n = 0; n < N; ++n) pw[n] = pw[n] / tpow;
 }
 
+// Output edits of control::forward (mod_control.f90:33-44), numeric part.
+// fx(i,j,k) is the node field on the box, 0 where there is no node.
+static std::vector<double> box_field(const Ora& o, const double* fn) {
+  std::vector<double> fx((size_t)o.nxx * o.nyy * o.nzz, 0.0);
+  for (int n = 0; n < o.nnod; ++n)
+    fx[(o.ix[n] - 1) + (size_t)o.nxx * ((o.iy[n] - 1) + (size_t)o.nyy * (o.iz[n] - 1))] = fn[n];
+  return fx;
+}
+
+// AsmPow (mod_io.f90:3267-3403): axially averaged node values, area-weighted
+// assembly averages, normalised so that the non-zero assemblies average 1,
+// and the first maximum in (j, i) order.  fasm is (nx,ny); imax/jmax 1-based.
+static void asmpow(Ora& o, const double* fn, double* fasm, int* imax, int* jmax) {
+  const std::vector<double> fx = box_field(o, fn);
+  auto FX = [&](int i, int j, int k) { return fx[(i - 1) + (size_t)o.nxx * ((j - 1) + (size_t)o.nyy * (k - 1))]; };
+  std::vector<double> fnode((size_t)o.nxx * o.nyy, 0.0);
+  for (int j = 1; j <= o.nyy; ++j)
+    for (int i = o.ysmin[j - 1]; i <= o.ysmax[j - 1]; ++i) {
+      double summ = 0.0, vsumm = 0.0;
+      for (int k = 1; k <= o.nzz; ++k) {
+        summ = summ + FX(i, j, k) * o.zdel[k - 1];
+        vsumm = vsumm + o.zdel[k - 1];
+      }
+      fnode[(i - 1) + (size_t)o.nxx * (j - 1)] = summ / vsumm;
+    }
+  int nfuel = 0;
+  double totp = 0.0;
+  int ys = 1, yf = 0;
+  for (int j = 1; j <= o.ny; ++j) {
+    yf += o.ydiv[j - 1];
+    int xf = 0, xs = 1;
+    for (int i = 1; i <= o.nx; ++i) {
+      xf += o.xdiv[i - 1];
+      double summ = 0.0, vsumm = 0.0;
+      for (int ly = ys; ly <= yf; ++ly)
+        for (int lx = xs; lx <= xf; ++lx) {
+          summ = summ + fnode[(lx - 1) + (size_t)o.nxx * (ly - 1)] * o.xdel[lx - 1] * o.ydel[ly - 1];
+          vsumm = vsumm + o.xdel[lx - 1] * o.ydel[ly - 1];
+        }
+      double& fa = fasm[(i - 1) + (size_t)o.nx * (j - 1)];
+      fa = summ / vsumm;
+      xs += o.xdiv[i - 1];
+      if (fa > 0.0) { ++nfuel; totp = totp + fa; }
+    }
+    ys += o.ydiv[j - 1];
+  }
+  *imax = 1;
+  *jmax = 1;
+  double fmax = 0.0;
+  for (int j = 1; j <= o.ny; ++j)
+    for (int i = 1; i <= o.nx; ++i) {
+      double& fa = fasm[(i - 1) + (size_t)o.nx * (j - 1)];
+      if (totp > 0.) fa = (double)(float)nfuel / totp * fa;   // REAL(nfuel) is default (single) real
+      if (fa > fmax) { *imax = i; *jmax = j; fmax = fa; }
+    }
+}
+
+// AxiPow (mod_io.f90:3406-3498): node values summed over each axial region
+// (zdiv planes) divided by its volume, normalised so the non-zero regions
+// average 1; the first maximum.  faxi is (nz); kmax 1-based.
+static void axipow(Ora& o, const double* fn, double* faxi, int* kmax) {
+  const std::vector<double> fx = box_field(o, fn);
+  int nfuel = 0, ztot = 0;
+  double totp = 0.0;
+  for (int k = 1; k <= o.nz; ++k) {
+    double summ = 0.0, vsumm = 0.0;
+    for (int lz = 1; lz <= o.zdiv[k - 1]; ++lz) {
+      ++ztot;
+      for (int j = 1; j <= o.nyy; ++j)
+        for (int i = o.ysmin[j - 1]; i <= o.ysmax[j - 1]; ++i) {
+          summ = summ + fx[(i - 1) + (size_t)o.nxx * ((j - 1) + (size_t)o.nyy * (ztot - 1))];
+          vsumm = vsumm + o.vdel[o.XYZ(i, j, ztot) - 1];
+        }
+    }
+    faxi[k - 1] = summ / vsumm;
+    if (faxi[k - 1] > 0.0) { ++nfuel; totp = totp + faxi[k - 1]; }
+  }
+  double fmax = 0.0;
+  *kmax = 1;
+  for (int k = 1; k <= o.nz; ++k) {
+    faxi[k - 1] = (double)(float)nfuel / totp * faxi[k - 1];
+    if (faxi[k - 1] > fmax) { *kmax = k; fmax = faxi[k - 1]; }
+  }
+}
+
+// AsmFlux (mod_io.f90:3501-3644): per group, volume-weighted axial average
+// of the node flux, area-weighted assembly averages, scaled by
+// norm / sum(positive assemblies) * norm when norm is given (forward calls
+// it with 1.0); negf = 1 when an assembly average is negative.
+static void asmflux(Ora& o, const double* f, bool has_norm, double norm, double* fasm, int* negf) {
+  const int G = o.ng;
+  std::vector<double> fnode((size_t)o.nxx * o.nyy * G, 0.0);
+  for (int g = 1; g <= G; ++g) {
+    const std::vector<double> fx = box_field(o, f + (size_t)o.nnod * (g - 1));
+    for (int j = 1; j <= o.nyy; ++j)
+      for (int i = o.ysmin[j - 1]; i <= o.ysmax[j - 1]; ++i) {
+        double summ = 0.0, vsumm = 0.0;
+        for (int k = 1; k <= o.nzz; ++k) {
+          const double v = fx[(i - 1) + (size_t)o.nxx * ((j - 1) + (size_t)o.nyy * (k - 1))];
+          summ = summ + v * o.xdel[i - 1] * o.ydel[j - 1] * o.zdel[k - 1];
+          vsumm = vsumm + o.xdel[i - 1] * o.ydel[j - 1] * o.zdel[k - 1];
+        }
+        fnode[(i - 1) + (size_t)o.nxx * ((j - 1) + (size_t)o.nyy * (g - 1))] = summ / vsumm;
+      }
+  }
+  *negf = 0;
+  std::vector<double> totp(G, 0.0);
+  for (int g = 1; g <= G; ++g) {
+    int ys = 1, yf = 0;
+    for (int j = 1; j <= o.ny; ++j) {
+      yf += o.ydiv[j - 1];
+      int xf = 0, xs = 1;
+      for (int i = 1; i <= o.nx; ++i) {
+        xf += o.xdiv[i - 1];
+        double summ = 0.0, vsumm = 0.0;
+        for (int ly = ys; ly <= yf; ++ly)
+          for (int lx = xs; lx <= xf; ++lx) {
+            summ = summ + fnode[(lx - 1) + (size_t)o.nxx * ((ly - 1) + (size_t)o.nyy * (g - 1))] * o.xdel[lx - 1] *
+                              o.ydel[ly - 1];
+            vsumm = vsumm + o.xdel[lx - 1] * o.ydel[ly - 1];
+          }
+        double& fa = fasm[(i - 1) + (size_t)o.nx * ((j - 1) + (size_t)o.ny * (g - 1))];
+        fa = summ / vsumm;
+        xs += o.xdiv[i - 1];
+        if (fa > 0.0) totp[g - 1] = totp[g - 1] + fa;
+        if (fa < 0.0) *negf = 1;
+      }
+      ys += o.ydiv[j - 1];
+    }
+  }
+  if (has_norm)
+    for (int g = 1; g <= G; ++g)
+      for (int q = 0; q < o.nx * o.ny; ++q) {
+        double& fa = fasm[q + (size_t)o.nx * o.ny * (g - 1)];
+        fa = norm / totp[g - 1] * fa * norm;
+      }
+}
+
 thread_local std::string g_err;
 
 template <class F>
@@ -1668,6 +1806,22 @@ int ora_get_matrix7(void* h, double* out) {
         }
       }
   });
+}
+
+int ora_asmpow(void* h, const double* fn, double* fasm, int* imax, int* jmax) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] { asmpow(*o, fn, fasm, imax, jmax); });
+}
+
+int ora_axipow(void* h, const double* fn, double* faxi, int* kmax) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] { axipow(*o, fn, faxi, kmax); });
+}
+
+// f: (nnod, ng) flux, NULL for the oracle's own f0; norm <= 0: not given
+int ora_asmflux(void* h, const double* f, double norm, double* fasm, int* negf) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] { asmflux(*o, f ? f : o->f0.data(), norm > 0, norm, fasm, negf); });
 }
 
 int ora_get_int(void* h, const char* name) {
