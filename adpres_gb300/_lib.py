@@ -97,6 +97,9 @@ SIGNATURES = {
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "adp_adjoint_sens": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _dp, _dp, ctypes.POINTER(AdpReport)]),
     "adp_get_timers": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpTimers)]),
+    "adp_reactivity": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_double)]),
+    "adp_core_beta": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, _dp, _ip,
+                                     ctypes.POINTER(ctypes.c_double)]),
     "adp_edit_asmpow": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, _ip, _dp, _ip, _ip]),
     "adp_edit_axipow": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _dp, _ip]),
     "adp_edit_asmflux": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, _ip, ctypes.c_double, _dp,

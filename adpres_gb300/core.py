@@ -203,6 +203,25 @@ class Core:
     def set_launch(self, blocks=0, threads=0):
         self._check(self.L.adp_set_launch(self.h, int(blocks), int(threads)))
 
+    # -- adjoint-weighted edits (mod_trans.f90:648-746) ------------------------
+    def reactivity(self, af, sigrp=None):
+        """reactivity: (src - lea - rem) / fde of the current state weighted by af (nnod, ng)."""
+        a = _fortran(af)
+        s = None if sigrp is None else _fortran(sigrp)
+        rho = ctypes.c_double()
+        self._check(self.L.adp_reactivity(self.h, dptr(a), dptr(s), ctypes.byref(rho)))
+        return rho.value
+
+    def core_beta(self, af, ibeta, mat):
+        """calc_beta: delayed fraction weighted by af, ibeta (nmat, nf), mat (nnod,) 1-based."""
+        a = _fortran(af)
+        ib = np.asfortranarray(ibeta, dtype=np.float64)
+        m = _c(mat, np.int32)
+        beta = ctypes.c_double()
+        self._check(self.L.adp_core_beta(self.h, dptr(a), int(ib.shape[0]), int(ib.shape[1]),
+                                         dptr(ib.reshape(-1, order="F")), iptr(m), ctypes.byref(beta)))
+        return beta.value
+
     # -- output edits (mod_io.f90:3267-3644) ----------------------------------
     def _divs(self, name, div):
         if div is None:

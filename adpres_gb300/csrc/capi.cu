@@ -239,6 +239,7 @@ adp_status adp_destroy(adp_handle* h) {
   if (h->ar.base) cudaFree(h->ar.base);
   if (h->adj_base) cudaFree(h->adj_base);
   if (h->edit_base) cudaFree(h->edit_base);
+  if (h->react_base) cudaFree(h->react_base);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   for (cudaEvent_t e : {h->e0, h->e1, h->e2, h->e3})
     if (e) cudaEventDestroy(e);

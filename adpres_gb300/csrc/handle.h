@@ -79,6 +79,9 @@ struct adp_handle {
   // output edits (adp_edit_*), allocated on first use
   char* edit_base = nullptr;
   size_t edit_size = 0;
+  // adjoint-weighted edits (adp_reactivity, adp_core_beta), allocated on first use
+  char* react_base = nullptr;
+  size_t react_size = 0;
   // discrete adjoint (adp_adjoint_sens), allocated on its first call
   char* adj_base = nullptr;
   double* d_AT = nullptr;

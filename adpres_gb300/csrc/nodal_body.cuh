@@ -70,6 +70,34 @@ __device__ __forceinline__ const double* latest_phi(const NodalParams& P) {
 // ---------------------------------------------------------------------------
 // get_source / Lxyz (mod_nodal.f90:901-1043)
 // ---------------------------------------------------------------------------
+// Net leakage of node b per direction (Lxyz): currents from df, dn and the
+// flux F of one group; df, dn are that group's [6][NB] planes.
+__device__ __forceinline__ void net_leakage(const BoxGeom& G, const double* F, const double* df, const double* dn,
+                                            int b, double (&L)[3]) {
+  const int NB = G.NB;
+  const unsigned m = G.nbm[b];
+  const double fn = F[b];
+  for (int u = 0; u < 3; ++u) {
+    const int fp = 2 * u, fm = 2 * u + 1;
+    const double dfp = df[(size_t)fp * NB + b], dnp = dn[(size_t)fp * NB + b];
+    const double dfm = df[(size_t)fm * NB + b], dnm = dn[(size_t)fm * NB + b];
+    double jp, jm;
+    if (!(m & (1u << fp))) {
+      jp = (G.bcf[fp] == 2) ? 0.0 : dfp * fn - dnp * fn;
+    } else {
+      const double fpv = F[b + face_off(G, fp)];
+      jp = -dfp * (fpv - fn) - dnp * (fpv + fn);
+    }
+    if (!(m & (1u << fm))) {
+      jm = (G.bcf[fm] == 2) ? 0.0 : -dfm * fn - dnm * fn;
+    } else {
+      const double fmv = F[b + face_off(G, fm)];
+      jm = -dfm * (fn - fmv) - dnm * (fn + fmv);
+    }
+    L[u] = (jp - jm) / hdir(G, u, b);
+  }
+}
+
 __device__ __forceinline__ void tl_source_items(const NodalParams& P, int start, int stride) {
   const BoxGeom& G = P.G;
   const int NB = G.NB, ng = P.ng;
@@ -78,31 +106,8 @@ __device__ __forceinline__ void tl_source_items(const NodalParams& P, int start,
   for (int q = start; q < total; q += stride) {
     const int n = q % P.nnod, g = q / P.nnod;
     const int b = P.act[n];
-    const unsigned m = G.nbm[b];
-    const double* F = phi + (size_t)g * P.NBH;
-    const double* df = P.df + (size_t)g * 6 * NB;
-    const double* dn = P.dn + (size_t)g * 6 * NB;
-    const double fn = F[b];
     double L[3];
-    for (int u = 0; u < 3; ++u) {
-      const int fp = 2 * u, fm = 2 * u + 1;
-      const double dfp = df[(size_t)fp * NB + b], dnp = dn[(size_t)fp * NB + b];
-      const double dfm = df[(size_t)fm * NB + b], dnm = dn[(size_t)fm * NB + b];
-      double jp, jm;
-      if (!(m & (1u << fp))) {
-        jp = (G.bcf[fp] == 2) ? 0.0 : dfp * fn - dnp * fn;
-      } else {
-        const double fpv = F[b + face_off(G, fp)];
-        jp = -dfp * (fpv - fn) - dnp * (fpv + fn);
-      }
-      if (!(m & (1u << fm))) {
-        jm = (G.bcf[fm] == 2) ? 0.0 : -dfm * fn - dnm * fn;
-      } else {
-        const double fmv = F[b + face_off(G, fm)];
-        jm = -dfm * (fn - fmv) - dnm * (fn + fmv);
-      }
-      L[u] = (jp - jm) / hdir(G, u, b);
-    }
+    net_leakage(G, phi + (size_t)g * P.NBH, P.df + (size_t)g * 6 * NB, P.dn + (size_t)g * 6 * NB, b, L);
     P.S[((size_t)0 * ng + g) * NB + b] = L[1] + L[2];
     P.S[((size_t)1 * ng + g) * NB + b] = L[0] + L[2];
     P.S[((size_t)2 * ng + g) * NB + b] = L[0] + L[1];

@@ -247,6 +247,21 @@ adp_status adp_edit_axipow(adp_handle* h, int nz, const int* zdiv, double* faxi,
 adp_status adp_edit_asmflux(adp_handle* h, int nx, int ny, const int* xdiv, const int* ydiv, double norm, double* fasm,
                             int* negative);
 
+/* -- adjoint-weighted edits (mod_trans.f90:648-746) ----------------------- */
+
+/* reactivity (mod_trans.f90:648-688) of the handle's current flux and
+ * fission source: rho = (src - lea - rem) / fde with the weight af
+ * (nnod, ng) (an adjoint flux: outer_ad's, or adp_adjoint_sens's psi), the
+ * scattering-in and fission sources, the net leakage of Lxyz from df, dn
+ * and the flux, and the removal sigrp (nnod, ng; NULL for the handle's
+ * sigr).  For a converged static solution rho = 1 - 1/k for any af. */
+adp_status adp_reactivity(adp_handle* h, const double* af, const double* sigrp, double* rho);
+/* calc_beta (mod_trans.f90:692-746): core-averaged delayed neutron
+ * fraction weighted by af (nnod, ng), from the delayed fractions
+ * ibeta (nmat, nf) of the materials mat (nnod), 1 <= nf <= 8. */
+adp_status adp_core_beta(adp_handle* h, const double* af, int nmat, int nf, const double* ibeta, const int* mat,
+                         double* beta);
+
 /* -- batched solves ------------------------------------------------------ */
 
 /* Many independent cores solved together; no counterpart in the reference,

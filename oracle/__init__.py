@@ -106,6 +106,8 @@ def lib(variant: str = "plain"):
         L.ora_get_trace.argtypes = [vp, ipp, dp, dp, dp, ipp, dp, ipp]
         L.ora_reset.argtypes = [vp]
         L.ora_asmpow.argtypes = [vp, dp, dp, ipp, ipp]
+        L.ora_reactivity.argtypes = [vp, dp, dp, dp]
+        L.ora_calc_beta.argtypes = [vp, dp, ip, dp, dp]
         L.ora_axipow.argtypes = [vp, dp, dp, ipp]
         L.ora_asmflux.argtypes = [vp, dp, ctypes.c_double, dp, ipp]
         _libs[variant] = L
@@ -184,6 +186,24 @@ class Oracle:
         p = np.zeros(self.geti("nnod"))
         self._check(self.L.ora_powdis(self.h, _dp(p)))
         return p
+
+    # -- adjoint-weighted edits (mod_trans.f90:648-746) ------------------------
+    def reactivity(self, af, sigrp=None):
+        """reactivity(af, sigrp): adjoint-weighted balance of the current state."""
+        a = np.asfortranarray(af, dtype=np.float64).reshape(-1, order="F")
+        s = None if sigrp is None else np.asfortranarray(sigrp, dtype=np.float64).reshape(-1, order="F")
+        rho = ctypes.c_double()
+        self._check(self.L.ora_reactivity(self.h, _dp(a), _dp(s) if s is not None else None, ctypes.byref(rho)))
+        return rho.value
+
+    def calc_beta(self, af, ibeta):
+        """calc_beta(af) with delayed fractions ibeta (nmat, nf)."""
+        a = np.asfortranarray(af, dtype=np.float64).reshape(-1, order="F")
+        ib = np.asfortranarray(ibeta, dtype=np.float64)
+        beta = ctypes.c_double()
+        self._check(self.L.ora_calc_beta(self.h, _dp(a), int(ib.shape[1]), _dp(ib.reshape(-1, order="F")),
+                                         ctypes.byref(beta)))
+        return beta.value
 
     # -- output edits of control::forward (mod_io.f90:3267-3644) ---------------
     def asmpow(self, fn):

@@ -1666,6 +1666,56 @@ static void asmflux(Ora& o, const double* f, bool has_norm, double norm, double*
       }
 }
 
+// reactivity (mod_trans.f90:648-688): adjoint-weighted balance of the
+// current state, rho = (src - lea - rem) / fde, with the scattering-in and
+// fission sources, the net leakage of Lxyz and the removal sigrp.
+static double reactivity(Ora& o, const double* af, const double* sigrp) {
+  const int N = o.nnod, G = o.ng;
+  double src = 0., rem = 0., lea = 0., fde = 0.;
+  std::vector<double> scg(N);
+  for (int g = 1; g <= G; ++g) {
+    std::fill(scg.begin(), scg.end(), 0.0);
+    for (int h = 1; h <= G; ++h)
+      for (int n = 1; n <= N; ++n)
+        if (g != h) scg[n - 1] = scg[n - 1] + o.SG(o.sigs, n, h, g) * o.N2(o.f0, n, h);
+    for (int n = 1; n <= N; ++n) {
+      double L1, L2, L3;
+      lxyz(o, n, g, L1, L2, L3);
+      const double L = L1 + L2 + L3;
+      const double a = af[(n - 1) + (size_t)N * (g - 1)];
+      const double chi = o.M2(o.chi, o.mat[n - 1], g);
+      src = src + a * (scg[n - 1] + chi * o.fs0[n - 1]) * o.vdel[n - 1];
+      rem = rem + a * sigrp[(n - 1) + (size_t)N * (g - 1)] * o.N2(o.f0, n, g) * o.vdel[n - 1];
+      lea = lea + a * L * o.vdel[n - 1];
+      fde = fde + a * chi * o.fs0[n - 1] * o.vdel[n - 1];
+    }
+  }
+  return (src - lea - rem) / fde;
+}
+
+// calc_beta (mod_trans.f90:692-746): core-averaged delayed neutron fraction
+// weighted by af, from the delayed fractions ibeta(nmat, nf).
+static double calc_beta(Ora& o, const double* af, int nf, const double* ibeta) {
+  const int N = o.nnod, G = o.ng;
+  std::vector<double> vdum(N, 0.0), vdum2(N, 0.0);
+  for (int g = 1; g <= G; ++g)
+    for (int n = 1; n <= N; ++n) vdum[n - 1] = vdum[n - 1] + o.N2(o.nuf, n, g) * o.N2(o.f0, n, g);
+  for (int g = 1; g <= G; ++g)
+    for (int n = 1; n <= N; ++n)
+      vdum2[n - 1] = vdum2[n - 1] + o.M2(o.chi, o.mat[n - 1], g) * vdum[n - 1] * af[(n - 1) + (size_t)N * (g - 1)];
+  const double F = integrate(o, vdum2);
+  double beta = 0.0;
+  for (int i = 1; i <= nf; ++i) {
+    std::fill(vdum2.begin(), vdum2.end(), 0.0);
+    for (int g = 1; g <= G; ++g)
+      for (int n = 1; n <= N; ++n)
+        vdum2[n - 1] = vdum2[n - 1] + o.M2(o.chi, o.mat[n - 1], g) * ibeta[(o.mat[n - 1] - 1) + (size_t)o.nmat * (i - 1)] *
+                                          vdum[n - 1] * af[(n - 1) + (size_t)N * (g - 1)];
+    beta = beta + integrate(o, vdum2) / F;
+  }
+  return beta;
+}
+
 thread_local std::string g_err;
 
 template <class F>
@@ -1806,6 +1856,17 @@ int ora_get_matrix7(void* h, double* out) {
         }
       }
   });
+}
+
+// af, sigrp: (nnod, ng); sigrp NULL for the oracle's own sigr
+int ora_reactivity(void* h, const double* af, const double* sigrp, double* rho) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] { *rho = reactivity(*o, af, sigrp ? sigrp : o->sigr.data()); });
+}
+
+int ora_calc_beta(void* h, const double* af, int nf, const double* ibeta, double* beta) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] { *beta = calc_beta(*o, af, nf, ibeta); });
 }
 
 int ora_asmpow(void* h, const double* fn, double* fasm, int* imax, int* jmax) {

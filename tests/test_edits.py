@@ -70,3 +70,35 @@ def test_edit_rejects_bad_divisions():
     with pytest.raises(AdpError) as e:
         c.asmpow(xdiv=bad)
     assert e.value.status == ADP_ERR_INPUT
+
+
+def test_reactivity_and_beta_match_oracle():
+    """adp_reactivity / adp_core_beta on the oracle's converged state against
+    the oracle's restatement (weights: the reference's own adjoint flux and
+    a seeded field)."""
+    text = synth.small_core(seed=7, ng=3, adf=True)
+    o, c = _pair(text)
+    nn, ng, nm = o.geti("nnod"), o.geti("ng"), o.geti("nmat")
+    # the GPU handle needs the oracle's dn and fission source for the leakage and sources
+    c.set_state(f0=o.fortran("f0", (nn, ng)), fs0=o.array("fs0"), keff=o.getd("Ke"),
+                dn=o.fortran("dn", (nn, ng, 6)))
+    c.outer(frozen_dn=True, trace=False)   # df/A on the handle; one frozen solve from the oracle's state
+    c.set_state(f0=o.fortran("f0", (nn, ng)), fs0=o.array("fs0"), keff=o.getd("Ke"),
+                dn=o.fortran("dn", (nn, ng, 6)))
+    rng = np.random.default_rng(3)
+    for af in (np.ones((nn, ng)), rng.uniform(0.2, 3.0, (nn, ng))):
+        assert abs(c.reactivity(af) - o.reactivity(af)) <= 1e-12 * max(1.0, abs(o.reactivity(af)))
+    ib = rng.uniform(1e-4, 2e-3, (nm, 6))
+    af = rng.uniform(0.2, 3.0, (nn, ng))
+    dk = c.deck
+    assert abs(c.core_beta(af, ib, dk.mat) - o.calc_beta(af, ib)) <= 1e-13
+
+
+def test_reactivity_static_identity_on_gpu_solution():
+    from adpres_gb300.core import Core
+    c = Core.from_deck(deck.parse(synth.quarter_core_2d(0)), serc=1e-12, ferc=1e-12)
+    rep = c.outer(trace=False)
+    S, psi, _ = c.adjoint_sens(tol=1e-12)
+    nn, ng = c.nnod, c.ng
+    for af in (np.ones((nn, ng)), psi):
+        assert abs(c.reactivity(af) - (1 - 1 / rep.keff)) < 1e-9
