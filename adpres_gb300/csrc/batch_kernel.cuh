@@ -62,7 +62,7 @@ __device__ __forceinline__ bool solve_core(const BatchInst& I, unsigned rank, un
     interface_items<NG>(N, start, stride, best);
     nd_block_reduce(N, best, rank);
     if (!team_barrier(C, size, rank)) return false;
-    if (lead) nodal_finish_body(N, size);
+    if (rank == 0 && threadIdx.x < 32) nodal_finish_warp(N, size);
     if (!team_barrier(C, size, rank)) return false;
     if (vld(&C->status) || vld(&C->converged) || vld(&C->max_reached)) break;
     assemble_items(I.ap0, start, stride);

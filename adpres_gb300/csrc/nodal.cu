@@ -35,8 +35,8 @@ __global__ void __launch_bounds__(128) k_interface(NodalParams P) {
 }
 
 __global__ void k_nodal_finish(NodalParams P) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  nodal_finish_body(P, P.nd_blocks);
+  if (threadIdx.x >= 32 || blockIdx.x != 0) return;
+  nodal_finish_warp(P, P.nd_blocks);
 }
 
 template <int NG>

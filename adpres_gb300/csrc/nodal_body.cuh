@@ -558,11 +558,24 @@ __device__ __forceinline__ void nd_block_reduce(const NodalParams& P, NdBest bes
 // ndmax with its location, the divergence check (mod_nodal.f90:131-142) and
 // the convergence test of the outer that triggered the update
 // (mod_cmfd.f90:495-505).
-__device__ __forceinline__ void nodal_finish_body(const NodalParams& P, int nparts) {
+// Run by the 32 lanes of one warp: the lanes scan the partials, then a
+// shuffle reduction; (value descending, sweep key ascending) is a total
+// order, so the winner does not depend on the scan order.  Lane 0 then
+// updates the control block.
+__device__ __forceinline__ void nodal_finish_warp(const NodalParams& P, int nparts) {
   OuterCtl* C = P.ctl;
+  const int lane = threadIdx.x & 31;
   NdBest bb{0.0, 0x7fffffffffffffffLL, -1};
-  for (int k = 0; k < nparts; ++k)
+  for (int k = lane; k < nparts; k += 32)
     nd_consider(bb, __ldcg(P.nd_val + k), __ldcg(P.nd_key + k), __ldcg(P.nd_loc + k));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double v = __shfl_xor_sync(0xffffffffu, bb.val, o);
+    const long long key = __shfl_xor_sync(0xffffffffu, bb.key, o);
+    const int loc = __shfl_xor_sync(0xffffffffu, bb.loc, o);
+    nd_consider(bb, v, key, loc);
+  }
+  if (lane != 0) return;
   C->ndmax = bb.val;
   if (bb.val > 0.0 && bb.loc >= 0) {
     const int b = bb.loc;

@@ -339,12 +339,15 @@ def run_ours(args):
         peak_src = "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
+    # DRAM traffic of one launch: the ncu capture of the 68x68x40 core's first
+    # launch gives the bytes per box row and outer; scaled to this launch by
+    # box rows x outers per launch (the same kernel on twice the planes)
     traffic = None
     prof = os.path.join(ROOT, "profiles", "k_outer_mixed_core_4g.json")
-    if os.path.exists(prof):
+    if os.path.exists(prof) and prec == "mixed":
         with open(prof) as f:
             pj = json.load(f)
-        traffic = pj.get("dram_bytes_per_launch_full")
+        traffic = pj["dram_bytes_per_row_outer"] * NB * n_outers / launches
     gpu_launches = int(sum(2 + 0 for _ in outers) + launches + 5 * sum(nodal))
 
     # FP64 path on the same core: solves/s and the mixed-precision error
