@@ -74,7 +74,13 @@ class Core:
         kw.update(over)
         core = cls(dk.nxx, dk.nyy, dk.nzz, dk.ix, dk.iy, dk.iz, dk.xdel, dk.ydel, dk.zdel, dk.bc, dk.ng, **kw)
         core.deck = dk
-        core.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
+        if getattr(dk, "feedback", None):
+            # XS_updt(bcon, ftem, mtem, cden, bpos) with the deck's feedback cards
+            from .feedback import xs_update
+            t = xs_update(dk)
+            core.xs_updt_nodes(t["sigtr"], t["siga"], t["nuf"], t["sigf"], dk.chi, dk.mat, t["sigs"], dk.dc)
+        else:
+            core.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
         return core
 
     def close(self):
@@ -179,6 +185,12 @@ class Core:
         return (f0.reshape((self.nnod, self.ng), order="F"), fs0, k.value,
                 dn.reshape((self.nnod, self.ng, 6), order="F"))
 
+    def flux(self):
+        """f0 (nnod, ng) of the current state, without the other state arrays."""
+        f0 = np.zeros(self.nnod * self.ng)
+        self._check(self.L.adp_get_state(self.h, dptr(f0), None, None, None))
+        return f0.reshape((self.nnod, self.ng), order="F")
+
     def set_state(self, f0=None, fs0=None, keff=None, dn=None):
         a = None if f0 is None else _fortran(f0)
         b = None if fs0 is None else _c(fs0)
@@ -265,7 +277,15 @@ class Core:
 
 
 def solve_deck(dk, precision="fp64"):
-    """control::forward / control::adjoint for a parsed deck: (report, power, core)."""
+    """control::forward / control::adjoint for a parsed deck: (report, power, core).
+
+    In mode BCSEARCH (th::cbsearch, mod_th.f90:752-837) the report is the last
+    outer of the critical boron search and core.bcsearch holds its iterates
+    (bcon, k, outers)."""
     core = Core.from_deck(dk, precision=precision)
+    if dk.mode == "BCSEARCH":
+        from .feedback import cbsearch
+        core.bcsearch = cbsearch(core, dk)
+        return core.last_report, core.power(), core
     rep, p = core.adjoint() if dk.adjoint else core.forward()
     return rep, p, core

@@ -144,6 +144,27 @@ struct BatchTask {
   int inst, rank, size, pad;
 };
 
+// Material tables of base_updt (mod_xsec.f90:172-195), Fortran (nmat, ng)
+// and sigs (nmat, ng, ng); null members are not expanded.
+struct XsTables {
+  const double* sigtr;
+  const double* siga;
+  const double* nuf;
+  const double* sigf;
+  const double* chi;
+  const double* sigs;
+};
+
+// The handle's box planes that base_updt writes: [ng][NB], sigs [ng][ng][NB].
+struct XsBox {
+  double* sigtr;
+  double* siga;
+  double* nuf;
+  double* sigf;
+  double* chin;
+  double* sigs;
+};
+
 // Launchers (return the launch error, if any)
 cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st);
 cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st);
@@ -164,10 +185,21 @@ cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* 
 // x = hi + lo with hi = (float)x (double-float copies of the mixed path)
 cudaError_t launch_split(const double* x, float* hi, float* lo, long long n, cudaStream_t st);
 cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st);
+// node-order <-> box transfers (transfer.cu): host layout a(nn, A, B), node
+// fastest; device planes [A][B] of stride `stride` indexed by act[n]
+cudaError_t launch_nodes_to_box(const double* src, double* dst, const int* act, int nn, int A, int B,
+                                long long dstride, int chk, int* flags, cudaStream_t st);
+cudaError_t launch_box_to_nodes(const double* src, double* dst, const int* act, int nn, int A, int B,
+                                long long sstride, cudaStream_t st);
+cudaError_t launch_fill_box(double* dst, const int* act, int nn, int ncomp, long long dstride, double v,
+                            cudaStream_t st);
+cudaError_t launch_base_updt(const XsTables& T, const int* mat, const int* act, int nn, int nmat, int G, long long NB,
+                             const XsBox& X, int* flags, cudaStream_t st);
 // batched solve (batch_k_*.cu): a cooperative launch of `blocks` blocks
-cudaError_t launch_batch(bool mixed, int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,
-                         const int* task_begin, cudaStream_t st);
-int batch_max_blocks_per_sm(bool mixed, int ng, int threads);
+// minb: blocks per SM the kernel's registers are sized for (1, or 2 with 256 threads)
+cudaError_t launch_batch(bool mixed, int ng, int threads, int minb, int blocks, const BatchInst* insts,
+                         const BatchTask* tasks, const int* task_begin, cudaStream_t st);
+int batch_max_blocks_per_sm(bool mixed, int ng, int threads, int minb);
 bool batch_supported(int ng, int threads);
 cudaError_t launch_batch_init(const BatchInst* insts, int n, cudaStream_t st);
 cudaError_t launch_batch_gather(const BatchInst* insts, int n, OuterCtl* out, cudaStream_t st);

@@ -30,21 +30,21 @@
 #include "handle.h"
 
 namespace adp {
-cudaError_t launch_batch_fp64(int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,
-                              const int* begin, cudaStream_t st);
-cudaError_t launch_batch_mixed(int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,
-                               const int* begin, cudaStream_t st);
-int batch_occupancy_fp64(int ng, int threads);
-int batch_occupancy_mixed(int ng, int threads);
+cudaError_t launch_batch_fp64(int ng, int threads, int minb, int blocks, const BatchInst* insts,
+                              const BatchTask* tasks, const int* begin, cudaStream_t st);
+cudaError_t launch_batch_mixed(int ng, int threads, int minb, int blocks, const BatchInst* insts,
+                               const BatchTask* tasks, const int* begin, cudaStream_t st);
+int batch_occupancy_fp64(int ng, int threads, int minb);
+int batch_occupancy_mixed(int ng, int threads, int minb);
 
-cudaError_t launch_batch(bool mixed, int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,
-                         const int* task_begin, cudaStream_t st) {
-  return mixed ? launch_batch_mixed(ng, threads, blocks, insts, tasks, task_begin, st)
-               : launch_batch_fp64(ng, threads, blocks, insts, tasks, task_begin, st);
+cudaError_t launch_batch(bool mixed, int ng, int threads, int minb, int blocks, const BatchInst* insts,
+                         const BatchTask* tasks, const int* task_begin, cudaStream_t st) {
+  return mixed ? launch_batch_mixed(ng, threads, minb, blocks, insts, tasks, task_begin, st)
+               : launch_batch_fp64(ng, threads, minb, blocks, insts, tasks, task_begin, st);
 }
 
-int batch_max_blocks_per_sm(bool mixed, int ng, int threads) {
-  return mixed ? batch_occupancy_mixed(ng, threads) : batch_occupancy_fp64(ng, threads);
+int batch_max_blocks_per_sm(bool mixed, int ng, int threads, int minb) {
+  return mixed ? batch_occupancy_mixed(ng, threads, minb) : batch_occupancy_fp64(ng, threads, minb);
 }
 
 bool batch_supported(int ng, int threads) { return ng >= 1 && ng <= 4 && (threads == 256 || threads == 512); }
@@ -201,8 +201,8 @@ adp_status upload_plan(adp_batch* b) {
 cudaError_t enqueue_solve(adp_batch* b) {
   cudaError_t e;
   if ((e = launch_batch_init(b->d_inst, b->n, b->st)) != cudaSuccess) return e;
-  if ((e = launch_batch(b->mixed, b->ng, b->cfg.threads, b->blocks, b->d_inst, b->d_tasks, b->d_begin, b->st)) !=
-      cudaSuccess)
+  if ((e = launch_batch(b->mixed, b->ng, b->cfg.threads, b->cfg.blocks_per_sm, b->blocks, b->d_inst, b->d_tasks,
+                        b->d_begin, b->st)) != cudaSuccess)
     return e;
   if ((e = launch_batch_gather(b->d_inst, b->n, b->d_res, b->st)) != cudaSuccess) return e;
   if ((e = cudaMemcpyAsync(b->h_res, b->d_res, b->n * sizeof(OuterCtl), cudaMemcpyDeviceToHost, b->st)) != cudaSuccess)
@@ -214,7 +214,7 @@ cudaError_t enqueue_solve(adp_batch* b) {
 adp_status prepare(adp_batch* b) {
   if (b->plan_ok) return ADP_OK;
   drop_graph(b);
-  const int occ = batch_max_blocks_per_sm(b->mixed, b->ng, b->cfg.threads);
+  const int occ = batch_max_blocks_per_sm(b->mixed, b->ng, b->cfg.threads, b->cfg.blocks_per_sm);
   if (occ < 1) return bfail(b, ADP_ERR_CUDA, "batched kernel cannot be resident with this block size");
   b->blocks = std::min(b->sms * std::min(occ, std::max(1, b->cfg.blocks_per_sm)), kMaxBlocks);
   make_plan(b);
@@ -444,19 +444,20 @@ adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best_out, double* 
   if (s != ADP_OK) return s;
   adp_batch_config best = base;
   double best_t = 1e300;
-  const int threads[2] = {256, 512};
+  // kernel shapes: (threads, blocks per SM) = (256, 1), (256, 2), (512, 1)
+  const int shapes[3][2] = {{256, 1}, {256, 2}, {512, 1}};
   const int teams[3] = {2, 8, 32};
   const double grains[2] = {1.0, 4.0};
   const std::vector<double> meas = b->measured;
-  for (int th : threads) {
-    if (batch_max_blocks_per_sm(b->mixed, b->ng, th) < 1) continue;
+  for (const auto& sh : shapes) {
+    if (batch_max_blocks_per_sm(b->mixed, b->ng, sh[0], sh[1]) < sh[1]) continue;
     for (int mt : teams)
       for (double gr : grains) {
         adp_batch_config c = base;
-        c.threads = th;
+        c.threads = sh[0];
         c.max_team = mt;
         c.grain = gr;
-        c.blocks_per_sm = 1;
+        c.blocks_per_sm = sh[1];
         s = adp_batch_set_config(b, &c);
         if (s != ADP_OK) return s;
         b->measured = meas;   // every candidate plans from the same measurement

@@ -94,8 +94,10 @@ __device__ __forceinline__ bool solve_core(const BatchInst& I, unsigned rank, un
   return true;
 }
 
-template <bool MIXED, int NG, int THREADS>
-__global__ void __launch_bounds__(THREADS, 1)
+// MINB: blocks per SM the register budget is sized for (1, or 2 for
+// 256-thread blocks: 128 registers, two cores' teams sharing an SM).
+template <bool MIXED, int NG, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_batch(const BatchInst* __restrict__ insts, const BatchTask* __restrict__ tasks, const int* __restrict__ begin) {
   __shared__ __align__(16) BatchInst sI;
   const int t0 = begin[blockIdx.x], t1 = begin[blockIdx.x + 1];
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
-template <bool MIXED, int NG, int THREADS>
+template <bool MIXED, int NG, int THREADS, int MINB>
 cudaError_t launch_batch_t(int blocks, const BatchInst* insts, const BatchTask* tasks, const int* begin,
                            cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
@@ -128,13 +130,13 @@ cudaError_t launch_batch_t(int blocks, const BatchInst* insts, const BatchTask* 
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_batch<MIXED, NG, THREADS>, insts, tasks, begin);
+  return cudaLaunchKernelEx(&cfg, k_batch<MIXED, NG, THREADS, MINB>, insts, tasks, begin);
 }
 
-template <bool MIXED, int NG, int THREADS>
+template <bool MIXED, int NG, int THREADS, int MINB>
 int batch_occupancy_t() {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<MIXED, NG, THREADS>, THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch<MIXED, NG, THREADS, MINB>, THREADS, 0);
   return nb;
 }
 
@@ -142,32 +144,42 @@ int batch_occupancy_t() {
 
 namespace adp {
 
-// Dispatch over the compiled group counts (1..4) and block sizes (256, 512).
+// Dispatch over the compiled group counts (1..4) and kernel shapes: 256
+// threads sized for one or two blocks per SM, or 512 threads.
+template <bool MIXED, int NG>
+cudaError_t batch_launch_ng(int threads, int minb, int blocks, const BatchInst* insts, const BatchTask* tasks,
+                            const int* begin, cudaStream_t st) {
+  if (threads == 512) return launch_batch_t<MIXED, NG, 512, 1>(blocks, insts, tasks, begin, st);
+  if (minb >= 2) return launch_batch_t<MIXED, NG, 256, 2>(blocks, insts, tasks, begin, st);
+  return launch_batch_t<MIXED, NG, 256, 1>(blocks, insts, tasks, begin, st);
+}
+
+template <bool MIXED, int NG>
+int batch_occupancy_ng(int threads, int minb) {
+  if (threads == 512) return batch_occupancy_t<MIXED, NG, 512, 1>();
+  if (minb >= 2) return batch_occupancy_t<MIXED, NG, 256, 2>();
+  return batch_occupancy_t<MIXED, NG, 256, 1>();
+}
+
 template <bool MIXED>
-cudaError_t batch_dispatch_launch(int ng, int threads, int blocks, const BatchInst* insts, const BatchTask* tasks,
-                                  const int* begin, cudaStream_t st) {
-  const bool big = threads == 512;
+cudaError_t batch_dispatch_launch(int ng, int threads, int minb, int blocks, const BatchInst* insts,
+                                  const BatchTask* tasks, const int* begin, cudaStream_t st) {
   switch (ng) {
-    case 1: return big ? launch_batch_t<MIXED, 1, 512>(blocks, insts, tasks, begin, st)
-                       : launch_batch_t<MIXED, 1, 256>(blocks, insts, tasks, begin, st);
-    case 2: return big ? launch_batch_t<MIXED, 2, 512>(blocks, insts, tasks, begin, st)
-                       : launch_batch_t<MIXED, 2, 256>(blocks, insts, tasks, begin, st);
-    case 3: return big ? launch_batch_t<MIXED, 3, 512>(blocks, insts, tasks, begin, st)
-                       : launch_batch_t<MIXED, 3, 256>(blocks, insts, tasks, begin, st);
-    case 4: return big ? launch_batch_t<MIXED, 4, 512>(blocks, insts, tasks, begin, st)
-                       : launch_batch_t<MIXED, 4, 256>(blocks, insts, tasks, begin, st);
+    case 1: return batch_launch_ng<MIXED, 1>(threads, minb, blocks, insts, tasks, begin, st);
+    case 2: return batch_launch_ng<MIXED, 2>(threads, minb, blocks, insts, tasks, begin, st);
+    case 3: return batch_launch_ng<MIXED, 3>(threads, minb, blocks, insts, tasks, begin, st);
+    case 4: return batch_launch_ng<MIXED, 4>(threads, minb, blocks, insts, tasks, begin, st);
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <bool MIXED>
-int batch_dispatch_occupancy(int ng, int threads) {
-  const bool big = threads == 512;
+int batch_dispatch_occupancy(int ng, int threads, int minb) {
   switch (ng) {
-    case 1: return big ? batch_occupancy_t<MIXED, 1, 512>() : batch_occupancy_t<MIXED, 1, 256>();
-    case 2: return big ? batch_occupancy_t<MIXED, 2, 512>() : batch_occupancy_t<MIXED, 2, 256>();
-    case 3: return big ? batch_occupancy_t<MIXED, 3, 512>() : batch_occupancy_t<MIXED, 3, 256>();
-    case 4: return big ? batch_occupancy_t<MIXED, 4, 512>() : batch_occupancy_t<MIXED, 4, 256>();
+    case 1: return batch_occupancy_ng<MIXED, 1>(threads, minb);
+    case 2: return batch_occupancy_ng<MIXED, 2>(threads, minb);
+    case 3: return batch_occupancy_ng<MIXED, 3>(threads, minb);
+    case 4: return batch_occupancy_ng<MIXED, 4>(threads, minb);
     default: return 0;
   }
 }

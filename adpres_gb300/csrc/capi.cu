@@ -240,6 +240,7 @@ adp_status adp_destroy(adp_handle* h) {
   if (h->adj_base) cudaFree(h->adj_base);
   if (h->edit_base) cudaFree(h->edit_base);
   if (h->react_base) cudaFree(h->react_base);
+  if (h->xfer_base) cudaFree(h->xfer_base);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   for (cudaEvent_t e : {h->e0, h->e1, h->e2, h->e3})
     if (e) cudaEventDestroy(e);
@@ -454,55 +455,119 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
   return ADP_OK;
 }
 
+// Device staging of the node-order transfers (transfer.cu): one host array
+// of up to max(ng*ng, 6*ng) components, the material numbers, the material
+// tables of nmat materials and the check flags.  Grows, never shrinks.
+struct Xfer {
+  double* stage;
+  int* mat;
+  double* tab;
+  int* flags;
+};
+
+static adp_status xfer_reserve(adp_handle* h, int nmat, Xfer& X) {
+  const size_t nn = h->nnod, G = h->ng;
+  const size_t ncomp = std::max(G * G, 6 * G);
+  const size_t ntab = (5 * G + G * G) * (size_t)std::max(nmat, 1);
+  size_t need = 0;
+  auto add = [&](size_t b) { need += ((b + 255) & ~(size_t)255) + 256; };
+  add(ncomp * nn * 8);
+  add(nn * 4);
+  add(ntab * 8);
+  add(64);
+  if (h->xfer_size < need) {
+    if (h->xfer_base) CK(cudaFree(h->xfer_base));
+    h->xfer_base = nullptr;
+    h->xfer_size = 0;
+    CK(cudaMalloc((void**)&h->xfer_base, need));
+    h->xfer_size = need;
+  }
+  DevArena A;
+  A.base = h->xfer_base;
+  A.size = h->xfer_size;
+  X.stage = (double*)A.take(ncomp * nn * 8);
+  X.mat = (int*)A.take(nn * 4);
+  X.tab = (double*)A.take(ntab * 8);
+  X.flags = (int*)A.take(64);
+  return ADP_OK;
+}
+
+// One host array a(nnod, A, B) (node fastest) into the box planes [A][B]
+// of stride `stride`: a contiguous copy, then the scatter on the device.
+static adp_status put_nodes(adp_handle* h, const Xfer& X, const double* src, int A, int B, double* dst,
+                            long long stride, int chk) {
+  CK(cudaMemcpyAsync(X.stage, src, (size_t)h->nnod * A * B * 8, cudaMemcpyHostToDevice, h->st));
+  CK(launch_nodes_to_box(X.stage, dst, h->d_act, h->nnod, A, B, stride, chk, X.flags, h->st));
+  return ADP_OK;
+}
+
+// The box planes [A][B] back into a host array a(nnod, A, B).
+static adp_status get_nodes(adp_handle* h, const Xfer& X, const double* src, int A, int B, long long stride,
+                            double* dst) {
+  CK(launch_box_to_nodes(src, X.stage, h->d_act, h->nnod, A, B, stride, h->st));
+  CK(cudaMemcpyAsync(dst, X.stage, (size_t)h->nnod * A * B * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return ADP_OK;
+}
+
+// Material numbers in range and chi >= 0 are checked on the host (nnod and
+// nmat*ng values); the node tables' signs on the device.
+static adp_status check_mat(adp_handle* h, int nmat, const int* mat) {
+  for (int n = 0; n < h->nnod; ++n)
+    if (mat[n] < 1 || mat[n] > nmat) return fail(h, ADP_ERR_INPUT, "adp_set_xs: material number out of range");
+  return ADP_OK;
+}
+
+static bool chi_negative(const adp_handle* h, int nmat, const double* chi) {
+  for (size_t q = 0; q < (size_t)h->ng * nmat; ++q)
+    if (chi[q] < 0.) return true;
+  return false;
+}
+
+// check_xs on the inputs that are not recomputed (mod_xsec.f90:90-168), in
+// its order: nu*fission, chi, scattering.
+static adp_status xs_flags(adp_handle* h, const Xfer& X, bool chi_neg) {
+  int fl = 0;
+  CK(cudaMemcpyAsync(&fl, X.flags, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (fl & 1) return fail(h, ADP_ERR_BADXS, "nu*fission xs is negative");
+  if (chi_neg) return fail(h, ADP_ERR_BADXS, "fission spectrum is negative");
+  if (fl & 4) return fail(h, ADP_ERR_BADXS, "scattering xs is negative");
+  return ADP_OK;
+}
+
+static XsBox xs_box(adp_handle* h) {
+  return XsBox{h->d_sigtr, h->d_siga, h->d_nuf, h->d_sigf, h->d_chin, h->d_sigs};
+}
+
+// ADFs dc(nnod, ng, 6) into [ng][6][NB]; 1 where the host gives none.
+static adp_status put_dc(adp_handle* h, const Xfer& X, const double* dc) {
+  if (dc) return put_nodes(h, X, dc, h->ng, 6, h->d_dc, h->NB, 0);
+  CK(launch_fill_box(h->d_dc, h->d_act, h->nnod, h->ng * 6, h->NB, 1.0, h->st));
+  return ADP_OK;
+}
+
+// nu*fission, fission, scattering and ADF node tables and chi of the node's
+// material: the part of the upload that adp_set_xs and adp_xs_updt_nodes share.
 static adp_status upload_xs_common(adp_handle* h, int nmat, const double* nuf, const double* sigf, const double* chi,
-                                   const int* mat, const double* sigs, const double* dc) {
+                                   const int* mat, const double* sigs, const double* dc, Xfer& X, bool& chi_neg) {
   const int nn = h->nnod, G = h->ng;
   h->fwd_ok = false;
   if (nmat < 1 || !nuf || !sigf || !chi || !mat || !sigs) return fail(h, ADP_ERR_INPUT, "adp_set_xs: null array");
-  std::vector<double> chin((size_t)G * nn);
-  for (int n = 0; n < nn; ++n) {
-    if (mat[n] < 1 || mat[n] > nmat) return fail(h, ADP_ERR_INPUT, "adp_set_xs: material number out of range");
-    for (int g = 0; g < G; ++g) chin[(size_t)g * nn + n] = chi[(size_t)g * nmat + (mat[n] - 1)];
-  }
-  // check_xs on the inputs that are not recomputed (mod_xsec.f90:90-168)
-  for (size_t q = 0; q < (size_t)G * nn; ++q)
-    if (nuf[q] < 0.) return fail(h, ADP_ERR_BADXS, "nu*fission xs is negative");
-  for (size_t q = 0; q < (size_t)G * nmat; ++q)
-    if (chi[q] < 0.) return fail(h, ADP_ERR_BADXS, "fission spectrum is negative");
-  for (size_t q = 0; q < (size_t)G * G * nn; ++q)
-    if (sigs[q] < 0.) return fail(h, ADP_ERR_BADXS, "scattering xs is negative");
-  std::vector<double> box;
-  to_box(h, nuf, G, box);
-  CK(cudaMemcpyAsync(h->d_nuf, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  to_box(h, sigf, G, box);
-  CK(cudaMemcpyAsync(h->d_sigf, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  to_box(h, chin.data(), G, box);
-  CK(cudaMemcpyAsync(h->d_chin, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  // sigs(n, g, h) (Fortran, n fastest, g -> h) -> device [g][h][b]
-  box.assign((size_t)G * G * h->NB, 0.0);
-  for (int g = 0; g < G; ++g)
-    for (int hh = 0; hh < G; ++hh)
-      for (int n = 0; n < nn; ++n)
-        box[((size_t)g * G + hh) * h->NB + h->node2box[n]] = sigs[((size_t)hh * G + g) * nn + n];
-  CK(cudaMemcpyAsync(h->d_sigs, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  if (dc) {
-    // dc(n, g, u) (Fortran) -> device [g][u][b]
-    box.assign((size_t)G * 6 * h->NB, 0.0);
-    for (int u = 0; u < 6; ++u)
-      for (int g = 0; g < G; ++g)
-        for (int n = 0; n < nn; ++n)
-          box[((size_t)g * 6 + u) * h->NB + h->node2box[n]] = dc[((size_t)u * G + g) * nn + n];
-  } else {
-    box.assign((size_t)G * 6 * h->NB, 0.0);
-    for (int c = 0; c < G * 6; ++c)
-      for (int n = 0; n < nn; ++n) box[(size_t)c * h->NB + h->node2box[n]] = 1.0;
-  }
-  CK(cudaMemcpyAsync(h->d_dc, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
+  adp_status s = check_mat(h, nmat, mat);
+  if (s != ADP_OK) return s;
+  chi_neg = chi_negative(h, nmat, chi);
+  if ((s = xfer_reserve(h, nmat, X)) != ADP_OK) return s;
+  CK(cudaMemsetAsync(X.flags, 0, sizeof(int), h->st));
+  CK(cudaMemcpyAsync(X.mat, mat, (size_t)nn * 4, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(X.tab, chi, (size_t)G * nmat * 8, cudaMemcpyHostToDevice, h->st));
+  XsTables T{};
+  T.chi = X.tab;
+  CK(launch_base_updt(T, X.mat, h->d_act, nn, nmat, G, h->NB, xs_box(h), X.flags, h->st));
+  if ((s = put_nodes(h, X, nuf, G, 1, h->d_nuf, h->NB, 1)) != ADP_OK) return s;
+  if ((s = put_nodes(h, X, sigf, G, 1, h->d_sigf, h->NB, 0)) != ADP_OK) return s;
+  if ((s = put_nodes(h, X, sigs, G, G, h->d_sigs, h->NB, 4)) != ADP_OK) return s;
+  if ((s = put_dc(h, X, dc)) != ADP_OK) return s;
   h->nmat = nmat;
   return ADP_OK;
 }
@@ -577,32 +642,19 @@ adp_status adp_set_xs(adp_handle* h, int nmat, const double* D, const double* si
     if (D[k] < (double)1.e-20f) return fail(h, ADP_ERR_BADXS, "diffusion coef. is close to zero or negative");
     if (sigr[k] < 0.) return fail(h, ADP_ERR_BADXS, "removal xs is negative");
   }
-  adp_status s = upload_xs_common(h, nmat, nuf, sigf, chi, mat, sigs, dc);
+  Xfer X;
+  bool chi_neg = false;
+  adp_status s = upload_xs_common(h, nmat, nuf, sigf, chi, mat, sigs, dc, X, chi_neg);
   if (s != ADP_OK) return s;
-  std::vector<double> box;
-  to_box(h, D, h->ng, box);
-  CK(cudaMemcpyAsync(h->d_D, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  to_box(h, sigr, h->ng, box);
-  CK(cudaMemcpyAsync(h->d_sigr, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
+  if ((s = put_nodes(h, X, D, h->ng, 1, h->d_D, h->NB, 0)) != ADP_OK) return s;
+  if ((s = put_nodes(h, X, sigr, h->ng, 1, h->d_sigr, h->NB, 0)) != ADP_OK) return s;
+  if ((s = xs_flags(h, X, chi_neg)) != ADP_OK) return s;
   return after_xs(h);
 }
 
-adp_status adp_xs_updt_nodes(adp_handle* h, int nmat, const double* sigtr, const double* siga, const double* nuf,
-                             const double* sigf, const double* chi, const int* mat, const double* sigs,
-                             const double* dc) {
-  if (!h) return ADP_ERR_INPUT;
-  CK(cudaSetDevice(h->dev));
-  if (!sigtr || !siga) return fail(h, ADP_ERR_INPUT, "adp_xs_updt: null sigtr or siga");
-  adp_status s = upload_xs_common(h, nmat, nuf, sigf, chi, mat, sigs, dc);
-  if (s != ADP_OK) return s;
-  std::vector<double> box;
-  to_box(h, sigtr, h->ng, box);
-  CK(cudaMemcpyAsync(h->d_sigtr, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  to_box(h, siga, h->ng, box);
-  CK(cudaMemcpyAsync(h->d_siga, box.data(), box.size() * 8, cudaMemcpyHostToDevice, h->st));
-  // reset the device status, then Dsigr_updt + checks on the device
+// Dsigr_updt and check_xs on the device (mod_xsec.f90:90-168, :198-227) for
+// the node tables in place, then the derived copies (after_xs).
+static adp_status xs_finish(adp_handle* h) {
   h->h_ctl->status = 0;
   h->h_ctl->err_node = -1;
   CK(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice, h->st));
@@ -621,27 +673,50 @@ adp_status adp_xs_updt_nodes(adp_handle* h, int nmat, const double* sigtr, const
   return after_xs(h);
 }
 
+adp_status adp_xs_updt_nodes(adp_handle* h, int nmat, const double* sigtr, const double* siga, const double* nuf,
+                             const double* sigf, const double* chi, const int* mat, const double* sigs,
+                             const double* dc) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!sigtr || !siga) return fail(h, ADP_ERR_INPUT, "adp_xs_updt: null sigtr or siga");
+  Xfer X;
+  bool chi_neg = false;
+  adp_status s = upload_xs_common(h, nmat, nuf, sigf, chi, mat, sigs, dc, X, chi_neg);
+  if (s != ADP_OK) return s;
+  if ((s = put_nodes(h, X, sigtr, h->ng, 1, h->d_sigtr, h->NB, 0)) != ADP_OK) return s;
+  if ((s = put_nodes(h, X, siga, h->ng, 1, h->d_siga, h->NB, 0)) != ADP_OK) return s;
+  if ((s = xs_flags(h, X, chi_neg)) != ADP_OK) return s;
+  return xs_finish(h);
+}
+
+// base_updt (mod_xsec.f90:172-195) on the device: only the material tables
+// and numbers (and the ADFs) cross to the GPU.
 adp_status adp_xs_updt(adp_handle* h, int nmat, const double* xsigtr, const double* xsiga, const double* xnuf,
                        const double* xsigf, const double* chi, const int* mat, const double* xsigs, const double* dc) {
   if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
   if (!xsigtr || !xsiga || !xnuf || !xsigf || !xsigs || !mat || !chi)
     return fail(h, ADP_ERR_INPUT, "adp_xs_updt: null array");
-  // base_updt (mod_xsec.f90:172-195)
+  if (nmat < 1) return fail(h, ADP_ERR_INPUT, "adp_xs_updt: no materials");
   const int nn = h->nnod, G = h->ng;
-  std::vector<double> st((size_t)G * nn), sa(st.size()), nf(st.size()), sf(st.size()), ss((size_t)G * G * nn);
-  for (int n = 0; n < nn; ++n) {
-    const int m = mat[n] - 1;
-    if (m < 0 || m >= nmat) return fail(h, ADP_ERR_INPUT, "adp_xs_updt: material number out of range");
-    for (int g = 0; g < G; ++g) {
-      st[(size_t)g * nn + n] = xsigtr[(size_t)g * nmat + m];
-      sa[(size_t)g * nn + n] = xsiga[(size_t)g * nmat + m];
-      nf[(size_t)g * nn + n] = xnuf[(size_t)g * nmat + m];
-      sf[(size_t)g * nn + n] = xsigf[(size_t)g * nmat + m];
-      for (int hh = 0; hh < G; ++hh)
-        ss[((size_t)hh * G + g) * nn + n] = xsigs[((size_t)hh * G + g) * nmat + m];
-    }
-  }
-  return adp_xs_updt_nodes(h, nmat, st.data(), sa.data(), nf.data(), sf.data(), chi, mat, ss.data(), dc);
+  h->fwd_ok = false;
+  adp_status s = check_mat(h, nmat, mat);
+  if (s != ADP_OK) return s;
+  const bool chi_neg = chi_negative(h, nmat, chi);
+  Xfer X;
+  if ((s = xfer_reserve(h, nmat, X)) != ADP_OK) return s;
+  const size_t t1 = (size_t)G * nmat;
+  CK(cudaMemsetAsync(X.flags, 0, sizeof(int), h->st));
+  CK(cudaMemcpyAsync(X.mat, mat, (size_t)nn * 4, cudaMemcpyHostToDevice, h->st));
+  const double* src[5] = {xsigtr, xsiga, xnuf, xsigf, chi};
+  for (int k = 0; k < 5; ++k) CK(cudaMemcpyAsync(X.tab + k * t1, src[k], t1 * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(X.tab + 5 * t1, xsigs, t1 * G * 8, cudaMemcpyHostToDevice, h->st));
+  XsTables T{X.tab, X.tab + t1, X.tab + 2 * t1, X.tab + 3 * t1, X.tab + 4 * t1, X.tab + 5 * t1};
+  CK(launch_base_updt(T, X.mat, h->d_act, nn, nmat, G, h->NB, xs_box(h), X.flags, h->st));
+  if ((s = put_dc(h, X, dc)) != ADP_OK) return s;
+  h->nmat = nmat;
+  if ((s = xs_flags(h, X, chi_neg)) != ADP_OK) return s;
+  return xs_finish(h);
 }
 
 }  // extern "C"
@@ -892,29 +967,17 @@ adp_status adp_get_state(adp_handle* h, double* f0, double* fs0, double* keff, d
   CK(cudaSetDevice(h->dev));
   CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  const int cur = h->h_ctl->cur, nn = h->nnod, G = h->ng, NB = h->NB;
+  const int cur = h->h_ctl->cur, G = h->ng, NB = h->NB;
   if (keff) *keff = h->h_ctl->Ke;
-  std::vector<double> box;
-  if (f0) {
-    box.resize((size_t)G * h->NBH);
-    CK(cudaMemcpy(box.data(), h->d_phi[cur] - h->plane, box.size() * 8, cudaMemcpyDeviceToHost));
-    for (int g = 0; g < G; ++g)
-      for (int n = 0; n < nn; ++n) f0[(size_t)g * nn + n] = box[(size_t)g * h->NBH + h->plane + h->node2box[n]];
-  }
-  if (fs0) {
-    box.resize(NB);
-    CK(cudaMemcpy(box.data(), h->d_fs[cur], (size_t)NB * 8, cudaMemcpyDeviceToHost));
-    for (int n = 0; n < nn; ++n) fs0[n] = box[h->node2box[n]];
-  }
-  if (dn) {
-    box.resize((size_t)G * 6 * NB);
-    CK(cudaMemcpy(box.data(), h->d_dn, box.size() * 8, cudaMemcpyDeviceToHost));
-    // dn(nnod, ng, 6): face is the slowest index
-    for (int u = 0; u < 6; ++u)
-      for (int g = 0; g < G; ++g)
-        for (int n = 0; n < nn; ++n)
-          dn[((size_t)u * G + g) * nn + n] = box[((size_t)g * 6 + u) * NB + h->node2box[n]];
-  }
+  if (!f0 && !fs0 && !dn) return ADP_OK;
+  Xfer X;
+  adp_status s = xfer_reserve(h, h->nmat, X);
+  if (s != ADP_OK) return s;
+  // gathered on the device; one contiguous copy per array
+  if (f0 && (s = get_nodes(h, X, h->d_phi[cur], G, 1, h->NBH, f0)) != ADP_OK) return s;
+  if (fs0 && (s = get_nodes(h, X, h->d_fs[cur], 1, 1, NB, fs0)) != ADP_OK) return s;
+  // dn(nnod, ng, 6): face is the slowest index
+  if (dn && (s = get_nodes(h, X, h->d_dn, G, 6, NB, dn)) != ADP_OK) return s;
   return ADP_OK;
 }
 
@@ -985,13 +1048,13 @@ adp_status adp_power(adp_handle* h, double* p) {
   *h->h_ctl = c;
   CK(cudaMemcpyAsync(&h->d_ctl->status, &h->h_ctl->status, sizeof(int), cudaMemcpyHostToDevice, h->st));
   CK(launch_power(box_geom(h), h->ng, h->NBH, h->d_phi[c.cur], h->d_sigf, h->d_pbox, h->d_red, h->d_ctl, h->st));
-  std::vector<double> box(h->NB);
-  CK(cudaMemcpyAsync(box.data(), h->d_pbox, (size_t)h->NB * 8, cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   if (h->h_ctl->status) return ctl_error(h, *h->h_ctl);
-  for (int n = 0; n < h->nnod; ++n) p[n] = box[h->node2box[n]];
-  return ADP_OK;
+  Xfer X;
+  adp_status s = xfer_reserve(h, h->nmat, X);
+  if (s != ADP_OK) return s;
+  return get_nodes(h, X, h->d_pbox, 1, 1, h->NB, p);
 }
 
 // Device state of the discrete adjoint, allocated once per handle.
@@ -1123,10 +1186,10 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
   const int nn = h->nnod, G = h->ng;
   if (dkdp) CK(cudaMemcpy(dkdp, h->d_sens, (size_t)nn * G * (4 + G) * 8, cudaMemcpyDeviceToHost));
   if (psi) {
-    std::vector<double> box((size_t)G * h->NBH);
-    CK(cudaMemcpy(box.data(), h->d_psi[c.cur] - h->plane, box.size() * 8, cudaMemcpyDeviceToHost));
-    for (int g = 0; g < G; ++g)
-      for (int n = 0; n < nn; ++n) psi[(size_t)g * nn + n] = box[(size_t)g * h->NBH + h->plane + h->node2box[n]];
+    Xfer X;
+    adp_status s = xfer_reserve(h, h->nmat, X);
+    if (s != ADP_OK) return s;
+    return get_nodes(h, X, h->d_psi[c.cur], G, 1, h->NBH, psi);
   }
   return ADP_OK;
 }

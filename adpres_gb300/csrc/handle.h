@@ -76,6 +76,10 @@ struct adp_handle {
   long long* d_ndkey = nullptr;
   int* d_ndloc = nullptr;
   double* d_pbox = nullptr;
+  // device staging of the node-order transfers (one host array at a time,
+  // the material numbers and tables, check flags), allocated on first use
+  char* xfer_base = nullptr;
+  size_t xfer_size = 0;
   // output edits (adp_edit_*), allocated on first use
   char* edit_base = nullptr;
   size_t edit_size = 0;

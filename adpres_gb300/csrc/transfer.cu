@@ -1,0 +1,126 @@
+// Node-order transfers between the host's arrays and the device's box
+// layout.  The host hands over arrays in its own layout, a(nnod, A[, B])
+// with the node index fastest (the sdata arrays of the reference); they
+// cross PCIe/C2C as one contiguous copy each, and the node -> box scatter
+// (with the component transpose to the device's [A][B][NB] planes) runs
+// here, as do the sign checks of check_xs (mod_xsec.f90:90-168) and
+// base_updt (:172-195), which expands the material tables on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "adp_kernels.h"
+
+namespace adp {
+
+namespace {
+
+constexpr int kXferThreads = 256;
+
+int xfer_blocks(long long work) {
+  const long long b = (work + kXferThreads - 1) / kXferThreads;
+  return (int)std::max(1LL, std::min(b, 152LL * 16));
+}
+
+// dst[(i*B + j)*dstride + act[n]] = src[(j*A + i)*nn + n]; flags |= chk if a value < 0
+__global__ void k_nodes_to_box(const double* __restrict__ src, double* __restrict__ dst, const int* __restrict__ act,
+                               int nn, int A, int B, long long dstride, int chk, int* flags) {
+  const long long total = (long long)nn * A * B;
+  int bad = 0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(q % nn);
+    const int cs = (int)(q / nn);
+    const int i = cs % A, j = cs / A;
+    const double v = src[q];
+    bad |= v < 0.0;
+    dst[(long long)(i * B + j) * dstride + act[n]] = v;
+  }
+  if (chk && __syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flags, chk);
+}
+
+// dst[(j*A + i)*nn + n] = src[(i*B + j)*sstride + act[n]]
+__global__ void k_box_to_nodes(const double* __restrict__ src, double* __restrict__ dst, const int* __restrict__ act,
+                               int nn, int A, int B, long long sstride) {
+  const long long total = (long long)nn * A * B;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(q % nn);
+    const int cs = (int)(q / nn);
+    const int i = cs % A, j = cs / A;
+    dst[q] = src[(long long)(i * B + j) * sstride + act[n]];
+  }
+}
+
+// dst[c*dstride + act[n]] = v for every component c < ncomp
+__global__ void k_fill_box(double* __restrict__ dst, const int* __restrict__ act, int nn, int ncomp,
+                           long long dstride, double v) {
+  const long long total = (long long)nn * ncomp;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x)
+    dst[(q / nn) * dstride + act[q % nn]] = v;
+}
+
+// base_updt from material tables t(nmat, G) (Fortran) and sigs(nmat, G, G):
+// the node's chi always; the other tables where given (null: the node
+// tables of that quantity were uploaded instead).  flags |= 1 for a
+// negative nu*fission, 4 for a negative scattering entry of a node.
+__global__ void k_base_updt(XsTables T, const int* __restrict__ mat, const int* __restrict__ act, int nn, int nmat,
+                            int G, long long NB, XsBox X, int* flags) {
+  const long long total = (long long)nn * G;
+  int bad = 0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(q % nn), g = (int)(q / nn);
+    const int m = mat[n] - 1;
+    const long long b = (long long)g * NB + act[n];
+    const int t = g * nmat + m;
+    X.chin[b] = T.chi[t];
+    if (T.sigtr) X.sigtr[b] = T.sigtr[t];
+    if (T.siga) X.siga[b] = T.siga[t];
+    if (T.nuf) {
+      const double v = T.nuf[t];
+      bad |= v < 0.0 ? 1 : 0;
+      X.nuf[b] = v;
+    }
+    if (T.sigf) X.sigf[b] = T.sigf[t];
+    if (T.sigs)
+      for (int h = 0; h < G; ++h) {
+        const double v = T.sigs[m + (long long)nmat * (g + (long long)G * h)];
+        bad |= v < 0.0 ? 4 : 0;
+        X.sigs[((long long)g * G + h) * NB + act[n]] = v;
+      }
+  }
+  const int nuf_bad = __syncthreads_or(bad & 1);
+  const int sigs_bad = __syncthreads_or(bad & 4);
+  if (threadIdx.x == 0 && (nuf_bad || sigs_bad)) atomicOr(flags, (nuf_bad ? 1 : 0) | (sigs_bad ? 4 : 0));
+}
+
+}  // namespace
+
+cudaError_t launch_nodes_to_box(const double* src, double* dst, const int* act, int nn, int A, int B,
+                                long long dstride, int chk, int* flags, cudaStream_t st) {
+  k_nodes_to_box<<<xfer_blocks((long long)nn * A * B), kXferThreads, 0, st>>>(src, dst, act, nn, A, B, dstride, chk,
+                                                                              flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_box_to_nodes(const double* src, double* dst, const int* act, int nn, int A, int B,
+                                long long sstride, cudaStream_t st) {
+  k_box_to_nodes<<<xfer_blocks((long long)nn * A * B), kXferThreads, 0, st>>>(src, dst, act, nn, A, B, sstride);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_box(double* dst, const int* act, int nn, int ncomp, long long dstride, double v,
+                            cudaStream_t st) {
+  k_fill_box<<<xfer_blocks((long long)nn * ncomp), kXferThreads, 0, st>>>(dst, act, nn, ncomp, dstride, v);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_base_updt(const XsTables& T, const int* mat, const int* act, int nn, int nmat, int G, long long NB,
+                             const XsBox& X, int* flags, cudaStream_t st) {
+  k_base_updt<<<xfer_blocks((long long)nn * G), kXferThreads, 0, st>>>(T, mat, act, nn, nmat, G, NB, X, flags);
+  return cudaGetLastError();
+}
+
+}  // namespace adp

@@ -22,7 +22,7 @@ from ._lib import ADP_ERR_INPUT, ADP_ERR_BADXS, ADP_ERR_UNSUPPORTED
 
 KNOWN_CARDS = ("MODE", "XSEC", "GEOM", "CASE", "ESRC", "ITER", "PRNT", "ADF", "CROD", "EJCT", "CBCS",
                "FTEM", "MTEM", "CDEN", "BCON", "THER", "XTAB", "KERN", "EXTR", "THET")
-OUT_OF_SCOPE = ("ESRC", "CROD", "EJCT", "CBCS", "FTEM", "MTEM", "CDEN", "BCON", "THER", "XTAB", "EXTR", "THET")
+OUT_OF_SCOPE = ("ESRC", "EJCT", "THER", "XTAB", "EXTR", "THET")
 
 F_1EM5 = float(np.float32(1.e-5))   # default serc/ferc (mod_data.f90:78-79)
 
@@ -68,6 +68,12 @@ class Deck:
     nac: int = 5
     nupd: int = 0
     prnt: tuple = (1, 1, 1)
+    coreh: float = 0.0                 # core height, the sum of zdel
+    # feedback cards: "bcon", "ftem", "mtem", "cden" -> dict(value, ref,
+    # changes); "crod" -> dict(nb, nstep, pos0, ssize, bpos, fbmap, changes);
+    # changes = sigtr, siga, nuf, sigf (nmat, ng) and sigs (nmat, ng, ng)
+    feedback: dict = field(default_factory=dict)
+    bcbcs: bool = False                # %CBCS given (critical boron search)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -192,8 +198,8 @@ def parse(text: str, basedir: str = ".") -> Deck:
     if "MODE" not in cards or not cards["MODE"]:
         raise DeckError(ADP_ERR_INPUT, "card %MODE does not present. this card is mandatory")
     dk.mode = cards["MODE"][0][1].strip().upper()
-    if dk.mode not in ("FORWARD", "ADJOINT"):
-        if dk.mode in ("FIXEDSRC", "RODEJECT", "BCSEARCH"):
+    if dk.mode not in ("FORWARD", "ADJOINT", "BCSEARCH"):
+        if dk.mode in ("FIXEDSRC", "RODEJECT"):
             raise DeckError(ADP_ERR_UNSUPPORTED, f"mode {dk.mode} is outside the static k-eigenvalue path")
         raise DeckError(ADP_ERR_INPUT, f"mode {dk.mode} is unidentified")
     if "KERN" in cards:
@@ -212,6 +218,27 @@ def parse(text: str, basedir: str = ".") -> Deck:
         r = _Card("PRNT", cards["PRNT"]).rec()
         dk.prnt = tuple(r.ints(3))
     _misc(dk, mnum)
+    dk.coreh = 0.0
+    for z in dk.zdel:
+        dk.coreh = dk.coreh + float(z)
+    dk.feedback = {}
+    if "CROD" in cards:
+        _crod(dk, cards["CROD"])
+    if "CBCS" in cards:
+        dk.feedback["bcon"] = _state_card(dk, "CBCS", cards["CBCS"], has_value=False)
+        dk.bcbcs = True
+    elif "BCON" in cards:
+        dk.feedback["bcon"] = _state_card(dk, "BCON", cards["BCON"], has_value=True)
+    for nm in ("FTEM", "MTEM", "CDEN"):
+        if nm in cards:
+            dk.feedback[nm.lower()] = _state_card(dk, nm, cards[nm], has_value=True)
+    # card checks of mode BCSEARCH (mod_io.f90:196-214)
+    if dk.mode == "BCSEARCH" and not dk.bcbcs:
+        raise DeckError(ADP_ERR_INPUT, "mode BCSEARCH needs card %CBCS")
+    if dk.mode != "BCSEARCH" and dk.bcbcs:
+        raise DeckError(ADP_ERR_INPUT, "card %CBCS is not necessary for this calculation mode")
+    if dk.mode == "BCSEARCH" and "BCON" in cards:
+        raise DeckError(ADP_ERR_INPUT, "card %BCON must not present for this calculation mode")
     if "ITER" in cards:
         r = _Card("ITER", cards["ITER"]).rec()
         dk.nout, dk.nin = r.i(), r.i()
@@ -224,6 +251,62 @@ def parse(text: str, basedir: str = ".") -> Deck:
     if "ADF" in cards:
         _adf(dk, cards["ADF"], mnum, pasm, zpln)
     return dk
+
+
+def _changes(dk, c):
+    """nmat x ng records: changes of sigtr, siga, nuf, sigf and sigs(g, 1..ng)."""
+    ng, nm = dk.ng, dk.nmat
+    ch = {k: np.zeros((nm, ng)) for k in ("sigtr", "siga", "nuf", "sigf")}
+    ch["sigs"] = np.zeros((nm, ng, ng))
+    for i in range(nm):
+        for g in range(ng):
+            v = c.rec().reals(4 + ng)
+            ch["sigtr"][i, g], ch["siga"][i, g], ch["nuf"][i, g], ch["sigf"][i, g] = v[:4]
+            ch["sigs"][i, g, :] = v[4:]
+    return ch
+
+
+def _state_card(dk, name, lines, has_value):
+    """%CBCS (reference only), %BCON, %FTEM, %MTEM, %CDEN (value and reference),
+    then the per-material changes (mod_io.f90:2486-2954)."""
+    c = _Card(name, lines)
+    r = c.rec()
+    if has_value:
+        val, ref = r.d(), r.d()
+    else:
+        ref = r.d()
+        val = ref
+    return dict(value=val, ref=ref, changes=_changes(dk, c))
+
+
+def _crod(dk, lines):
+    """%CROD (mod_io.f90:2148-2328): banks, steps, zero position and step size,
+    bank positions, the assembly bank map (north row first) and the changes of
+    a fully rodded node."""
+    c = _Card("CROD", lines)
+    r = c.rec()
+    nb, nstep = r.i(), r.i()
+    r = c.rec()
+    pos0, ssize = r.d(), r.d()
+    r = c.rec()
+    bpos = r.reals(nb)
+    for b in bpos:
+        if b > float(np.float32(nstep)):
+            r.fail("control rod bank position is larger than the number of steps")
+        if b < 0.0:
+            r.fail("control rod bank position is negative")
+        if dk.coreh < b * ssize:
+            r.fail("core height is lower than the control rod position")
+    bmap = np.zeros((dk.nx, dk.ny), dtype=np.int64)
+    for j in range(dk.ny - 1, -1, -1):
+        rr = c.rec()
+        bmap[:, j] = rr.ints(dk.nx)
+        if (bmap[:, j] > nb).any():
+            rr.fail("control rod bank number is larger than the number of banks")
+    xdiv, ydiv = dk.extra["xdiv"], dk.extra["ydiv"]
+    fbmap = np.repeat(np.repeat(bmap, xdiv, axis=0), ydiv, axis=1)   # (nxx, nyy)
+    dk.feedback["crod"] = dict(nb=nb, nstep=nstep, pos0=pos0, ssize=ssize, bpos=np.array(bpos), fbmap=fbmap,
+                               changes=_changes(dk, c))
 
 
 def load(path: str) -> Deck:

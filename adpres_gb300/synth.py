@@ -17,6 +17,9 @@ and the CPU oracle.
                    axial size (10..40 nodes) and a cylindrical outline (fuel
                    inside, one reflector ring), cross sections perturbed by
                    1% lognormal factors per material value.
+  boron_search_3d  the full-core geometry in mode BCSEARCH with boron, fuel
+                   and moderator temperature, coolant density and two
+                   control-rod banks as feedback cards.
   small_core       a small ragged core with optional ADFs, any boundary
                    conditions and 1-4 groups (parity tests).
 
@@ -236,6 +239,72 @@ def batch_member(seed, index, zref=True, zsize=10.0, nupd=100):
         zpln[0] = zpln[-1] = 2
     return _deck(f"BATCH{index}", 2, mats, nx, nx, nzn, size, div, size, div, [zsize] * nzn, [1] * nzn,
                  planars, zpln, (1, 1, 1, 1, 1, 1), iter_=it)
+
+
+def _changes2(rows):
+    """Feedback-card records of 2-group materials: per material two rows
+    sigtr siga nuf sigf sigs(g->1) sigs(g->2)."""
+    return [" ".join(_fmt(v) for v in row) for mat in rows for row in mat]
+
+
+def boron_search_3d(seed=0, n=17, planes=20, rbcon=1000.0):
+    """Critical boron search on a 3D full core (mode BCSEARCH).
+
+    n x n assemblies of 2x2 nodes (fuel inside a circle of radius 0.42 n,
+    reflector outside), `planes` fuel layers of 20 cm between reflector
+    layers, 3 fuel types, 2 groups, SANM.  Cross sections are given at the
+    reference boron concentration rbcon; the feedback cards carry boron
+    worth (about 9 pcm/ppm), fuel and moderator temperatures and coolant
+    density away from their references, and two control-rod banks of four
+    assemblies each, at 120 and 200 of 228 steps over the fuel height (tips
+    inside nodes, so the volume-weighted rodded nodes are exercised)."""
+    rng = np.random.default_rng(2000 + seed)
+    fuels = [_fuel2(rng) for _ in range(3)]
+
+    def borated(f):   # the tables hold rbcon's absorption on top of the unborated values
+        g = dict(f)
+        g["sa"] = [f["sa"][0] + rbcon * 1.9e-7, f["sa"][1] + rbcon * 1.03e-5]
+        return g
+
+    mats = [_mat2(**borated(REFL2))] + [_mat2(**borated(f)) for f in fuels]
+    fuel = _circle_outline(n, 0.42 * n)
+    types = rng.integers(0, 3, size=(n, n))
+    fuel_pos = np.argwhere(fuel)
+    rods = fuel_pos[rng.choice(len(fuel_pos), size=8, replace=False)]
+    refl = np.ones((n, n), dtype=int)
+    unrod = np.where(fuel, 2 + types, 1)
+    nz = planes + 2
+    zpln = [1] + [2] * planes + [1]
+    nxx = nyy = 2 * n
+    it = [3000, 2, "1.0e-5", "1.0e-5", 5, _nupd(nxx, nyy, nz), 30, 20]
+    text = _deck("BCSEARCH3D", 2, mats, n, n, nz, [20.0] * n, [2] * n, [20.0] * n, [2] * n, [20.0] * nz, [1] * nz,
+                 [refl, unrod], zpln, (1, 1, 1, 1, 1, 1), iter_=it, mode="BCSEARCH")
+    nm = len(mats)
+    # control rods: banks 1 and 2, map written north row first
+    bank = np.zeros((n, n), dtype=int)
+    bank[rods[:4, 0], rods[:4, 1]] = 1
+    bank[rods[4:, 0], rods[4:, 1]] = 2
+    rod = [[3.7e-3, 2.5e-3, -1.0e-4, -1.0e-4 / NU, 0.0, -3.2e-3],
+           [-2.2e-2, 2.56e-2, -2.8e-3, -2.8e-3 / NU, 0.0, 0.0]]
+    # 228 steps span the fuel height; bank 1 at step 120, bank 2 at 200
+    L = ["%CROD", "2 228", "20.0 " + _fmt(20.0 * planes / 228.0), "120.0 200.0"]
+    for j in range(n - 1, -1, -1):
+        L.append(" ".join(str(int(bank[i, j])) for i in range(n)))
+    L += _changes2([rod] * nm)
+    # boron, per ppm (water in every material)
+    bor = [[6.1e-8, 1.9e-7, 0.0, 0.0, 0.0, 7.9e-10], [5.2e-6, 1.03e-5, 0.0, 0.0, 0.0, 0.0]]
+    L += ["%CBCS", _fmt(rbcon)] + _changes2([bor] * nm)
+    zero = [[0.0] * 6, [0.0] * 6]
+    # fuel temperature, per sqrt(K): Doppler absorption in the fast group
+    ftem = [[0.0, 3.0e-5, 0.0, 0.0, 0.0, 0.0], [0.0, 5.0e-6, -5.0e-6, -5.0e-6 / NU, 0.0, 0.0]]
+    L += ["%FTEM", "950.0 900.0"] + _changes2([zero] + [ftem] * (nm - 1))
+    # moderator temperature, per K
+    mtem = [[-6.0e-5, -3.0e-5, -4.0e-5, -4.0e-5 / NU, 0.0, -1.0e-5], [-5.0e-4, -2.0e-4, -3.0e-4, -3.0e-4 / NU, 0.0, 0.0]]
+    L += ["%MTEM", "580.0 575.0"] + _changes2([zero] + [mtem] * (nm - 1))
+    # coolant density, per g/cm3
+    cden = [[7.5e-2, 2.1e-4, 0.0, 0.0, 0.0, 3.7e-2], [5.3e-1, 7.6e-3, 0.0, 0.0, 0.0, 0.0]]
+    L += ["%CDEN", "0.72 0.71"] + _changes2([cden] * nm)
+    return text + "\n".join(L) + "\n"
 
 
 def small_core(seed=0, ng=2, kern="SANM", nx=4, ny=4, nz=3, xdiv=2, ydiv=2, zdiv=1, ragged=True, adf=False,

@@ -178,6 +178,61 @@ def adjoint_leg(flush, steps=3):
     return out
 
 
+# ------------------------------------------- critical boron search leg ----
+def _cbsearch_oracle(text):
+    import oracle
+    o = oracle.Oracle(text=text)
+    t0 = time.perf_counter()
+    it = o.cbsearch()
+    return time.perf_counter() - t0, it
+
+
+def cbsearch_leg(flush, steps=3):
+    """th::cbsearch on the 34x34x22-node full core with boron, temperature,
+    density and control-rod feedback cards (seed 0): each search step is the
+    host cross-section update at the iterate, the upload of the node tables
+    and a warm-started outer on the GPU.  Timed end to end (wall clock,
+    synchronised); device_ms sums the outer calls.  CPU baseline: the
+    oracle's whole search on one host core."""
+    import multiprocessing as mp
+
+    import torch
+
+    from adpres_gb300 import deck, synth
+    from adpres_gb300.core import Core
+    from adpres_gb300.feedback import cbsearch
+
+    text = synth.boron_search_3d(0)
+    dk = deck.parse(text)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        t_cpu, it_cpu = pool.apply(_cbsearch_oracle, (text,))
+    out = {"workload": "boron_search_3d seed 0: 34x34 radial nodes x 22 planes, 2 groups, SANM, boron, fuel and "
+                       "moderator temperature, coolant density and 2 rod banks",
+           "nodes": int(dk.nnod), "oracle": {"iterates": len(it_cpu), "bcon": it_cpu[-1][0], "keff": it_cpu[-1][1],
+                                             "outers": int(sum(r[2] for r in it_cpu))}}
+    for prec in ("fp64", "mixed"):
+        c = Core.from_deck(dk, precision=prec)
+        cbsearch(c, dk)
+        walls, devs = [], []
+        for _ in range(steps):
+            c.reset()
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            it = cbsearch(c, dk)
+            torch.cuda.synchronize()
+            walls.append(time.perf_counter() - t0)
+            devs.append(c.cbsearch_device_ms)
+        out[prec] = {"searches_per_s": steps / sum(walls), "ms_per_search": sum(walls) / steps * 1e3,
+                     "device_ms": sum(devs) / steps, "iterates": len(it), "bcon": it[-1][0], "keff": it[-1][1],
+                     "outers": int(sum(r[2] for r in it)), "dbcon_ppm_vs_oracle": abs(it[-1][0] - it_cpu[-1][0])}
+        c.close()
+    out["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "searches/s", "cores": 1, "kind": "port",
+                           "sample": f"the oracle's whole search on this core ({t_cpu:.2f} s)"}
+    return out
+
+
 # ------------------------------------------------- batched solves leg ----
 def _batch_oracle_member(args):
     seed, i = args
@@ -367,20 +422,34 @@ def run_ours(args):
     core64.close()
 
     adjoint = adjoint_leg(flush)
+    boron = cbsearch_leg(flush)
     batched = batch_leg(flush) if not args.no_batch else None
 
-    # e2e through the C ABI from host buffers
+    # e2e through the C ABI from host buffers: the inputs sit in pinned host
+    # memory in the reference's column-major layouts (set up before timing)
     e2e_steps = max(2, min(args.steps, 5))
-    h2d = (dk.ng * 5 + dk.ng * dk.ng + 6 * dk.ng) * dk.nnod * 8 + dk.nnod * 4
+    keep = []
+
+    def pinned(a, dt=np.float64):
+        flat = np.asfortranarray(a, dtype=dt).reshape(-1, order="F")
+        t = torch.empty(flat.size, dtype=torch.float64 if dt == np.float64 else torch.int32, pin_memory=True)
+        v = t.numpy()
+        v[:] = flat
+        keep.append(t)
+        return v.reshape(np.shape(a), order="F")
+
+    xin = [pinned(a) for a in (dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi)]
+    mat_p, sigs_p, dc_p = pinned(dk.mat, np.int32), pinned(dk.xsigs), pinned(dk.dc)
+    h2d = sum(a.nbytes for a in xin) + mat_p.nbytes + sigs_p.nbytes + dc_p.nbytes
     d2h = dk.nnod * 8 + dk.nnod * dk.ng * 8
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        core.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
+        core.xs_updt(*xin, mat_p, sigs_p, dc_p)
         core.reset()
         core.outer(adjoint=False, popt=1, trace=False)
         core.power()
-        core.state()
+        core.flux()
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * e2e_steps / e2e_s
@@ -408,6 +477,7 @@ def run_ours(args):
                      "launches": launches},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "adjoint": adjoint,
+        "cbsearch": boron,
         "batched": batched,
         "gpu_launches": gpu_launches,
         "clocks": ck,

@@ -277,7 +277,9 @@ typedef struct adp_batch adp_batch;
 /* Launch shape and schedule: threads per block (256 or 512), the largest
  * team of blocks on one core, grain (cores are split into teams so that a
  * team member's share is about 1/grain of a block's average load),
- * blocks per SM, and whether the solve is replayed from a captured graph. */
+ * blocks per SM (2 with 256 threads selects the kernel built for two
+ * resident blocks per SM, 128 registers a thread), and whether the solve is
+ * replayed from a captured graph. */
 typedef struct adp_batch_config {
   int threads;
   int max_team;
@@ -307,9 +309,10 @@ adp_status adp_batch_get_config(const adp_batch* b, adp_batch_config* c);
  * device_ms is the whole launch (CUDA events).  Returns the first failing
  * core's status, or ADP_OK. */
 adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_ms);
-/* Time the batch over block size {256, 512} x max_team {2, 8, 32} x grain
- * {1, 4} (schedules built from the measured per-core times of one solve)
- * and keep the fastest: 13 solves of the whole batch. */
+/* Time the batch over the kernel shapes (threads, blocks per SM) = (256, 1),
+ * (256, 2), (512, 1) x max_team {2, 8, 32} x grain {1, 4} (schedules built
+ * from the measured per-core times of one solve) and keep the fastest:
+ * 19 solves of the whole batch. */
 adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best, double* best_ms);
 adp_status adp_batch_core(adp_batch* b, int i, adp_handle** h);
 /* Per-outer trace of core i from the last adp_batch_solve (as the trace of

@@ -69,6 +69,18 @@ module adpres_gb300_bind
       integer(c_int), intent(in) :: mat(*)
     end function
 
+    ! node tables sigtr/siga/nuf/sigf(nnod, ng), sigs(nnod, ng, ng): the
+    ! host's XS_updt with its feedback updates (mod_xsec.f90:11-46) hands
+    ! its results over here before each outer (th::cbsearch, mod_th.f90:752)
+    integer(c_int) function adp_xs_updt_nodes(h, nmat, sigtr, siga, nuf, sigf, chi, mat, sigs, dc) &
+        bind(C, name="adp_xs_updt_nodes")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: nmat
+      real(c_double), intent(in) :: sigtr(*), siga(*), nuf(*), sigf(*), chi(*), sigs(*), dc(*)
+      integer(c_int), intent(in) :: mat(*)
+    end function
+
     integer(c_int) function adp_set_xs(h, nmat, D, sigr, nuf, sigf, chi, mat, sigs, dc) bind(C, name="adp_set_xs")
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: h
@@ -114,6 +126,54 @@ module adpres_gb300_bind
       real(c_double), value :: tol
       real(c_double), intent(out) :: dkdp(*), psi(*)
       type(adp_report), intent(inout) :: rep
+    end function
+
+    ! output edits of control::forward (mod_io.f90:3267-3644)
+    integer(c_int) function adp_edit_asmpow(h, nx, ny, xdiv, ydiv, fasm, imax, jmax) bind(C, name="adp_edit_asmpow")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: nx, ny
+      integer(c_int), intent(in) :: xdiv(*), ydiv(*)
+      real(c_double), intent(out) :: fasm(*)
+      integer(c_int), intent(out) :: imax, jmax
+    end function
+
+    integer(c_int) function adp_edit_axipow(h, nz, zdiv, faxi, kmax) bind(C, name="adp_edit_axipow")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: nz
+      integer(c_int), intent(in) :: zdiv(*)
+      real(c_double), intent(out) :: faxi(*)
+      integer(c_int), intent(out) :: kmax
+    end function
+
+    integer(c_int) function adp_edit_asmflux(h, nx, ny, xdiv, ydiv, norm, fasm, negative) &
+        bind(C, name="adp_edit_asmflux")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      integer(c_int), value :: nx, ny
+      integer(c_int), intent(in) :: xdiv(*), ydiv(*)
+      real(c_double), value :: norm
+      real(c_double), intent(out) :: fasm(*)
+      integer(c_int), intent(out) :: negative
+    end function
+
+    ! adjoint-weighted edits (mod_trans.f90:648-746); sigrp may be c_null_ptr
+    integer(c_int) function adp_reactivity(h, af, sigrp, rho) bind(C, name="adp_reactivity")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: af(*)
+      type(c_ptr), value :: sigrp
+      real(c_double), intent(out) :: rho
+    end function
+
+    integer(c_int) function adp_core_beta(h, af, nmat, nf, ibeta, mat, beta) bind(C, name="adp_core_beta")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: af(*), ibeta(*)
+      integer(c_int), value :: nmat, nf
+      integer(c_int), intent(in) :: mat(*)
+      real(c_double), intent(out) :: beta
     end function
   end interface
 

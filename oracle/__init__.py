@@ -107,6 +107,8 @@ def lib(variant: str = "plain"):
         L.ora_reset.argtypes = [vp]
         L.ora_asmpow.argtypes = [vp, dp, dp, ipp, ipp]
         L.ora_reactivity.argtypes = [vp, dp, dp, dp]
+        L.ora_cbsearch.argtypes = [vp, dp, dp, ipp, ip, ipp]
+        L.ora_xs_updt_at.argtypes = [vp, ctypes.c_double]
         L.ora_calc_beta.argtypes = [vp, dp, ip, dp, dp]
         L.ora_axipow.argtypes = [vp, dp, dp, ipp]
         L.ora_asmflux.argtypes = [vp, dp, ctypes.c_double, dp, ipp]
@@ -178,9 +180,25 @@ class Oracle:
         self._check(self.L.ora_outer(self.h, int(adjoint), popt, max_outers))
 
     def run(self):
-        """control::forward / control::adjoint (mod_control.f90:11-86)."""
+        """control::forward / control::adjoint (mod_control.f90:11-86), or
+        th::cbsearch (mod_th.f90:752-837) in mode BCSEARCH."""
+        if self.geti("bcsearch"):
+            return self.cbsearch()
         self.xs_updt()
         self.outer(adjoint=bool(self.geti("adjoint")), popt=1)
+
+    def cbsearch(self, cap=64):
+        """Critical boron search: list of (bcon, k, outers) iterates; the last is critical."""
+        bc, k = np.zeros(cap), np.zeros(cap)
+        no = np.zeros(cap, dtype=np.int32)
+        n = ctypes.c_int()
+        self._check(self.L.ora_cbsearch(self.h, _dp(bc), _dp(k), _ip(no), cap, ctypes.byref(n)))
+        m = min(n.value, cap)
+        return [(float(bc[i]), float(k[i]), int(no[i])) for i in range(m)]
+
+    def xs_updt_at(self, bcon):
+        """XS_updt with the boron concentration bcon (feedback cards applied)."""
+        self._check(self.L.ora_xs_updt_at(self.h, float(bcon)))
 
     def powdis(self):
         p = np.zeros(self.geti("nnod"))

@@ -86,6 +86,20 @@ struct Ora {
   int nin = 2, nout = 500, nac = 5, th_niter = 30, nth = 20, nupd = 0;
   int aprad = 1, apaxi = 1, afrad = 1;
   bool badf = false;
+  // cross-section feedback cards (mod_io.f90:2148-2954): per-material changes
+  // (nmat,ng[,ng]) per unit of a state variable
+  struct Feedback {
+    bool on = false;
+    double ref = 0.0, val = 0.0;                        // reference and current value
+    std::vector<double> str, sa, nf, sf, ss;            // sigtr siga nuf sigf sigs changes
+  };
+  Feedback fb_bcon, fb_ftem, fb_mtem, fb_cden, fb_crod;  // fb_crod.ss etc.: per fully rodded node
+  bool bcbcs = false;                                   // %CBCS (critical boron search) rather than %BCON
+  int nb = 0, nstep = 0;
+  double pos0 = 0.0, ssize = 0.0, coreh = 0.0;
+  std::vector<double> bpos;                             // (nb) bank positions in steps
+  std::vector<int> fbmap;                               // (nxx,nyy) bank of each node column, 0 none
+  double bcon = 0.0;                                    // %BCON concentration (forward mode)
   std::vector<double> dc;               // (nnod,ng,6)
   std::vector<double> exsrc;            // (nnod,ng)
   // node XS
@@ -560,20 +574,94 @@ static void read_adf(Ora& o, std::vector<Line>* L) {
   }
 }
 
+// Per-material changes of sigtr, siga, nuf, sigf and sigs(g,1..ng): nmat x ng
+// records as inp_crod/inp_cbcs/inp_bcon/inp_ftem/inp_mtem/inp_cden read them.
+static void read_changes(Ora& o, CardReader& cr, Ora::Feedback& f) {
+  const size_t mg = (size_t)o.nmat * o.ng;
+  f.str.assign(mg, 0); f.sa = f.nf = f.sf = f.str;
+  f.ss.assign(mg * o.ng, 0);
+  for (int i = 1; i <= o.nmat; ++i)
+    for (int g = 1; g <= o.ng; ++g) {
+      Rec x = cr.rec();
+      o.M2(f.str, i, g) = x.getd();
+      o.M2(f.sa, i, g) = x.getd();
+      o.M2(f.nf, i, g) = x.getd();
+      o.M2(f.sf, i, g) = x.getd();
+      for (int h = 1; h <= o.ng; ++h) o.M3(f.ss, i, g, h) = x.getd();
+    }
+  f.on = true;
+}
+
+// inp_crod (mod_io.f90:2148-2328)
+static void read_crod(Ora& o, std::vector<Line>* L) {
+  CardReader cr(L, "CROD");
+  Rec a = cr.rec();
+  o.nb = a.geti();
+  o.nstep = a.geti();
+  Rec b = cr.rec();
+  o.pos0 = b.getd();
+  o.ssize = b.getd();
+  Rec c = cr.rec();
+  o.bpos.assign(o.nb, 0.0);
+  for (int i = 0; i < o.nb; ++i) o.bpos[i] = c.getd();
+  for (int i = 0; i < o.nb; ++i) {
+    if (o.bpos[i] > (double)(float)o.nstep) c.fail("control rod bank position is larger than the number of steps");
+    if (o.bpos[i] < 0.) c.fail("control rod bank position is negative");
+    if (o.coreh < o.bpos[i] * o.ssize) c.fail("core height is lower than the control rod position");
+  }
+  std::vector<int> bmap((size_t)o.nx * o.ny);
+  for (int j = o.ny; j >= 1; --j) {
+    Rec r = cr.rec();
+    for (int i = 1; i <= o.nx; ++i) {
+      const int v = r.geti();
+      if (v > o.nb) r.fail("control rod bank number is larger than the number of banks");
+      bmap[(i - 1) + (size_t)o.nx * (j - 1)] = v;
+    }
+  }
+  o.fbmap.assign((size_t)o.nxx * o.nyy, 0);
+  int ytot = 0;
+  for (int j = 1; j <= o.ny; ++j)
+    for (int ly = 1; ly <= o.ydiv[j - 1]; ++ly) {
+      ++ytot;
+      int xtot = 0;
+      for (int i = 1; i <= o.nx; ++i)
+        for (int lx = 1; lx <= o.xdiv[i - 1]; ++lx) {
+          ++xtot;
+          o.fbmap[(xtot - 1) + (size_t)o.nxx * (ytot - 1)] = bmap[(i - 1) + (size_t)o.nx * (j - 1)];
+        }
+    }
+  read_changes(o, cr, o.fb_crod);
+}
+
+// inp_cbcs (mod_io.f90:2486-2571) / inp_bcon (:2575-2662) / inp_ftem, inp_mtem,
+// inp_cden (:2666-2954): the state value (and reference) then the changes
+static void read_state_card(Ora& o, std::vector<Line>* L, const char* name, Ora::Feedback& f, bool has_value) {
+  CardReader cr(L, name);
+  Rec a = cr.rec();
+  if (has_value) {
+    f.val = a.getd();
+    f.ref = a.getd();
+  } else {
+    f.ref = a.getd();
+    f.val = f.ref;
+  }
+  read_changes(o, cr, f);
+}
+
 static void parse_deck(Ora& o, const std::string& text, const std::string& basedir) {
   std::vector<Line> buf;
   strip_comments(text, buf);
   Cards cards;
   split_cards(buf, basedir, cards);
-  static const char* oos[] = {"ESRC", "CROD", "EJCT", "CBCS", "FTEM", "MTEM", "CDEN", "BCON", "THER", "XTAB", "EXTR", "THET"};
+  static const char* oos[] = {"ESRC", "EJCT", "THER", "XTAB", "EXTR", "THET"};
   for (auto& c : cards.cards)
     for (auto k : oos)
       if (c.first == k) throw OraError(ORA_ERR_UNSUPPORTED, "card %" + c.first + " is outside the static k-eigenvalue path");
   auto* m = cards.find("MODE");
   if (!m || m->empty()) throw OraError(ORA_ERR_INPUT, "card %MODE does not present. this card is mandatory");
   o.mode = upper(trim((*m)[0].text));
-  if (o.mode != "FORWARD" && o.mode != "ADJOINT") {
-    if (o.mode == "FIXEDSRC" || o.mode == "RODEJECT" || o.mode == "BCSEARCH")
+  if (o.mode != "FORWARD" && o.mode != "ADJOINT" && o.mode != "BCSEARCH") {
+    if (o.mode == "FIXEDSRC" || o.mode == "RODEJECT")
       throw OraError(ORA_ERR_UNSUPPORTED, "mode " + o.mode + " is outside the static k-eigenvalue path");
     throw OraError(ORA_ERR_INPUT, "mode " + o.mode + " is unidentified");
   }
@@ -590,6 +678,21 @@ static void parse_deck(Ora& o, const std::string& text, const std::string& based
     o.aprad = r.geti(); o.apaxi = r.geti(); o.afrad = r.geti();
   }
   misc(o);
+  o.coreh = 0.0;
+  for (int k = 0; k < o.nzz; ++k) o.coreh = o.coreh + o.zdel[k];
+  if (auto* c = cards.find("CROD")) read_crod(o, c);
+  if (auto* c = cards.find("CBCS")) { read_state_card(o, c, "CBCS", o.fb_bcon, false); o.bcbcs = true; }
+  else if (auto* c = cards.find("BCON")) { read_state_card(o, c, "BCON", o.fb_bcon, true); o.bcon = o.fb_bcon.val; }
+  if (auto* c = cards.find("FTEM")) read_state_card(o, c, "FTEM", o.fb_ftem, true);
+  if (auto* c = cards.find("MTEM")) read_state_card(o, c, "MTEM", o.fb_mtem, true);
+  if (auto* c = cards.find("CDEN")) read_state_card(o, c, "CDEN", o.fb_cden, true);
+  // card checks of mode BCSEARCH (mod_io.f90:196-214)
+  if (o.mode == "BCSEARCH" && !o.bcbcs)
+    throw OraError(ORA_ERR_INPUT, "mode BCSEARCH needs card %CBCS");
+  if (o.mode != "BCSEARCH" && o.bcbcs)
+    throw OraError(ORA_ERR_INPUT, "card %CBCS is not necessary for this calculation mode");
+  if (o.mode == "BCSEARCH" && cards.find("BCON"))
+    throw OraError(ORA_ERR_INPUT, "card %BCON must not present for this calculation mode");
   if (auto* it = cards.find("ITER")) read_iter(o, it);
   o.dc.assign((size_t)o.nnod * o.ng * 6, 1.0);
   if (auto* a = cards.find("ADF")) { o.badf = true; read_adf(o, a); }
@@ -642,12 +745,96 @@ static void check_xs(Ora& o) {
   }
 }
 
-// XS_updt (mod_xsec.f90:11-46), static path: base + D/sigr + checks
-static void xs_updt(Ora& o) {
+// bcon_updt / ftem_updt / mtem_updt / cden_updt (mod_xsec.f90:394-521):
+// node XS += change(mat) * dv, dv the state's difference from its reference
+// (sqrt(T) - sqrt(Tref) for the fuel temperature)
+static void state_updt(Ora& o, const Ora::Feedback& f, double dv) {
+  for (int n = 1; n <= o.nnod; ++n) {
+    const int m = o.mat[n - 1];
+    for (int g = 1; g <= o.ng; ++g) {
+      o.N2(o.sigtr, n, g) = o.N2(o.sigtr, n, g) + o.M2(const_cast<std::vector<double>&>(f.str), m, g) * dv;
+      o.N2(o.siga, n, g) = o.N2(o.siga, n, g) + o.M2(const_cast<std::vector<double>&>(f.sa), m, g) * dv;
+      o.N2(o.nuf, n, g) = o.N2(o.nuf, n, g) + o.M2(const_cast<std::vector<double>&>(f.nf), m, g) * dv;
+      o.N2(o.sigf, n, g) = o.N2(o.sigf, n, g) + o.M2(const_cast<std::vector<double>&>(f.sf), m, g) * dv;
+      for (int h = 1; h <= o.ng; ++h)
+        o.SG(o.sigs, n, g, h) = o.SG(o.sigs, n, g, h) + o.M3(const_cast<std::vector<double>&>(f.ss), m, g, h) * dv;
+    }
+  }
+}
+
+// crod_updt (mod_xsec.f90:230-303): fully rodded nodes get the rod changes,
+// the node holding the rod tip a volume fraction of them; then negative
+// siga, nuf, sigf and sigs of the rodded columns are set to zero
+static void crod_updt(Ora& o) {
+  const Ora::Feedback& f = o.fb_crod;
+  auto add = [&](int n, double w) {
+    const int m = o.mat[n - 1];
+    for (int g = 1; g <= o.ng; ++g) {
+      o.N2(o.sigtr, n, g) = o.N2(o.sigtr, n, g) + w * o.M2(const_cast<std::vector<double>&>(f.str), m, g);
+      o.N2(o.siga, n, g) = o.N2(o.siga, n, g) + w * o.M2(const_cast<std::vector<double>&>(f.sa), m, g);
+      o.N2(o.nuf, n, g) = o.N2(o.nuf, n, g) + w * o.M2(const_cast<std::vector<double>&>(f.nf), m, g);
+      o.N2(o.sigf, n, g) = o.N2(o.sigf, n, g) + w * o.M2(const_cast<std::vector<double>&>(f.sf), m, g);
+      for (int h = 1; h <= o.ng; ++h)
+        o.SG(o.sigs, n, g, h) = o.SG(o.sigs, n, g, h) + w * o.M3(const_cast<std::vector<double>&>(f.ss), m, g, h);
+    }
+  };
+  auto addfull = [&](int n) {   // the reference adds the change itself (no factor) to fully rodded nodes
+    const int m = o.mat[n - 1];
+    for (int g = 1; g <= o.ng; ++g) {
+      o.N2(o.sigtr, n, g) = o.N2(o.sigtr, n, g) + o.M2(const_cast<std::vector<double>&>(f.str), m, g);
+      o.N2(o.siga, n, g) = o.N2(o.siga, n, g) + o.M2(const_cast<std::vector<double>&>(f.sa), m, g);
+      o.N2(o.nuf, n, g) = o.N2(o.nuf, n, g) + o.M2(const_cast<std::vector<double>&>(f.nf), m, g);
+      o.N2(o.sigf, n, g) = o.N2(o.sigf, n, g) + o.M2(const_cast<std::vector<double>&>(f.sf), m, g);
+      for (int h = 1; h <= o.ng; ++h)
+        o.SG(o.sigs, n, g, h) = o.SG(o.sigs, n, g, h) + o.M3(const_cast<std::vector<double>&>(f.ss), m, g, h);
+    }
+  };
+  for (int j = 1; j <= o.nyy; ++j)
+    for (int i = 1; i <= o.nxx; ++i) {
+      const int bank = o.fbmap[(i - 1) + (size_t)o.nxx * (j - 1)];
+      if (bank <= 0) continue;
+      const double rodh = o.coreh - o.pos0 - o.bpos[bank - 1] * o.ssize;
+      double dum = 0.0;
+      for (int k = o.nzz; k >= 1; --k) {
+        const int n = o.XYZ(i, j, k);
+        if (rodh >= dum && rodh <= dum + o.zdel[k - 1]) {
+          const double vfrac = (rodh - dum) / o.zdel[k - 1];
+          if (n > 0) add(n, vfrac);
+          break;
+        }
+        if (n > 0) addfull(n);
+        dum = dum + o.zdel[k - 1];
+      }
+      for (int k = o.nzz; k >= 1; --k) {
+        const int n = o.XYZ(i, j, k);
+        if (n <= 0) continue;
+        for (int g = 1; g <= o.ng; ++g) {
+          if (o.N2(o.siga, n, g) < 0.) o.N2(o.siga, n, g) = 0.;
+          if (o.N2(o.nuf, n, g) < 0.) o.N2(o.nuf, n, g) = 0.;
+          if (o.N2(o.sigf, n, g) < 0.) o.N2(o.sigf, n, g) = 0.;
+          for (int h = 1; h <= o.ng; ++h)
+            if (o.SG(o.sigs, n, g, h) < 0.) o.SG(o.sigs, n, g, h) = 0.;
+        }
+      }
+    }
+}
+
+// XS_updt (mod_xsec.f90:11-46): base, the feedback updates in the
+// reference's order (boron, fuel temperature, moderator temperature,
+// coolant density, control rods), D/sigr and the checks.  xbcon is the
+// boron concentration (cbsearch passes its iterate).
+static void xs_updt_at(Ora& o, double xbcon) {
   base_updt(o);
+  if (o.fb_bcon.on) state_updt(o, o.fb_bcon, xbcon - o.fb_bcon.ref);
+  if (o.fb_ftem.on) state_updt(o, o.fb_ftem, std::sqrt(o.fb_ftem.val) - std::sqrt(o.fb_ftem.ref));
+  if (o.fb_mtem.on) state_updt(o, o.fb_mtem, o.fb_mtem.val - o.fb_mtem.ref);
+  if (o.fb_cden.on) state_updt(o, o.fb_cden, o.fb_cden.val - o.fb_cden.ref);
+  if (o.fb_crod.on) crod_updt(o);
   dsigr_updt(o);
   check_xs(o);
 }
+
+static void xs_updt(Ora& o) { xs_updt_at(o, o.bcon); }
 
 // ===========================================================================
 // CMFD (mod_cmfd.f90)
@@ -1810,6 +1997,53 @@ int ora_dsigr_updt(void* h) { Ora* o = (Ora*)h; return guard(o, [&] { dsigr_updt
 
 // mode: 0 forward, 1 adjoint.  max_outers > 0 stops early after that many
 // outers without the maximum-outer error (used for bounded timing samples).
+// cbsearch (mod_th.f90:752-837): secant search of the boron concentration
+// that makes k = 1, each step XS_updt at the iterate and a warm-started
+// outer(0).  Writes at most cap iterates (bcon, k, outers of the step) and
+// returns their count; the STOPs of the reference become errors.
+static int cbsearch(Ora& o, double* bc_out, double* k_out, int* n_out, int cap) {
+  int rec = 0;
+  auto log = [&](double b, double k) {
+    if (rec < cap) { bc_out[rec] = b; k_out[rec] = k; n_out[rec] = o.last_outers; }
+    ++rec;
+  };
+  double bcon = o.fb_bcon.ref;
+  xs_updt_at(o, bcon);
+  outer(o, false, 0, 0);
+  double bc1 = bcon, ke1 = o.Ke;
+  log(bc1, ke1);
+  bcon = bcon + (o.Ke - 1.) * bcon;
+  xs_updt_at(o, bcon);
+  outer(o, false, 0, 0);
+  double bc2 = bcon, ke2 = o.Ke;
+  log(bc2, ke2);
+  int n = 3;
+  while (true) {
+    bcon = bc2 + (1.0 - ke2) / (ke1 - ke2) * (bc1 - bc2);
+    xs_updt_at(o, bcon);
+    outer(o, false, 0, 0);
+    bc1 = bc2;
+    bc2 = bcon;
+    ke1 = ke2;
+    ke2 = o.Ke;
+    log(bcon, o.Ke);
+    if (std::fabs(o.Ke - 1.0) < 1.e-5 && o.last_ser < 1.e-5 && o.last_fer < 1.e-5) break;
+    ++n;
+    if (bcon > 3000.) throw OraError(ORA_ERR_INPUT, "critical boron concentration exceeds the limit (3000 ppm)");
+    if (bcon < 0.) throw OraError(ORA_ERR_INPUT, "critical boron concentration is not found (less than zero)");
+    if (n == 20) throw OraError(ORA_ERR_MAXOUTER, "maximum iteration for critical boron search is reaching maximum");
+  }
+  o.bcon = bcon;
+  return rec;
+}
+
+int ora_cbsearch(void* h, double* bc, double* k, int* outers, int cap, int* count) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] { *count = cbsearch(*o, bc, k, outers, cap); });
+}
+
+int ora_xs_updt_at(void* h, double bcon) { Ora* o = (Ora*)h; return guard(o, [&] { xs_updt_at(*o, bcon); }); }
+
 int ora_outer(void* h, int adj, int popt, int max_outers) {
   Ora* o = (Ora*)h;
   return guard(o, [&] { outer(*o, adj != 0, popt, max_outers); });
@@ -1909,6 +2143,7 @@ int ora_get_int(void* h, const char* name) {
   if (s == "ztop") return o->ztop;
   if (s == "kern") return o->kern == " FDM" ? 0 : (o->kern == " PNM" ? 1 : 2);
   if (s == "adjoint") return o->mode == "ADJOINT" ? 1 : 0;
+  if (s == "bcsearch") return o->mode == "BCSEARCH" ? 1 : 0;
   if (s == "im") return o->im;
   if (s == "jm") return o->jm;
   if (s == "km") return o->km;

@@ -68,10 +68,10 @@ def parse_trace(md_path: str) -> dict:
             "nodal_at": 22, "keff": keff, "outers": rows[-1]["p"]}
 
 
-def deck_fixture(path: str) -> dict:
-    o = oracle.Oracle(path)
+def deck_inputs(o) -> dict:
+    """The parsed input state of a deck as the oracle's reader holds it."""
     nnod, ng, nmat = o.geti("nnod"), o.geti("ng"), o.geti("nmat")
-    inp = {
+    return {
         "ng": ng, "nmat": nmat, "nnod": nnod,
         "nxx": o.geti("nxx"), "nyy": o.geti("nyy"), "nzz": o.geti("nzz"),
         "ix": o.array("ix"), "iy": o.array("iy"), "iz": o.array("iz"), "mat": o.array("mat"),
@@ -84,6 +84,11 @@ def deck_fixture(path: str) -> dict:
         "iter_real": np.array([o.getd("serc"), o.getd("ferc")]),
         "kern": o.geti("kern"), "adjoint": o.geti("adjoint"),
     }
+
+
+def deck_fixture(path: str) -> dict:
+    o = oracle.Oracle(path)
+    inp = deck_inputs(o)
     o.run()
     tr = o.trace()
     out = {

@@ -119,6 +119,32 @@ def test_team_sizes_give_the_same_answer(members):
         assert pcm(a["keff"], c["keff"]) <= 0.01
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_kernel_shapes_give_the_same_answer(members, precision):
+    """The three kernel shapes (256 threads for one or two blocks per SM,
+    512 threads) solve the same cores to the same eigenvalue; in FP64 with
+    the same outer count.  The shapes group the block partial sums
+    differently, and on the mixed path's FP32 Krylov vectors that rounding
+    moves the outer count (418 against 449 outers on one of these cores,
+    at the same k)."""
+    from adpres_gb300.batch import Batch
+    b = Batch([deck.parse(t) for t in members[:6]], precision=precision)
+    out = []
+    for th, bps in ((256, 1), (256, 2), (512, 1)):
+        b.set_config(threads=th, blocks_per_sm=bps, max_team=2)
+        res, _ = b.solve()
+        assert b.config()["blocks_per_sm"] == bps
+        out.append(res)
+    for rs in out[1:]:
+        for a, c in zip(out[0], rs):
+            assert c["converged"] == 1
+            if precision == "fp64":
+                assert pcm(a["keff"], c["keff"]) <= 0.01
+                assert a["outers"] == c["outers"]
+            else:
+                assert pcm(a["keff"], c["keff"]) <= 1.0
+
+
 def test_graph_and_direct_launch_agree(members):
     from adpres_gb300.batch import Batch
     b = Batch([deck.parse(t) for t in members[:3]], precision="mixed")

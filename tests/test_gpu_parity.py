@@ -251,3 +251,60 @@ def test_create_rejects_wrong_node_order():
     with pytest.raises(AdpError) as e:
         Core(dk.nxx, dk.nyy, dk.nzz, ix, dk.iy, dk.iz, dk.xdel, dk.ydel, dk.zdel, dk.bc, dk.ng)
     assert e.value.status == ADP_ERR_INPUT
+
+
+def test_node_table_uploads_agree_and_check():
+    """adp_xs_updt (material tables, base_updt on the device),
+    adp_xs_updt_nodes (node tables) and adp_set_xs (D and sigr given) put the
+    same bits on the device for the same core (ADFs included); check_xs's
+    messages come back from the device checks in the reference's order."""
+    from adpres_gb300.core import Core
+    dk = deck.parse(synth.small_core(seed=3, ng=3, adf=True))
+    m = dk.mat - 1
+    cores = [Core.from_deck(dk) for _ in range(3)]
+    cores[1].xs_updt_nodes(dk.xsigtr[m], dk.xsiga[m], dk.xnuf[m], dk.xsigf[m], dk.chi, dk.mat, dk.xsigs[m], dk.dc)
+    D = 1.0 / (3.0 * dk.xsigtr[m])
+    sigr = dk.xsiga[m].copy()
+    for g in range(dk.ng):
+        for h in range(dk.ng):
+            if h != g:
+                sigr[:, g] = sigr[:, g] + dk.xsigs[m][:, g, h]
+    cores[2].set_xs(D, sigr, dk.xnuf[m], dk.xsigf[m], dk.chi, dk.mat, dk.xsigs[m], dk.dc)
+    reps = [c.outer() for c in cores]
+    assert reps[0].keff == reps[1].keff and reps[0].outers == reps[1].outers
+    assert pcm(reps[2].keff, reps[0].keff) <= 1e-6
+    np.testing.assert_array_equal(cores[0].power(), cores[1].power())
+    f0, fs0, k, dn = cores[0].state()
+    np.testing.assert_array_equal(cores[0].flux(), f0)
+    c = cores[1]
+    c.set_state(f0=f0, fs0=fs0, keff=k, dn=dn)
+    f1, fs1, k1, dn1 = c.state()
+    np.testing.assert_array_equal(f1, f0)
+    np.testing.assert_array_equal(fs1, fs0)
+    np.testing.assert_array_equal(dn1, dn)
+    assert k1 == k
+    c = cores[2]
+    cases = []
+    nuf = dk.xnuf[m].copy()
+    nuf[5, 1] = -1e-3
+    cases.append((dict(nuf=nuf), "nu\\*fission"))
+    chi = dk.chi.copy()
+    chi[0, 0] = -0.1
+    cases.append((dict(chi=chi), "fission spectrum"))
+    sigs = dk.xsigs[m].copy()
+    sigs[7, 0, 1] = -1e-3
+    cases.append((dict(sigs=sigs), "scattering"))
+    mat = dk.mat.copy()
+    mat[3] = dk.nmat + 1
+    cases.append((dict(mat=mat), "out of range"))
+    for over, msg in cases:
+        a = dict(sigtr=dk.xsigtr[m], siga=dk.xsiga[m], nuf=dk.xnuf[m], sigf=dk.xsigf[m], chi=dk.chi, mat=dk.mat,
+                 sigs=dk.xsigs[m], dc=dk.dc)
+        a.update(over)
+        with pytest.raises(AdpError, match=msg) as e:
+            c.xs_updt_nodes(**a)
+        assert e.value.status in (ADP_ERR_BADXS, ADP_ERR_INPUT)
+    # a good upload after the failures solves again
+    c.xs_updt_nodes(dk.xsigtr[m], dk.xsiga[m], dk.xnuf[m], dk.xsigf[m], dk.chi, dk.mat, dk.xsigs[m], dk.dc)
+    c.reset()
+    assert c.outer().keff == reps[0].keff
