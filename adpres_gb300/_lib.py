@@ -68,6 +68,18 @@ class AdpTimers(ctypes.Structure):
                 ("block_threads", ctypes.c_int), ("adjoint_ms", ctypes.c_double), ("adjoint_outers", ctypes.c_long)]
 
 
+class AdpTransOpts(ctypes.Structure):
+    _fields_ = [("nf", ctypes.c_int), ("beta", ctypes.POINTER(ctypes.c_double)),
+                ("lambda_", ctypes.POINTER(ctypes.c_double)), ("velo", ctypes.POINTER(ctypes.c_double)),
+                ("theta", ctypes.c_double), ("extr", ctypes.c_int)]
+
+
+class AdpTransResult(ctypes.Structure):
+    _fields_ = [("rho", ctypes.c_double), ("rho_dollar", ctypes.c_double), ("relpow", ctypes.c_double),
+                ("power", ctypes.c_double), ("maxi", ctypes.c_int), ("outers", ctypes.c_int),
+                ("device_ms", ctypes.c_double)]
+
+
 class AdpBatchConfig(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int), ("max_team", ctypes.c_int), ("grain", ctypes.c_double),
                 ("blocks_per_sm", ctypes.c_int), ("use_graph", ctypes.c_int)]
@@ -120,6 +132,10 @@ SIGNATURES = {
     "adp_batch_power": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "adp_batch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _ip, _dp]),
     "adp_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "adp_trans_init": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpTransOpts), _dp,
+                                      ctypes.POINTER(AdpTransResult)]),
+    "adp_trans_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                      ctypes.POINTER(AdpTransResult)]),
 }
 
 _lib = None

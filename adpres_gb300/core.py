@@ -212,6 +212,24 @@ class Core:
         self._check(self.L.adp_get_timers(self.h, ctypes.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
 
+    # -- rod ejection transient (mod_trans.f90) -------------------------------
+    def trans_init(self, beta, lamb, velo, theta, extr, af):
+        """adp_trans_init after the steady state: af (nnod, ng) adjoint weight.
+        Returns the t = 0 record (rho absolute, relative power 1)."""
+        self._trans_keep = [_c(beta), _c(lamb), _c(velo)]
+        b, l, v = self._trans_keep
+        o = _lib.AdpTransOpts(len(b), dptr(b), dptr(l), dptr(v), float(theta), int(bool(extr)))
+        r = _lib.AdpTransResult()
+        a = _fortran(af)
+        self._check(self.L.adp_trans_init(self.h, ctypes.byref(o), dptr(a), ctypes.byref(r)))
+        return r
+
+    def trans_step(self, dt, omeg_mode):
+        """adp_trans_step: one time step after the step's cross sections are set."""
+        r = _lib.AdpTransResult()
+        self._check(self.L.adp_trans_step(self.h, float(dt), int(omeg_mode), ctypes.byref(r)))
+        return r
+
     def set_launch(self, blocks=0, threads=0):
         self._check(self.L.adp_set_launch(self.h, int(blocks), int(threads)))
 
@@ -281,11 +299,17 @@ def solve_deck(dk, precision="fp64"):
 
     In mode BCSEARCH (th::cbsearch, mod_th.f90:752-837) the report is the last
     outer of the critical boron search and core.bcsearch holds its iterates
-    (bcon, k, outers)."""
+    (bcon, k, outers); in mode RODEJECT the report is the last steady-state
+    outer and core.transient holds the time steps (adpres_gb300.transient)."""
     core = Core.from_deck(dk, precision=precision)
     if dk.mode == "BCSEARCH":
         from .feedback import cbsearch
         core.bcsearch = cbsearch(core, dk)
+        return core.last_report, core.power(), core
+    if dk.mode == "RODEJECT":
+        # rod_eject (mod_trans.f90:17-160): core.transient holds the records
+        from .transient import rod_eject
+        core.transient = rod_eject(core, dk)
         return core.last_report, core.power(), core
     rep, p = core.adjoint() if dk.adjoint else core.forward()
     return rep, p, core

@@ -18,6 +18,8 @@ struct OuterParams {
   BoxGeom G;
   int ng, nin, nac, nupd, nout, adj, do_nodal, mixed;
   int smem_rows;              // > 0: rows per block of the matrix copy in shared memory
+  int trans;                  // 1: outer_tr (mod_cmfd.f90:800-868): source wsrc fs + s0 + exsrc, no k update
+  const double* exsrc;        // [ng][NB] external source of the transient step (trans only)
   double serc, ferc;
   long long NBH;              // group stride of halo'd arrays
   const double* A;            // [ng][7][NB] FP64 CMFD matrix
@@ -90,6 +92,8 @@ struct NodalParams {
   long long* nd_key;
   int* nd_loc;
   int nd_blocks;
+  const double* exsrc;        // cmode 2: [ng][NB] external source of the transient step
+  const double* wnode;        // cmode 2: [NB] 1 - tbeta + dfis of the node
   OuterCtl* ctl;
   double* tr_ndmax;
   int* tr_flags;

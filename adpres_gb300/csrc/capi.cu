@@ -240,6 +240,7 @@ adp_status adp_destroy(adp_handle* h) {
   if (h->adj_base) cudaFree(h->adj_base);
   if (h->edit_base) cudaFree(h->edit_base);
   if (h->react_base) cudaFree(h->react_base);
+  if (h->trans_base) cudaFree(h->trans_base);
   if (h->xfer_base) cudaFree(h->xfer_base);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   for (cudaEvent_t e : {h->e0, h->e1, h->e2, h->e3})
@@ -604,6 +605,10 @@ NodalParams adp::nodal_params(adp_handle* h, int cmode) {
   P.L1 = h->d_L1;
   P.Bc = h->d_Bc;
   P.evbase = h->d_evbase;
+  if (cmode == 2) {
+    P.exsrc = h->d_exsrc;
+    P.wnode = h->d_wnode;
+  }
   P.nd_val = h->d_ndval;
   P.nd_key = h->d_ndkey;
   P.nd_loc = h->d_ndloc;
@@ -883,7 +888,15 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
   const int do_nodal = !frozen && (h->o.kern != ADP_KERN_FDM) && (!adj || popt > 0);
   P.do_nodal = do_nodal;
-  NodalParams NP = nodal_params(h, adj ? 0 : 1);
+  NodalParams NP = nodal_params(h, adj ? 0 : (h->trans_on ? 2 : 1));
+  if (h->trans_on) {
+    // outer_tr (mod_cmfd.f90:800-868): the FP64 kernel with the step's
+    // source weights and external source, no eigenvalue update
+    P.trans = 1;
+    P.mixed = 0;
+    P.wsrc = h->d_wtr;
+    P.exsrc = h->d_exsrc;
+  }
   int blocks, threads;
   launch_shape(h, blocks, threads);
   P.smem_rows = outer_smem_rows(h->NB, blocks, threads, P.mixed);
@@ -905,7 +918,8 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
     if (c.status) { result = ctl_error(h, c); break; }
     if (c.converged) break;
     if (c.max_reached) {
-      result = fail(h, ADP_ERR_MAXOUTER, "maximum number of outer iteration is reached");
+      // outer_tr only flags it (maxi, mod_cmfd.f90:861-865)
+      if (!h->trans_on) result = fail(h, ADP_ERR_MAXOUTER, "maximum number of outer iteration is reached");
       break;
     }
     if (c.nodal_due) {
@@ -925,7 +939,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
       if (c.status) { result = ctl_error(h, c); break; }
       if (c.converged) break;
       if (c.max_reached) {
-        result = fail(h, ADP_ERR_MAXOUTER, "maximum number of outer iteration is reached");
+        if (!h->trans_on) result = fail(h, ADP_ERR_MAXOUTER, "maximum number of outer iteration is reached");
         break;
       }
     }

@@ -94,6 +94,18 @@ struct adp_handle {
   double* d_fsa[2] = {nullptr, nullptr};
   adp::OuterCtl* d_ctla = nullptr;
   double *d_sens = nullptr, *d_spart = nullptr;
+  // rod ejection transient (trans.cu), allocated by adp_trans_init
+  char* trans_base = nullptr;
+  bool trans_ready = false;
+  bool trans_on = false;      // the current adp_outer call is outer_tr
+  int nf = 0;
+  double beta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, lamb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::vector<double> velo;
+  double sth = 1.0, bth = 0.0, tbeta = 0.0, tpow1 = 0.0;
+  int extr = 0;
+  double *d_c0 = nullptr, *d_omeg = nullptr, *d_ft = nullptr, *d_fst = nullptr, *d_sigrp = nullptr;
+  double *d_Lt = nullptr, *d_exsrc = nullptr, *d_wtr = nullptr, *d_wnode = nullptr, *d_af = nullptr;
+  double *d_velo = nullptr, *d_tpart = nullptr, *d_s0q = nullptr;
   // state
   bool xs_set = false;
   bool fwd_ok = false;        // the flux is a converged forward solution of the current XS

@@ -108,9 +108,17 @@ __device__ __forceinline__ void tl_source_items(const NodalParams& P, int start,
     const int b = P.act[n];
     double L[3];
     net_leakage(G, phi + (size_t)g * P.NBH, P.df + (size_t)g * 6 * NB, P.dn + (size_t)g * 6 * NB, b, L);
-    P.S[((size_t)0 * ng + g) * NB + b] = L[1] + L[2];
-    P.S[((size_t)1 * ng + g) * NB + b] = L[0] + L[2];
-    P.S[((size_t)2 * ng + g) * NB + b] = L[0] + L[1];
+    if (P.cmode == 2) {
+      // transient: the step's external source joins the leakage (mod_nodal.f90:1031-1035)
+      const double e = P.exsrc[(size_t)g * NB + b];
+      P.S[((size_t)0 * ng + g) * NB + b] = L[1] + L[2] - e;
+      P.S[((size_t)1 * ng + g) * NB + b] = L[0] + L[2] - e;
+      P.S[((size_t)2 * ng + g) * NB + b] = L[0] + L[1] - e;
+    } else {
+      P.S[((size_t)0 * ng + g) * NB + b] = L[1] + L[2];
+      P.S[((size_t)1 * ng + g) * NB + b] = L[0] + L[2];
+      P.S[((size_t)2 * ng + g) * NB + b] = L[0] + L[1];
+    }
   }
 }
 
@@ -193,7 +201,8 @@ __device__ __forceinline__ TLGeom tl_geom(const BoxGeom& G, int u, int b) {
 
 // get_B (mod_nodal.f90:1345-1405): buckling matrix of node b in direction u,
 // B(g,h) = 0.25 h^2 / D_g * (sigr_g delta_gh - sigs(h->g) - chi_g nuf_h / k)
-// (forward, cmode 1) or the transposed group coupling (adjoint, cmode 0).
+// (forward, cmode 1), the transposed group coupling (adjoint, cmode 0), or
+// the transient form (cmode 2).
 template <int NG>
 __device__ __forceinline__ void get_B(const NodalParams& P, int b, double invKe, const double (&fac)[NG],
                                       double (&B)[NG][NG]) {
@@ -203,7 +212,14 @@ __device__ __forceinline__ void get_B(const NodalParams& P, int b, double invKe,
 #pragma unroll
     for (int h = 0; h < NG; ++h) {
       double dum;
-      if (g == h) {
+      if (P.cmode == 2) {
+        // transient (mod_nodal.f90:1379-1390): prompt and delayed fission of
+        // the step, no eigenvalue; the diagonal carries chi twice, as the
+        // reference writes it
+        const double w = P.wnode[b], chi = P.chin[(size_t)g * NB + b];
+        if (g == h) dum = P.sigr[(size_t)g * NB + b] - w * chi * chi * P.nuf[(size_t)h * NB + b];
+        else dum = -P.sigs[((size_t)h * NG + g) * NB + b] - w * chi * P.nuf[(size_t)h * NB + b];
+      } else if (g == h) {
         dum = P.sigr[(size_t)g * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] * invKe;
       } else if (P.cmode == 1) {
         dum = -P.sigs[((size_t)h * NG + g) * NB + b] - P.chin[(size_t)g * NB + b] * P.nuf[(size_t)h * NB + b] * invKe;

@@ -197,7 +197,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     const double* fsO = P.fs[old];
     double* fsN = P.fs[nw];
     if (threadIdx.x == 0) {
-      const double ik = 1.0 / Ke;
+      const double ik = P.trans ? 1.0 : 1.0 / Ke;   // the transient source has no 1/k
       const ff ikf = ff_from_double(ik);
       s_d[0] = ik;
       s_f[0] = ikf.hi;
@@ -220,6 +220,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       // ---- P0: source and initial residual (TSrc + r = b - A x) --------
       double tot1[1];
       if constexpr (MIXED) {
+        // (the transient runs the FP64 kernel only)
         // Defect of the current flux in double-float: one compensated dot
         // product over the source and the seven matrix terms (A = A32 + lo).
         const float* xOh = P.xh[old] + (size_t)g * NBH;
@@ -272,7 +273,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                     P.adj ? P.sigs[((size_t)g * ng + h) * NB + b] : P.sigs[((size_t)h * ng + g) * NB + b];
                 s0 = fma(sg, ph, s0);
               }
-              const double bs = wsrc[b] * fsO[b] * invKe + s0;
+              double bs = wsrc[b] * fsO[b] * invKe + s0;
+              if (P.trans) bs = bs + P.exsrc[(size_t)g * NB + b];   // TSrcTr (mod_cmfd.f90:1091-1093)
               double a64[7];
 #pragma unroll
               for (int c = 0; c < 7; ++c) a64[c] = A64[(size_t)c * NB + b];
@@ -642,7 +644,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       ser = tot[1];
     }
     e1 = e2;
-    if (threadIdx.x == 0) s_d[2] = Ke * fsum / f;
+    if (threadIdx.x == 0) s_d[2] = P.trans ? Ke : Ke * fsum / f;
     __syncthreads();
     Ke = s_d[2];
     f = fsum;

@@ -22,7 +22,7 @@ from ._lib import ADP_ERR_INPUT, ADP_ERR_BADXS, ADP_ERR_UNSUPPORTED
 
 KNOWN_CARDS = ("MODE", "XSEC", "GEOM", "CASE", "ESRC", "ITER", "PRNT", "ADF", "CROD", "EJCT", "CBCS",
                "FTEM", "MTEM", "CDEN", "BCON", "THER", "XTAB", "KERN", "EXTR", "THET")
-OUT_OF_SCOPE = ("ESRC", "EJCT", "THER", "XTAB", "EXTR", "THET")
+OUT_OF_SCOPE = ("ESRC", "THER", "XTAB")
 
 F_1EM5 = float(np.float32(1.e-5))   # default serc/ferc (mod_data.f90:78-79)
 
@@ -74,6 +74,10 @@ class Deck:
     # changes = sigtr, siga, nuf, sigf (nmat, ng) and sigs (nmat, ng, ng)
     feedback: dict = field(default_factory=dict)
     bcbcs: bool = False                # %CBCS given (critical boron search)
+    # rod ejection transient (%EJCT, %THET, %EXTR): fbpos, tmove, bspeed,
+    # mdir (nb); ttot, tstep1, tdiv, tstep2; beta, lamb (6); velo (ng);
+    # theta (default 1, fully implicit); extr
+    trans: dict = field(default_factory=lambda: {"theta": 1.0, "extr": False})
     extra: dict = field(default_factory=dict)
 
     @property
@@ -198,8 +202,8 @@ def parse(text: str, basedir: str = ".") -> Deck:
     if "MODE" not in cards or not cards["MODE"]:
         raise DeckError(ADP_ERR_INPUT, "card %MODE does not present. this card is mandatory")
     dk.mode = cards["MODE"][0][1].strip().upper()
-    if dk.mode not in ("FORWARD", "ADJOINT", "BCSEARCH"):
-        if dk.mode in ("FIXEDSRC", "RODEJECT"):
+    if dk.mode not in ("FORWARD", "ADJOINT", "BCSEARCH", "RODEJECT"):
+        if dk.mode in ("FIXEDSRC",):
             raise DeckError(ADP_ERR_UNSUPPORTED, f"mode {dk.mode} is outside the static k-eigenvalue path")
         raise DeckError(ADP_ERR_INPUT, f"mode {dk.mode} is unidentified")
     if "KERN" in cards:
@@ -239,6 +243,15 @@ def parse(text: str, basedir: str = ".") -> Deck:
         raise DeckError(ADP_ERR_INPUT, "card %CBCS is not necessary for this calculation mode")
     if dk.mode == "BCSEARCH" and "BCON" in cards:
         raise DeckError(ADP_ERR_INPUT, "card %BCON must not present for this calculation mode")
+    # card checks of mode RODEJECT (mod_io.f90:227-245)
+    if dk.mode == "RODEJECT" and "EJCT" not in cards:
+        raise DeckError(ADP_ERR_INPUT, "mode RODEJECT needs card %EJCT")
+    if dk.mode == "RODEJECT" and "CROD" not in cards:
+        raise DeckError(ADP_ERR_INPUT, "mode RODEJECT needs card %CROD")
+    if dk.mode != "RODEJECT" and "EJCT" in cards:
+        raise DeckError(ADP_ERR_INPUT, "card %EJCT is not necessary for this calculation mode")
+    if "EJCT" in cards:
+        _ejct(dk, cards["EJCT"])
     if "ITER" in cards:
         r = _Card("ITER", cards["ITER"]).rec()
         dk.nout, dk.nin = r.i(), r.i()
@@ -247,10 +260,56 @@ def parse(text: str, basedir: str = ".") -> Deck:
         r.i(), r.i()   # th_niter, nth: thermal-hydraulics only
         if dk.nout < dk.nupd and dk.kern != "FDM":
             r.fail("max. number of outer iteration should be bigger than nodal update interval")
+    if "THET" in cards:
+        r = _Card("THET", cards["THET"]).rec()
+        th = r.d()
+        if th < 0.001:
+            r.fail("theta value is too small")
+        if th > 1.0:
+            r.fail("theta value shall not greater than 1.0")
+        dk.trans["theta"] = th
+    dk.trans["extr"] = "EXTR" in cards
     dk.dc = np.ones((dk.nnod, dk.ng, 6))
     if "ADF" in cards:
         _adf(dk, cards["ADF"], mnum, pasm, zpln)
     return dk
+
+
+def _ejct(dk, lines):
+    """%EJCT (mod_io.f90:2332-2482): per bank the final position, start time
+    and speed; ttot, tstep1, tdiv, tstep2; beta and lambda of the six
+    families; the group velocities (an optional print flag follows)."""
+    c = _Card("EJCT", lines)
+    cr = dk.feedback["crod"]
+    nb = cr["nb"]
+    fbpos, tmove, bspeed, mdir = np.zeros(nb), np.zeros(nb), np.zeros(nb), np.zeros(nb, dtype=np.int64)
+    for i in range(nb):
+        r = c.rec()
+        fbpos[i], tmove[i], bspeed[i] = r.d(), r.d(), r.d()
+        if fbpos[i] > float(cr["nstep"]):
+            r.fail("wrong final control rod position")
+        d = fbpos[i] - cr["bpos"][i]
+        mdir[i] = 0 if abs(d) < 1.e-5 else (2 if d > 1.e-5 else 1)
+    r = c.rec()
+    ttot, tstep1, tdiv, tstep2 = r.d(), r.d(), r.d(), r.d()
+    beta = np.array(c.rec().reals(6))
+    lamb = np.array(c.rec().reals(6))
+    velo = np.array(c.rec().reals(dk.ng))
+    if ttot < tstep1 or ttot < tstep2:
+        r.fail("total simulation time shall be greater than the time steps")
+    if tdiv < tstep1:
+        r.fail("when to start the second time step shall be greater than the first time step")
+    if tdiv > ttot:
+        r.fail("when to start the second time step shall be less than the total time")
+    if _nint(tdiv / tstep1) + _nint((ttot - tdiv) / tstep2) > 10000:
+        r.fail("too many time steps (more than 10000)")
+    dk.trans.update(fbpos=fbpos, tmove=tmove, bspeed=bspeed, mdir=mdir, ttot=ttot, tstep1=tstep1, tdiv=tdiv,
+                    tstep2=tstep2, beta=beta, lamb=lamb, velo=velo)
+
+
+def _nint(x):
+    """Fortran NINT: nearest integer, halves away from zero."""
+    return int(np.floor(x + 0.5)) if x >= 0 else -int(np.floor(-x + 0.5))
 
 
 def _changes(dk, c):

@@ -5,7 +5,7 @@ cards: node tables from the material tables (base_updt), then per node
 x += change(mat) * dv for boron (bcon - rbcon), fuel temperature
 (sqrt(T) - sqrt(Tref)), moderator temperature and coolant density
 (bcon_updt, ftem_updt, mtem_updt, cden_updt, :394-521), then the control
-rods (crod_updt, :230-303): fully rodded nodes get the rod changes, the
+rods (crod_updt, :230-303) at the given bank positions: fully rodded nodes get the rod changes, the
 node holding the tip a volume fraction of them, and negative siga, nuf,
 sigf and sigs of rodded columns become 0.  The result goes to the device
 through adp_xs_updt_nodes, which forms D and sigr and checks them.
@@ -36,7 +36,7 @@ def _rod_tip(rodh, zdel):
     return -1, None
 
 
-def xs_update(dk, bcon=None):
+def xs_update(dk, bcon=None, bpos=None):
     """Node tables sigtr, siga, nuf, sigf (nnod, ng) and sigs (nnod, ng, ng).
 
     Up to the control rods a node's values are those of its material, so the
@@ -61,14 +61,16 @@ def xs_update(dk, bcon=None):
     m = dk.mat - 1
     t = {k: tab[k][m] for k in KEYS}
     if "crod" in fb:
-        _crod_update(dk, fb["crod"], t)
+        _crod_update(dk, fb["crod"], t, bpos)
     return t
 
 
-def _crod_update(dk, cr, t):
+def _crod_update(dk, cr, t, bpos=None):
     """Each node is in one column, so the reference's column loop is a per-bank
-    selection: planes above the tip get x + c, the tip's plane x + w*c."""
+    selection: planes above the tip get x + c, the tip's plane x + w*c.
+    bpos: bank positions (steps) when they differ from the card's."""
     ch = cr["changes"]
+    bpos = cr["bpos"] if bpos is None else bpos
     m = dk.mat - 1
     z = np.asarray(dk.iz) - 1
     bank = np.asarray(cr["fbmap"])[np.asarray(dk.ix) - 1, np.asarray(dk.iy) - 1]
@@ -77,7 +79,7 @@ def _crod_update(dk, cr, t):
         sel = bank == b
         if not sel.any():
             continue
-        kt, vf = _rod_tip(dk.coreh - cr["pos0"] - cr["bpos"][b - 1] * cr["ssize"], zdel)
+        kt, vf = _rod_tip(dk.coreh - cr["pos0"] - bpos[b - 1] * cr["ssize"], zdel)
         full = np.nonzero(sel & (z > kt))[0]
         part = np.nonzero(sel & (z == kt))[0]
         for k in KEYS:

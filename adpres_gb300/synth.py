@@ -20,6 +20,7 @@ and the CPU oracle.
   boron_search_3d  the full-core geometry in mode BCSEARCH with boron, fuel
                    and moderator temperature, coolant density and two
                    control-rod banks as feedback cards.
+  rod_ejection_3d  the same core in mode RODEJECT: one bank ejected in 0.05 s.
   small_core       a small ragged core with optional ADFs, any boundary
                    conditions and 1-4 groups (parity tests).
 
@@ -304,6 +305,32 @@ def boron_search_3d(seed=0, n=17, planes=20, rbcon=1000.0):
     # coolant density, per g/cm3
     cden = [[7.5e-2, 2.1e-4, 0.0, 0.0, 0.0, 3.7e-2], [5.3e-1, 7.6e-3, 0.0, 0.0, 0.0, 0.0]]
     L += ["%CDEN", "0.72 0.71"] + _changes2([cden] * nm)
+    return text + "\n".join(L) + "\n"
+
+
+def rod_ejection_3d(seed=0, n=17, planes=20, ttot=0.5, tstep1=0.01, tdiv=0.1, tstep2=0.05, theta=0.5):
+    """Rod ejection (mode RODEJECT) on the core of boron_search_3d: the same
+    geometry, cross sections (at its reference boron, no boron card) and two
+    rod banks; bank 1 is ejected from step 120 to 228 at 2280 steps/s (0.05 s),
+    bank 2 stays.  Six delayed families, 2-group velocities; theta 0.5
+    (Crank-Nicolson); the steady state is brought to k = 1 by KNE1."""
+    text = boron_search_3d(seed, n=n, planes=planes)
+    out, skip = [], False
+    for ln in text.splitlines():
+        t = ln.strip()
+        if t.startswith("%"):
+            skip = t[1:] in ("CBCS", "FTEM", "MTEM", "CDEN")
+        if not skip:
+            out.append(ln)
+    text = "\n".join(out).replace("%MODE\nBCSEARCH", "%MODE\nRODEJECT") + "\n"
+    L = ["%EJCT",
+         "228.0 0.0 2280.0",
+         "200.0 0.0 0.0",
+         " ".join(_fmt(v) for v in (ttot, tstep1, tdiv, tstep2)),
+         "0.000215 0.001424 0.001274 0.002568 0.000748 0.000273",
+         "0.0124 0.0305 0.111 0.301 1.14 3.01",
+         "2.0e7 2.2e5",
+         "%THET", _fmt(theta)]
     return text + "\n".join(L) + "\n"
 
 

@@ -233,6 +233,56 @@ def cbsearch_leg(flush, steps=3):
     return out
 
 
+# ---------------------------------------------------- transient leg ----
+def _transient_oracle(text):
+    import oracle
+    o = oracle.Oracle(text=text)
+    t0 = time.perf_counter()
+    r = o.rodeject()
+    return time.perf_counter() - t0, r
+
+
+def transient_leg(steps=2):
+    """rod_eject on the 34x34x22-node core (seed 0): steady state with k
+    brought to one, adjoint weight, then 18 time steps (bank 1 ejected in
+    0.05 s, theta 0.5); each step XS_updt at the new bank positions on the
+    host, then removal, external source, outer_tr (FP64 kernel), precursors,
+    power and reactivity on the GPU.  Timed end to end (wall clock); the
+    oracle's whole transient on one host core is the CPU baseline."""
+    import multiprocessing as mp
+
+    import numpy as np
+
+    from adpres_gb300 import deck, synth
+    from adpres_gb300.core import Core
+    from adpres_gb300.transient import rod_eject
+
+    text = synth.rod_ejection_3d(0)
+    dk = deck.parse(text)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        t_cpu, ref = pool.apply(_transient_oracle, (text,))
+    walls, rec = [], None
+    for i in range(steps + 1):
+        core = Core.from_deck(dk, precision="fp64")
+        t0 = time.perf_counter()
+        rec = rod_eject(core, dk)
+        if i:
+            walls.append(time.perf_counter() - t0)
+        core.close()
+    t = sum(walls) / len(walls)
+    pw = np.array([r[2] for r in ref])
+    got = np.array([r[2] for r in rec])
+    nsteps = len(rec) - 1
+    return {"workload": "rod_ejection_3d seed 0: 34x34 radial nodes x 22 planes, 2 groups, SANM, 18 steps "
+                        "(0.01 s to 0.1 s, then 0.05 s), theta 0.5",
+            "nodes": int(dk.nnod), "steps": nsteps, "ms_per_transient": t * 1e3, "steps_per_s": nsteps / t,
+            "outers": int(sum(r[4] for r in rec[1:])), "device_ms": float(sum(r[5] for r in rec[1:])),
+            "peak_relpow": float(got.max()), "max_relpow_diff_vs_oracle": float(np.max(np.abs(got - pw) / pw)),
+            "cpu_baseline": {"value": nsteps / t_cpu, "unit": "time steps/s", "cores": 1, "kind": "port",
+                             "sample": f"the oracle's whole transient on this core ({t_cpu:.1f} s)"}}
+
+
 # ------------------------------------------------- batched solves leg ----
 def _batch_oracle_member(args):
     seed, i = args
@@ -423,6 +473,7 @@ def run_ours(args):
 
     adjoint = adjoint_leg(flush)
     boron = cbsearch_leg(flush)
+    transient = transient_leg()
     batched = batch_leg(flush) if not args.no_batch else None
 
     # e2e through the C ABI from host buffers: the inputs sit in pinned host
@@ -478,6 +529,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "adjoint": adjoint,
         "cbsearch": boron,
+        "transient": transient,
         "batched": batched,
         "gpu_launches": gpu_launches,
         "clocks": ck,

@@ -262,6 +262,45 @@ adp_status adp_reactivity(adp_handle* h, const double* af, const double* sigrp, 
 adp_status adp_core_beta(adp_handle* h, const double* af, int nmat, int nf, const double* ibeta, const int* mat,
                          double* beta);
 
+/* -- rod ejection transient (mod_trans.f90:17-640, mod_cmfd.f90:800-952) -- */
+
+/* Delayed neutron data and time integration of the transient: nf (1..8)
+ * precursor families' fractions and decay constants, ng group velocities,
+ * theta of the theta method (%THET, 0.001..1), and whether the exponential
+ * flux transformation is on (%EXTR). */
+typedef struct adp_trans_opts {
+  int nf;
+  const double* beta;
+  const double* lambda;
+  const double* velo;
+  double theta;
+  int extr;
+} adp_trans_opts;
+
+typedef struct adp_trans_result {
+  double rho;               /* adjoint-weighted reactivity (mod_trans.f90:648-688) */
+  double rho_dollar;        /* rho / total beta                                */
+  double relpow;            /* PowTot relative to the initial state            */
+  double power;             /* PowTot                                          */
+  int maxi;                 /* 1 when the step's outer_tr reached nout          */
+  int outers;               /* outers of the step                               */
+  double device_ms;
+} adp_trans_result;
+
+/* After the steady state of rod_eject (forward outer, k brought to one,
+ * the adjoint af (nnod, ng) of outer_ad, the forward outer again): iPden,
+ * PowTot and the reactivity of the initial state (rho in absolute units),
+ * and the leakage the first step's source needs. */
+adp_status adp_trans_init(adp_handle* h, const adp_trans_opts* opts, const double* af, adp_trans_result* r0);
+/* One time step of trans_calc (mod_trans.f90:332-479) after the host has
+ * moved the rods and uploaded the step's cross sections (adp_xs_updt or
+ * adp_xs_updt_nodes): removal sigr + 1/(theta v dt) + omega/v, get_exsrc,
+ * outer_tr (FP64 kernel, nodal update in its transient form), uPden,
+ * PowTot and the reactivity with the step's XS_updt removal.  omeg_mode 1:
+ * omega = log(f0/ft)/dt (rod_eject applies it from the second step on when
+ * %EXTR is given), 0: omega = 0.  Reaching nout only sets r->maxi. */
+adp_status adp_trans_step(adp_handle* h, double dt, int omeg_mode, adp_trans_result* r);
+
 /* -- batched solves ------------------------------------------------------ */
 
 /* Many independent cores solved together; no counterpart in the reference,

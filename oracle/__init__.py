@@ -109,6 +109,7 @@ def lib(variant: str = "plain"):
         L.ora_reactivity.argtypes = [vp, dp, dp, dp]
         L.ora_cbsearch.argtypes = [vp, dp, dp, ipp, ip, ipp]
         L.ora_xs_updt_at.argtypes = [vp, ctypes.c_double]
+        L.ora_rodeject.argtypes = [vp, dp, dp, dp, ipp, ipp, ip, ip, ipp]
         L.ora_calc_beta.argtypes = [vp, dp, ip, dp, dp]
         L.ora_axipow.argtypes = [vp, dp, dp, ipp]
         L.ora_asmflux.argtypes = [vp, dp, ctypes.c_double, dp, ipp]
@@ -184,6 +185,8 @@ class Oracle:
         th::cbsearch (mod_th.f90:752-837) in mode BCSEARCH."""
         if self.geti("bcsearch"):
             return self.cbsearch()
+        if self.geti("rodeject"):
+            return self.rodeject()
         self.xs_updt()
         self.outer(adjoint=bool(self.geti("adjoint")), popt=1)
 
@@ -195,6 +198,17 @@ class Oracle:
         self._check(self.L.ora_cbsearch(self.h, _dp(bc), _dp(k), _ip(no), cap, ctypes.byref(n)))
         m = min(n.value, cap)
         return [(float(bc[i]), float(k[i]), int(no[i])) for i in range(m)]
+
+    def rodeject(self, cap=20000, max_steps=-1):
+        """rod_eject (mod_trans.f90:17-160): list of (t, rho, relative power,
+        nout reached, outers); rho is in dollars after t = 0 and absolute at t = 0."""
+        t, rho, pw = np.zeros(cap), np.zeros(cap), np.zeros(cap)
+        mx, no = np.zeros(cap, dtype=np.int32), np.zeros(cap, dtype=np.int32)
+        n = ctypes.c_int()
+        self._check(self.L.ora_rodeject(self.h, _dp(t), _dp(rho), _dp(pw), _ip(mx), _ip(no), cap, int(max_steps),
+                                        ctypes.byref(n)))
+        m = min(n.value, cap)
+        return [(float(t[i]), float(rho[i]), float(pw[i]), bool(mx[i]), int(no[i])) for i in range(m)]
 
     def xs_updt_at(self, bcon):
         """XS_updt with the boron concentration bcon (feedback cards applied)."""

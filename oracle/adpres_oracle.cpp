@@ -100,6 +100,22 @@ struct Ora {
   std::vector<double> bpos;                             // (nb) bank positions in steps
   std::vector<int> fbmap;                               // (nxx,nyy) bank of each node column, 0 none
   double bcon = 0.0;                                    // %BCON concentration (forward mode)
+  // rod ejection transient (%EJCT, %THET, %EXTR; mod_io.f90:1650-1689,
+  // 2332-2482): bank motion, time steps, delayed neutron data, velocities
+  static constexpr int nf = 6;                          // precursor families (mod_data.f90:131)
+  double ibeta[nf] = {0, 0, 0, 0, 0, 0}, lamb[nf] = {0, 0, 0, 0, 0, 0};
+  std::vector<double> velo;                             // (ng)
+  double ttot = 0.0, tstep1 = 0.0, tdiv = 0.0, tstep2 = 0.0;
+  std::vector<double> fbpos, tmove, bspeed;             // (nb)
+  std::vector<int> mdir;                                // 0 still, 1 down, 2 up
+  double sth = 1.0, bth = 0.0;                          // theta and (1 - theta) / theta
+  bool bextr = false;                                   // exponential flux transformation
+  // transient state (mod_trans.f90, mod_cmfd.f90:800-952)
+  std::vector<double> c0;                               // (nnod,nf) precursor densities
+  std::vector<double> omeg, Lt, ft, sigrp;              // (nnod,ng) frequencies, leakage, old flux, removal
+  std::vector<double> fst, dfis;                        // (nnod)
+  std::vector<double> tbeta;                            // (nmat)
+  double ctbeta = 0.0;
   std::vector<double> dc;               // (nnod,ng,6)
   std::vector<double> exsrc;            // (nnod,ng)
   // node XS
@@ -633,6 +649,47 @@ static void read_crod(Ora& o, std::vector<Line>* L) {
   read_changes(o, cr, o.fb_crod);
 }
 
+// inp_ejct (mod_io.f90:2332-2482), without %XTAB: per bank the final
+// position, start time and speed; ttot, tstep1, tdiv, tstep2; beta and
+// lambda of the six families; the group velocities; an optional print flag
+static void read_ejct(Ora& o, std::vector<Line>* L) {
+  CardReader cr(L, "EJCT");
+  o.fbpos.assign(o.nb, 0.0); o.tmove = o.fbpos; o.bspeed = o.fbpos;
+  o.mdir.assign(o.nb, 0);
+  for (int i = 0; i < o.nb; ++i) {
+    Rec r = cr.rec();
+    o.fbpos[i] = r.getd(); o.tmove[i] = r.getd(); o.bspeed[i] = r.getd();
+    if (o.fbpos[i] > (double)o.nstep) r.fail("wrong final control rod position");
+    if (std::fabs(o.fbpos[i] - o.bpos[i]) < 1.e-5) o.mdir[i] = 0;
+    else if (o.fbpos[i] - o.bpos[i] > 1.e-5) o.mdir[i] = 2;
+    else o.mdir[i] = 1;
+  }
+  Rec t = cr.rec();
+  o.ttot = t.getd(); o.tstep1 = t.getd(); o.tdiv = t.getd(); o.tstep2 = t.getd();
+  Rec b = cr.rec();
+  for (int i = 0; i < Ora::nf; ++i) o.ibeta[i] = b.getd();
+  Rec l = cr.rec();
+  for (int i = 0; i < Ora::nf; ++i) o.lamb[i] = l.getd();
+  Rec v = cr.rec();
+  o.velo.assign(o.ng, 0.0);
+  for (int g = 0; g < o.ng; ++g) o.velo[g] = v.getd();
+  if (o.ttot < o.tstep1 || o.ttot < o.tstep2) t.fail("total simulation time shall be greater than the time steps");
+  if (o.tdiv < o.tstep1) t.fail("when to start the second time step shall be greater than the first time step");
+  if (o.tdiv > o.ttot) t.fail("when to start the second time step shall be less than the total time");
+  if (std::lround(o.tdiv / o.tstep1) + std::lround((o.ttot - o.tdiv) / o.tstep2) > 10000)
+    t.fail("too many time steps (more than 10000)");
+}
+
+// inp_thet (mod_io.f90:1650-1689)
+static void read_thet(Ora& o, std::vector<Line>* L) {
+  CardReader cr(L, "THET");
+  Rec r = cr.rec();
+  o.sth = r.getd();
+  if (o.sth < 0.001) r.fail("theta value is too small");
+  if (o.sth > 1.0) r.fail("theta value shall not greater than 1.0");
+  o.bth = (1.0 - o.sth) / o.sth;
+}
+
 // inp_cbcs (mod_io.f90:2486-2571) / inp_bcon (:2575-2662) / inp_ftem, inp_mtem,
 // inp_cden (:2666-2954): the state value (and reference) then the changes
 static void read_state_card(Ora& o, std::vector<Line>* L, const char* name, Ora::Feedback& f, bool has_value) {
@@ -653,15 +710,15 @@ static void parse_deck(Ora& o, const std::string& text, const std::string& based
   strip_comments(text, buf);
   Cards cards;
   split_cards(buf, basedir, cards);
-  static const char* oos[] = {"ESRC", "EJCT", "THER", "XTAB", "EXTR", "THET"};
+  static const char* oos[] = {"ESRC", "THER", "XTAB"};
   for (auto& c : cards.cards)
     for (auto k : oos)
       if (c.first == k) throw OraError(ORA_ERR_UNSUPPORTED, "card %" + c.first + " is outside the static k-eigenvalue path");
   auto* m = cards.find("MODE");
   if (!m || m->empty()) throw OraError(ORA_ERR_INPUT, "card %MODE does not present. this card is mandatory");
   o.mode = upper(trim((*m)[0].text));
-  if (o.mode != "FORWARD" && o.mode != "ADJOINT" && o.mode != "BCSEARCH") {
-    if (o.mode == "FIXEDSRC" || o.mode == "RODEJECT")
+  if (o.mode != "FORWARD" && o.mode != "ADJOINT" && o.mode != "BCSEARCH" && o.mode != "RODEJECT") {
+    if (o.mode == "FIXEDSRC")
       throw OraError(ORA_ERR_UNSUPPORTED, "mode " + o.mode + " is outside the static k-eigenvalue path");
     throw OraError(ORA_ERR_INPUT, "mode " + o.mode + " is unidentified");
   }
@@ -693,7 +750,15 @@ static void parse_deck(Ora& o, const std::string& text, const std::string& based
     throw OraError(ORA_ERR_INPUT, "card %CBCS is not necessary for this calculation mode");
   if (o.mode == "BCSEARCH" && cards.find("BCON"))
     throw OraError(ORA_ERR_INPUT, "card %BCON must not present for this calculation mode");
+  // card checks of mode RODEJECT (mod_io.f90:227-245)
+  auto* ej = cards.find("EJCT");
+  if (o.mode == "RODEJECT" && !ej) throw OraError(ORA_ERR_INPUT, "mode RODEJECT needs card %EJCT");
+  if (o.mode == "RODEJECT" && !cards.find("CROD")) throw OraError(ORA_ERR_INPUT, "mode RODEJECT needs card %CROD");
+  if (o.mode != "RODEJECT" && ej) throw OraError(ORA_ERR_INPUT, "card %EJCT is not necessary for this calculation mode");
+  if (ej) read_ejct(o, ej);
   if (auto* it = cards.find("ITER")) read_iter(o, it);
+  if (auto* th = cards.find("THET")) read_thet(o, th);
+  o.bextr = cards.find("EXTR") != nullptr;
   o.dc.assign((size_t)o.nnod * o.ng * 6, 1.0);
   if (auto* a = cards.find("ADF")) { o.badf = true; read_adf(o, a); }
   o.exsrc.assign((size_t)o.nnod * o.ng, 0.0);
@@ -1079,7 +1144,14 @@ static void get_B(Ora& o, int u, int n, std::vector<double>& B) {
   for (int g = 1; g <= o.ng; ++g)
     for (int h = 1; h <= o.ng; ++h) {
       double dum;
-      if (g == h) dum = o.N2(o.sigr, n, g) - o.M2(o.chi, m, g) * o.N2(o.nuf, n, h) / o.Ke;
+      if (o.cmode == 2) {
+        // transient (mod_nodal.f90:1379-1390): prompt and delayed fission of
+        // the step, no eigenvalue; the diagonal carries chi twice, as the
+        // reference writes it
+        const double w = (1.0 - o.tbeta[m - 1] + o.dfis[n - 1]);
+        if (g == h) dum = o.N2(o.sigr, n, g) - w * o.M2(o.chi, m, g) * o.M2(o.chi, m, g) * o.N2(o.nuf, n, h);
+        else dum = -o.SG(o.sigs, n, h, g) - w * o.M2(o.chi, m, g) * o.N2(o.nuf, n, h);
+      } else if (g == h) dum = o.N2(o.sigr, n, g) - o.M2(o.chi, m, g) * o.N2(o.nuf, n, h) / o.Ke;
       else if (o.cmode == 1) dum = -o.SG(o.sigs, n, h, g) - o.M2(o.chi, m, g) * o.N2(o.nuf, n, h) / o.Ke;
       else dum = -o.SG(o.sigs, n, g, h) - o.M2(o.chi, m, h) * o.N2(o.nuf, n, g) / o.Ke;
       o.Bm(B, g, h) = 0.25 * (dn * dn) / o.N2(o.D, n, g) * dum;
@@ -1147,9 +1219,15 @@ static void get_source(Ora& o) {
     for (int n = 1; n <= o.nnod; ++n) {
       double L1, L2, L3;
       lxyz(o, n, g, L1, L2, L3);
-      o.N2(o.S1, n, g) = L2 + L3;
-      o.N2(o.S2, n, g) = L1 + L3;
-      o.N2(o.S3, n, g) = L1 + L2;
+      if (o.cmode == 2) {   // transient: the step's external source joins the leakage (:1031-1035)
+        o.N2(o.S1, n, g) = L2 + L3 - o.N2(o.exsrc, n, g);
+        o.N2(o.S2, n, g) = L1 + L3 - o.N2(o.exsrc, n, g);
+        o.N2(o.S3, n, g) = L1 + L2 - o.N2(o.exsrc, n, g);
+      } else {
+        o.N2(o.S1, n, g) = L2 + L3;
+        o.N2(o.S2, n, g) = L1 + L3;
+        o.N2(o.S3, n, g) = L1 + L2;
+      }
     }
 }
 
@@ -1306,14 +1384,16 @@ static void lu_solve(Ora& o, int nt, int msize, const std::vector<double>& mat, 
   }
 }
 
-// get_a2matvec (mod_nodal.f90:769-825), static path (cmode /= 2)
+// get_a2matvec (mod_nodal.f90:769-825); in the transient mode (cmode 2)
+// the source already holds -exsrc
 static void get_a2matvec(Ora& o, int u, int n, std::vector<double>& A, std::vector<double>& b) {
   int G = o.ng;
   std::vector<double> Bf(G, 0.0);
   double h = hdir(o, u, n);
   std::vector<double>& S = (u == 1) ? o.S1 : (u == 2) ? o.S2 : o.S3;
   for (int g = 1; g <= G; ++g) {
-    double Sv = 0.25 * (h * h) / o.N2(o.D, n, g) * (o.N2(S, n, g) - o.N2(o.exsrc, n, g));
+    double Sv = (o.cmode == 2) ? 0.25 * (h * h) / o.N2(o.D, n, g) * o.N2(S, n, g)
+                               : 0.25 * (h * h) / o.N2(o.D, n, g) * (o.N2(S, n, g) - o.N2(o.exsrc, n, g));
     for (int hh = 1; hh <= G; ++hh) {
       if (hh == g) A[(g - 1) + G * (hh - 1)] = o.Bm(o.Bcp, g, hh) * o.Ep[g - 1] + 3.0;
       else A[(g - 1) + G * (hh - 1)] = o.Bm(o.Bcp, g, hh) * o.Ep[g - 1];
@@ -1869,6 +1949,7 @@ static double reactivity(Ora& o, const double* af, const double* sigrp) {
       double L1, L2, L3;
       lxyz(o, n, g, L1, L2, L3);
       const double L = L1 + L2 + L3;
+      if (!o.Lt.empty()) o.N2(o.Lt, n, g) = L;   // L(n,g) of the transient source
       const double a = af[(n - 1) + (size_t)N * (g - 1)];
       const double chi = o.M2(o.chi, o.mat[n - 1], g);
       src = src + a * (scg[n - 1] + chi * o.fs0[n - 1]) * o.vdel[n - 1];
@@ -1903,6 +1984,212 @@ static double calc_beta(Ora& o, const double* af, int nf, const double* ibeta) {
   return beta;
 }
 
+// ===========================================================================
+// Rod ejection transient (mod_trans.f90:17-160, 332-640; mod_cmfd.f90:800-952,
+// 1068-1095), without thermal-hydraulics and %XTAB
+// ===========================================================================
+
+// TSrcTr (mod_cmfd.f90:1068-1095): zero-fills all of s0, as TSrc does
+static void tsrctr(Ora& o, int g, std::vector<double>& bs) {
+  std::fill(o.s0.begin(), o.s0.end(), 0.0);
+  for (int h = 1; h <= o.ng; ++h)
+    for (int n = 1; n <= o.nnod; ++n)
+      if (g != h) o.N2(o.s0, n, g) = o.N2(o.s0, n, g) + o.SG(o.sigs, n, h, g) * o.N2(o.f0, n, h);
+  for (int n = 1; n <= o.nnod; ++n) {
+    const int m = o.mat[n - 1];
+    bs[n - 1] = (1.0 - o.tbeta[m - 1] + o.dfis[n - 1]) * o.M2(o.chi, m, g) * o.fs0[n - 1] + o.N2(o.s0, n, g) +
+                o.N2(o.exsrc, n, g);
+  }
+}
+
+// get_exsrc (mod_cmfd.f90:872-952): delayed source of the step and the
+// theta-method terms of the previous step
+static void get_exsrc(Ora& o, double ht) {
+  for (int n = 1; n <= o.nnod; ++n) {
+    const int m = o.mat[n - 1];
+    double dt = 0.0, dtp = 0.0;
+    o.dfis[n - 1] = 0.0;
+    for (int i = 0; i < Ora::nf; ++i) {
+      const double pxe = std::exp(-o.lamb[i] * ht);
+      double a1 = (1.0 - pxe) / (o.lamb[i] * ht);
+      const double a2 = 1.0 - a1;
+      a1 = a1 - pxe;
+      const double c = o.c0[(n - 1) + (size_t)o.nnod * i];
+      o.dfis[n - 1] = o.dfis[n - 1] + o.ibeta[i] * a2;
+      dt = dt + o.lamb[i] * c * pxe + o.ibeta[i] * a1 * o.fst[n - 1];
+      dtp = dtp + o.lamb[i] * c;
+    }
+    for (int g = 1; g <= o.ng; ++g) {
+      const double chi = o.M2(o.chi, m, g);
+      const double pthet = -o.N2(o.Lt, n, g) - o.N2(o.sigrp, n, g) * o.N2(o.ft, n, g) + o.N2(o.s0, n, g) +
+                           (1.0 - o.tbeta[m - 1]) * chi * o.fst[n - 1] + chi * dtp;
+      o.N2(o.exsrc, n, g) = chi * dt + std::exp(o.N2(o.omeg, n, g) * ht) * o.N2(o.ft, n, g) /
+                                           (o.sth * o.velo[g - 1] * ht) + o.bth * pthet;
+    }
+  }
+}
+
+// outer_tr (mod_cmfd.f90:800-868): fixed-source outer iterations of one
+// step; true when nout is reached (the reference's maxi)
+static bool outer_tr(Ora& o, double ht) {
+  const int N = o.nnod, G = o.ng;
+  matrix_setup(o, 1);
+  get_exsrc(o, ht);
+  std::vector<double> fs0c(N), bs(N), f0c((size_t)N * G), errn(N, 0.0);
+  double e1 = 0.0, e2;
+  o.trace.clear();
+  int p;
+  for (p = 1; p <= o.nout; ++p) {
+    TraceRec tr{};
+    tr.p = p;
+    fs0c = o.fs0; f0c = o.f0;
+    for (int g = 1; g <= G; ++g) {
+      tsrctr(o, g, bs);
+      bicg(o, o.nin, g, bs, &o.f0[(size_t)N * (g - 1)]);
+    }
+    fsrc(o, o.fs0, false);
+    for (int n = 0; n < N; ++n) errn[n] = o.fs0[n] - fs0c[n];
+    e2 = l2norm(errn);
+    if (p % o.nac == 0) { fiss_extrp(e1, e2, errn, o.fs0); tr.extrapolated = 1; }
+    e1 = e2;
+    const double ser = rele(o, o.fs0, fs0c);
+    const double fer = releg(o, o.f0, f0c);
+    if (p % o.nupd == 0 && o.kern != " FDM") {
+      nodal_upd(o, 2);
+      tr.nodal = 1; tr.ndmax = o.ndmax; tr.im = o.im; tr.jm = o.jm; tr.km = o.km;
+    }
+    tr.k = o.Ke; tr.ser = ser; tr.fer = fer;
+    o.trace.push_back(tr);
+    o.last_ser = ser; o.last_fer = fer;
+    if (ser < o.serc && fer < o.ferc && o.ndmax < F_1em2) break;
+  }
+  o.last_outers = std::min(p, o.nout);
+  return p == o.nout + 1;
+}
+
+// iPden (mod_trans.f90:561-597)
+static void ipden(Ora& o) {
+  o.c0.assign((size_t)o.nnod * Ora::nf, 0.0);
+  for (int n = 0; n < o.nnod; ++n)
+    for (int j = 0; j < Ora::nf; ++j) o.c0[n + (size_t)o.nnod * j] = o.ibeta[j] / o.lamb[j] * o.fs0[n];
+}
+
+// uPden (mod_trans.f90:601-640)
+static void upden(Ora& o, double ht) {
+  for (int i = 0; i < Ora::nf; ++i) {
+    const double pxe = std::exp(-o.lamb[i] * ht);
+    double a1 = (1.0 - pxe) / (o.lamb[i] * ht);
+    const double a2 = 1.0 - a1;
+    a1 = a1 - pxe;
+    for (int n = 0; n < o.nnod; ++n) {
+      double& c = o.c0[n + (size_t)o.nnod * i];
+      c = c * pxe + o.ibeta[i] / o.lamb[i] * (a1 * o.fst[n] + a2 * o.fs0[n]);
+    }
+  }
+}
+
+// PowTot (mod_trans.f90:522-557)
+static double powtot(Ora& o) {
+  std::vector<double> pw(o.nnod, 0.0);
+  for (int g = 1; g <= o.ng; ++g)
+    for (int n = 1; n <= o.nnod; ++n) {
+      double q = o.N2(o.f0, n, g) * o.N2(o.sigf, n, g) * o.vdel[n - 1];
+      if (q < 0.) q = 0.;
+      pw[n - 1] = pw[n - 1] + q;
+    }
+  double t = 0.0;
+  for (int n = 0; n < o.nnod; ++n) t = t + pw[n];
+  return t;
+}
+
+// KNE1 (mod_trans.f90:483-518): scale nu*sigf (and its rod change) by 1/k
+// until k = 1.  The reference tests the loop index after the loop, so an
+// exit on the tenth pass stops as well, and ten passes without an exit do
+// not.
+static void kne1(Ora& o) {
+  int i;
+  for (i = 1; i <= 10; ++i) {
+    for (auto& x : o.xnuf) x = x / o.Ke;
+    for (auto& x : o.fb_crod.nf) x = x / o.Ke;
+    xs_updt(o);
+    outer(o, false, 0, 0);
+    if (std::fabs(o.Ke - 1.0) < 1.e-5) break;
+  }
+  if (i == 10) throw OraError(ORA_ERR_INPUT, "k-eff still not equal to one");
+}
+
+struct TransRec { double t, rho, pow; int maxi, outers; };
+
+// trans_calc (mod_trans.f90:332-479) for thc = 0
+static TransRec trans_calc(Ora& o, double ht, const std::vector<double>& af, double tpow1, double t2) {
+  for (int n = 0; n < o.nb; ++n) {
+    if (o.mdir[n] == 1) {
+      if (t2 - o.tmove[n] > 1.e-5 && o.fbpos[n] - o.bpos[n] < 1.e-5) {
+        o.bpos[n] = o.bpos[n] - ht * o.bspeed[n];
+        if (o.bpos[n] < o.fbpos[n]) o.bpos[n] = o.fbpos[n];
+      }
+    } else if (o.mdir[n] == 2) {
+      if (t2 - o.tmove[n] > 1.e-5 && o.fbpos[n] - o.bpos[n] > 1.e-5) {
+        o.bpos[n] = o.bpos[n] + ht * o.bspeed[n];
+        if (o.bpos[n] > o.fbpos[n]) o.bpos[n] = o.fbpos[n];
+      }
+    }
+  }
+  xs_updt(o);
+  o.sigrp = o.sigr;
+  for (int g = 1; g <= o.ng; ++g)
+    for (int n = 1; n <= o.nnod; ++n)
+      o.N2(o.sigr, n, g) = o.N2(o.sigr, n, g) + 1.0 / (o.sth * o.velo[g - 1] * ht) + o.N2(o.omeg, n, g) / o.velo[g - 1];
+  o.ft = o.f0;
+  o.fst = o.fs0;
+  const bool maxi = outer_tr(o, ht);
+  upden(o, ht);
+  const double tpow2 = powtot(o);
+  const double rho = reactivity(o, af.data(), o.sigrp.data());
+  return TransRec{t2, rho / o.ctbeta, tpow2 / tpow1, maxi ? 1 : 0, o.last_outers};
+}
+
+// rod_eject (mod_trans.f90:17-160): the steady state (k forced to one),
+// the adjoint weight, initial precursors, then the two time-step phases.
+// Record 0 is t = 0 with rho in absolute units, as the reference prints it.
+static std::vector<TransRec> rod_eject(Ora& o, int max_steps) {
+  const int N = o.nnod, G = o.ng;
+  o.omeg.assign((size_t)N * G, 0.0);
+  o.Lt.assign((size_t)N * G, 0.0);
+  o.dfis.assign(N, 0.0);
+  xs_updt(o);
+  outer(o, false, 0, 0);
+  if (std::fabs(o.Ke - 1.0) > 1.e-5) kne1(o);
+  outer(o, true, 0, 0);
+  const std::vector<double> af = o.f0;
+  outer(o, false, 0, 0);
+  ipden(o);
+  const double tpow1 = powtot(o);
+  o.tbeta.assign(o.nmat, 0.0);
+  for (int n = 0; n < o.nmat; ++n) {
+    for (int j = 0; j < Ora::nf; ++j) o.tbeta[n] = o.tbeta[n] + o.ibeta[j];
+    o.ctbeta = o.tbeta[0];
+  }
+  std::vector<TransRec> out;
+  out.push_back(TransRec{0.0, reactivity(o, af.data(), o.sigr.data()), 1.0, 0, o.last_outers});
+  const long imax1 = std::lround(o.tdiv / o.tstep1);
+  auto more = [&]() { return max_steps < 0 || (long)out.size() <= max_steps; };
+  for (long i = 1; i <= imax1 && more(); ++i) {
+    const double t2 = (double)(float)i * o.tstep1;
+    for (size_t q = 0; q < o.omeg.size(); ++q)
+      o.omeg[q] = (i > 1 && o.bextr) ? std::log(o.f0[q] / o.ft[q]) / o.tstep1 : 0.0;
+    out.push_back(trans_calc(o, o.tstep1, af, tpow1, t2));
+  }
+  const long imax2 = std::lround((o.ttot - o.tdiv) / o.tstep2);
+  for (long i = 1; i <= imax2 && more(); ++i) {
+    const double t2 = o.tdiv + (double)(float)i * o.tstep2;
+    for (size_t q = 0; q < o.omeg.size(); ++q)
+      o.omeg[q] = o.bextr ? std::log(o.f0[q] / o.ft[q]) / o.tstep2 : 0.0;
+    out.push_back(trans_calc(o, o.tstep2, af, tpow1, t2));
+  }
+  return out;
+}
+
 thread_local std::string g_err;
 
 template <class F>
@@ -1929,6 +2216,12 @@ static std::vector<double>* dvec(Ora* o, const char* name) {
   if (s == "df") return &o->df;
   if (s == "D") return &o->D;
   if (s == "sigr") return &o->sigr;
+  if (s == "exsrc") return &o->exsrc;
+  if (s == "Lt") return &o->Lt;
+  if (s == "sigrp") return &o->sigrp;
+  if (s == "ft") return &o->ft;
+  if (s == "s0") return &o->s0;
+  if (s == "c0") return &o->c0;
   if (s == "sigtr") return &o->sigtr;
   if (s == "siga") return &o->siga;
   if (s == "nuf") return &o->nuf;
@@ -2042,6 +2335,22 @@ int ora_cbsearch(void* h, double* bc, double* k, int* outers, int cap, int* coun
   return guard(o, [&] { *count = cbsearch(*o, bc, k, outers, cap); });
 }
 
+// The rod ejection transient: up to cap records (t, reactivity in dollars
+// (absolute at t = 0), relative power, nout reached, outers of the step);
+// max_steps >= 0 stops after that many time steps.
+int ora_rodeject(void* h, double* t, double* rho, double* pw, int* maxi, int* outers, int cap, int max_steps,
+                 int* count) {
+  Ora* o = (Ora*)h;
+  return guard(o, [&] {
+    const std::vector<TransRec> r = rod_eject(*o, max_steps);
+    const int n = (int)std::min((size_t)cap, r.size());
+    for (int i = 0; i < n; ++i) {
+      t[i] = r[i].t; rho[i] = r[i].rho; pw[i] = r[i].pow; maxi[i] = r[i].maxi; outers[i] = r[i].outers;
+    }
+    *count = (int)r.size();
+  });
+}
+
 int ora_xs_updt_at(void* h, double bcon) { Ora* o = (Ora*)h; return guard(o, [&] { xs_updt_at(*o, bcon); }); }
 
 int ora_outer(void* h, int adj, int popt, int max_outers) {
@@ -2144,6 +2453,7 @@ int ora_get_int(void* h, const char* name) {
   if (s == "kern") return o->kern == " FDM" ? 0 : (o->kern == " PNM" ? 1 : 2);
   if (s == "adjoint") return o->mode == "ADJOINT" ? 1 : 0;
   if (s == "bcsearch") return o->mode == "BCSEARCH" ? 1 : 0;
+  if (s == "rodeject") return o->mode == "RODEJECT" ? 1 : 0;
   if (s == "im") return o->im;
   if (s == "jm") return o->jm;
   if (s == "km") return o->km;

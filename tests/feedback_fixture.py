@@ -11,8 +11,8 @@ from conftest import GOLDEN
 KERNS = {0: "FDM", 1: "PNM", 2: "SANM"}
 
 
-def fixture():
-    return np.load(os.path.join(GOLDEN, "decks", "CBCsearch.npz"))
+def fixture(name="CBCsearch"):
+    return np.load(os.path.join(GOLDEN, "decks", name + ".npz"))
 
 
 def unpack_changes(a):
@@ -35,6 +35,13 @@ def deck_from_fixture(fx, mode="BCSEARCH"):
                    nnod=nn, ix=np.asarray(fx["ix"]), iy=np.asarray(fx["iy"]), iz=np.asarray(fx["iz"]),
                    mat=np.asarray(fx["mat"]), dc=F(fx["dc"], (nn, ng, 6)), nin=nin, nout=nout, serc=serc, ferc=ferc,
                    nac=nac, nupd=nupd, coreh=float(fx["coreh"]), bcbcs=True)
+    if "tr_scal" in fx:
+        ttot, tstep1, tdiv, tstep2, theta, extr = (float(v) for v in fx["tr_scal"])
+        dk.bcbcs = False
+        dk.trans = dict(fbpos=np.asarray(fx["tr_fbpos"]), tmove=np.asarray(fx["tr_tmove"]),
+                        bspeed=np.asarray(fx["tr_bspeed"]), mdir=np.asarray(fx["tr_mdir"]), ttot=ttot, tstep1=tstep1,
+                        tdiv=tdiv, tstep2=tstep2, beta=np.asarray(fx["tr_beta"]), lamb=np.asarray(fx["tr_lamb"]),
+                        velo=np.asarray(fx["tr_velo"]), theta=theta, extr=bool(extr))
     for nm_ in (str(s) for s in fx["fb_names"]):
         ch = unpack_changes(fx["fb_%s_ch" % nm_])
         if nm_ == "crod":
