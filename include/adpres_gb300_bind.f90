@@ -40,6 +40,19 @@ module adpres_gb300_bind
     real(c_double) :: device_ms
   end type
 
+  type, bind(C) :: adp_trans_opts
+    integer(c_int) :: nf
+    type(c_ptr)    :: beta, lambda, velo   ! double[nf], [nf], [ng]
+    real(c_double) :: theta
+    integer(c_int) :: extr
+  end type
+
+  type, bind(C) :: adp_trans_result
+    real(c_double) :: rho, rho_dollar, relpow, power
+    integer(c_int) :: maxi, outers
+    real(c_double) :: device_ms
+  end type
+
   interface
     integer(c_int) function adp_create(geom, opts, h) bind(C, name="adp_create")
       import :: adp_geom, adp_opts, c_int, c_ptr
@@ -174,6 +187,23 @@ module adpres_gb300_bind
       integer(c_int), value :: nmat, nf
       integer(c_int), intent(in) :: mat(*)
       real(c_double), intent(out) :: beta
+    end function
+
+    ! rod ejection transient (mod_trans.f90:17-640)
+    integer(c_int) function adp_trans_init(h, opts, af, r0) bind(C, name="adp_trans_init")
+      import :: c_int, c_ptr, c_double, adp_trans_opts, adp_trans_result
+      type(c_ptr), value :: h
+      type(adp_trans_opts), intent(in) :: opts
+      real(c_double), intent(in) :: af(*)
+      type(adp_trans_result), intent(out) :: r0
+    end function
+
+    integer(c_int) function adp_trans_step(h, dt, omeg_mode, r) bind(C, name="adp_trans_step")
+      import :: c_int, c_ptr, c_double, adp_trans_result
+      type(c_ptr), value :: h
+      real(c_double), value :: dt
+      integer(c_int), value :: omeg_mode
+      type(adp_trans_result), intent(out) :: r
     end function
   end interface
 
