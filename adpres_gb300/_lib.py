@@ -80,6 +80,17 @@ class AdpTransResult(ctypes.Structure):
                 ("device_ms", ctypes.c_double)]
 
 
+ADP_FB_BORON, ADP_FB_FUEL_TEMP, ADP_FB_MOD_TEMP, ADP_FB_COOL_DENS = 0, 1, 2, 3
+
+
+class AdpFbTables(ctypes.Structure):
+    _fields_ = [("nmat", ctypes.c_int), ("xsigtr", _dp), ("xsiga", _dp), ("xnuf", _dp), ("xsigf", _dp),
+                ("xsigs", _dp), ("chi", _dp), ("mat", _ip), ("dc", _dp), ("nstate", ctypes.c_int),
+                ("kind", _ip), ("ref", _dp), ("dsig", ctypes.POINTER(_dp)), ("nbank", ctypes.c_int),
+                ("rsig", ctypes.POINTER(_dp)), ("bank", _ip), ("coreh", ctypes.c_double),
+                ("pos0", ctypes.c_double), ("ssize", ctypes.c_double)]
+
+
 class AdpBatchConfig(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int), ("max_team", ctypes.c_int), ("grain", ctypes.c_double),
                 ("blocks_per_sm", ctypes.c_int), ("use_graph", ctypes.c_int)]
@@ -100,6 +111,8 @@ SIGNATURES = {
     "adp_set_xs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp]),
     "adp_xs_updt": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp]),
     "adp_xs_updt_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp]),
+    "adp_fb_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpFbTables)]),
+    "adp_fb_updt": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
     "adp_outer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(AdpReport)]),
     "adp_get_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
     "adp_set_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),

@@ -66,6 +66,7 @@ class Core:
         self.h = h
         self.nout = int(nout) if nout and nout > 0 else 500
         self.precision = precision
+        self._fb_cards = []
 
     @classmethod
     def from_deck(cls, dk, precision="fp64", **over):
@@ -76,9 +77,8 @@ class Core:
         core.deck = dk
         if getattr(dk, "feedback", None):
             # XS_updt(bcon, ftem, mtem, cden, bpos) with the deck's feedback cards
-            from .feedback import xs_update
-            t = xs_update(dk)
-            core.xs_updt_nodes(t["sigtr"], t["siga"], t["nuf"], t["sigf"], dk.chi, dk.mat, t["sigs"], dk.dc)
+            core.fb_set(dk)
+            core.fb_updt(dk)
         else:
             core.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
         return core
@@ -123,6 +123,59 @@ class Core:
         s = _fortran(sigs)
         d = None if dc is None else _fortran(dc)
         self._check(self.L.adp_xs_updt_nodes(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
+
+    def fb_set(self, dk):
+        """Upload the deck's feedback tables (adp_fb_set): the material
+        tables, the change tables of its state cards (in the reference's
+        order boron, fuel temperature, moderator temperature, coolant
+        density) and of %CROD, the bank of every node's column."""
+        from .feedback import KEYS, STATE_CARDS
+        fb = dk.feedback or {}
+        keep = []
+
+        def arr(a, dt=np.float64, fortran=True):
+            a = _fortran(a, dt) if fortran else _c(a, dt)
+            keep.append(a)
+            return a
+
+        def table_set(tabs):
+            return [dptr(arr(tabs[k])) for k in KEYS]
+
+        t = _lib.AdpFbTables()
+        t.nmat = int(np.asarray(dk.chi).shape[0])
+        base = dict(sigtr=dk.xsigtr, siga=dk.xsiga, nuf=dk.xnuf, sigf=dk.xsigf, sigs=dk.xsigs)
+        t.xsigtr, t.xsiga, t.xnuf, t.xsigf, t.xsigs = table_set(base)
+        t.chi = dptr(arr(dk.chi))
+        t.mat = iptr(arr(dk.mat, np.int32, False))
+        t.dc = None if dk.dc is None else dptr(arr(dk.dc))
+        cards = [(nm, kind) for nm, kind in STATE_CARDS if nm in fb]
+        t.nstate = len(cards)
+        if cards:
+            t.kind = iptr(arr([kind for _, kind in cards], np.int32, False))
+            t.ref = dptr(arr([fb[nm]["ref"] for nm, _ in cards], np.float64, False))
+            ptrs = [p for nm, _ in cards for p in table_set(fb[nm]["changes"])]
+            t.dsig = (_lib._dp * len(ptrs))(*ptrs)
+        if "crod" in fb:
+            cr = fb["crod"]
+            t.nbank = int(cr["nb"])
+            t.rsig = (_lib._dp * 5)(*table_set(cr["changes"]))
+            bank = np.asarray(cr["fbmap"])[np.asarray(dk.ix) - 1, np.asarray(dk.iy) - 1]
+            t.bank = iptr(arr(bank, np.int32, False))
+            t.coreh, t.pos0, t.ssize = float(dk.coreh), float(cr["pos0"]), float(cr["ssize"])
+        self._check(self.L.adp_fb_set(self.h, ctypes.byref(t)))
+        self._fb_cards = [nm for nm, _ in cards]
+
+    def fb_updt(self, dk, bcon=None, bpos=None):
+        """XS_updt on the device from the tables of fb_set at the deck's state
+        values (boron `bcon` when given) and bank positions (`bpos` when given)."""
+        fb = dk.feedback or {}
+        vals = [float(bcon) if (nm == "bcon" and bcon is not None) else float(fb[nm]["value"])
+                for nm in self._fb_cards]
+        st = _c(vals) if vals else None
+        bp = None
+        if "crod" in fb:
+            bp = _c(fb["crod"]["bpos"] if bpos is None else bpos)
+        self._check(self.L.adp_fb_updt(self.h, dptr(st), dptr(bp)))
 
     def set_xs(self, D, sigr, nuf, sigf, chi, mat, sigs, dc=None):
         nmat = int(np.asarray(chi).shape[0])

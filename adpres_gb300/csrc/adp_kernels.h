@@ -169,7 +169,33 @@ struct XsBox {
   double* sigs;
 };
 
+// Feedback update of XS_updt on the device (transfer.cu).  A table set is
+// sigtr, siga, nuf, sigf (nmat, G) and sigs (nmat, G, G), Fortran order,
+// packed one after another: `tq` doubles per set, table q at off[q].
+constexpr int kFbMaxState = 4;
+constexpr int kFbMaxBanks = 64;
+struct FbParams {
+  int nmat, G, nn, nst, nb, plane;
+  long long NB;
+  long long tq;             // doubles in one table set
+  long long off[5];         // start of each table in a set
+  const double* base;       // the material tables
+  const double* dsig;       // [nst] change sets
+  const double* rsig;       // rod change set (nb > 0)
+  double* tab;              // the material tables after the state changes
+  const double* chi;        // (nmat, G)
+  const int* mat;           // (nn) 1-based
+  const int* bank;          // (nn) 0 = unrodded column
+  const int* act;           // (nn) box index
+  double dv[kFbMaxState];   // state change of each card
+  int tip[kFbMaxBanks];     // plane of the rod tip (-1: none holds it)
+  double vf[kFbMaxBanks];   // rodded fraction of that plane
+  XsBox X;
+  int* flags;
+};
+
 // Launchers (return the launch error, if any)
+cudaError_t launch_fb_updt(const FbParams& P, cudaStream_t st);
 cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st);
 cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st);
 cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st);

@@ -242,6 +242,7 @@ adp_status adp_destroy(adp_handle* h) {
   if (h->react_base) cudaFree(h->react_base);
   if (h->trans_base) cudaFree(h->trans_base);
   if (h->xfer_base) cudaFree(h->xfer_base);
+  if (h->fb_base) cudaFree(h->fb_base);
   if (h->h_ctl) cudaFreeHost(h->h_ctl);
   for (cudaEvent_t e : {h->e0, h->e1, h->e2, h->e3})
     if (e) cudaEventDestroy(e);
@@ -721,6 +722,155 @@ adp_status adp_xs_updt(adp_handle* h, int nmat, const double* xsigtr, const doub
   if ((s = put_dc(h, X, dc)) != ADP_OK) return s;
   h->nmat = nmat;
   if ((s = xs_flags(h, X, chi_neg)) != ADP_OK) return s;
+  return xs_finish(h);
+}
+
+// Feedback tables (mod_xsec.f90:11-46 with its state and rod cards) resident
+// on the device: base set, nst change sets, the rod set, the working set,
+// chi, material and bank numbers in one allocation.
+adp_status adp_fb_set(adp_handle* h, const adp_fb_tables* t) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  h->fb_ready = false;
+  if (!t) return fail(h, ADP_ERR_INPUT, "adp_fb_set: null tables");
+  const int nn = h->nnod, G = h->ng, nmat = t->nmat;
+  if (nmat < 1 || !t->xsigtr || !t->xsiga || !t->xnuf || !t->xsigf || !t->xsigs || !t->chi || !t->mat)
+    return fail(h, ADP_ERR_INPUT, "adp_fb_set: null base table or no materials");
+  if (t->nstate < 0 || t->nstate > ADP_FB_MAX_STATE || (t->nstate > 0 && (!t->kind || !t->ref || !t->dsig)))
+    return fail(h, ADP_ERR_INPUT, "adp_fb_set: 0..4 state cards with kinds, references and change tables");
+  if (t->nbank < 0 || t->nbank > ADP_FB_MAX_BANKS || (t->nbank > 0 && (!t->rsig || !t->bank)))
+    return fail(h, ADP_ERR_INPUT, "adp_fb_set: 0..64 rod banks with change tables and the bank map");
+  for (int s = 0; s < t->nstate; ++s) {
+    if (t->kind[s] < ADP_FB_BORON || t->kind[s] > ADP_FB_COOL_DENS)
+      return fail(h, ADP_ERR_INPUT, "adp_fb_set: unknown state kind");
+    for (int q = 0; q < 5; ++q)
+      if (!t->dsig[5 * s + q]) return fail(h, ADP_ERR_INPUT, "adp_fb_set: null state change table");
+  }
+  for (int q = 0; q < 5 && t->nbank > 0; ++q)
+    if (!t->rsig[q]) return fail(h, ADP_ERR_INPUT, "adp_fb_set: null rod change table");
+  adp_status s = check_mat(h, nmat, t->mat);
+  if (s != ADP_OK) return s;
+  if (t->nbank > 0)
+    for (int n = 0; n < nn; ++n)
+      if (t->bank[n] < 0 || t->bank[n] > t->nbank) return fail(h, ADP_ERR_INPUT, "adp_fb_set: bank number out of range");
+  const size_t t1 = (size_t)G * nmat, tq = 4 * t1 + t1 * G;
+  const size_t nsets = 2 + (size_t)t->nstate + (t->nbank > 0 ? 1 : 0);   // base, work, states, rods
+  size_t need = 0;
+  auto add = [&](size_t b) { need += ((b + 255) & ~(size_t)255) + 256; };
+  add(nsets * tq * 8);
+  add(t1 * 8);
+  add((size_t)nn * 4);
+  add((size_t)nn * 4);
+  if (h->fb_size < need) {
+    if (h->fb_base) CK(cudaFree(h->fb_base));
+    h->fb_base = nullptr;
+    h->fb_size = 0;
+    CK(cudaMalloc((void**)&h->fb_base, need));
+    h->fb_size = need;
+  }
+  DevArena A;
+  A.base = h->fb_base;
+  A.size = h->fb_size;
+  double* sets = (double*)A.take(nsets * tq * 8);
+  h->d_fb_base = sets;
+  h->d_fb_tab = sets + tq;
+  h->d_fb_dsig = sets + 2 * tq;
+  h->d_fb_rsig = t->nbank > 0 ? sets + (2 + (size_t)t->nstate) * tq : nullptr;
+  h->d_fb_chi = (double*)A.take(t1 * 8);
+  h->d_fb_mat = (int*)A.take((size_t)nn * 4);
+  h->d_fb_bank = (int*)A.take((size_t)nn * 4);
+  auto put_set = [&](double* dst, const double* const* src) -> cudaError_t {
+    for (int q = 0; q < 4; ++q) {
+      cudaError_t e = cudaMemcpyAsync(dst + q * t1, src[q], t1 * 8, cudaMemcpyHostToDevice, h->st);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaMemcpyAsync(dst + 4 * t1, src[4], t1 * G * 8, cudaMemcpyHostToDevice, h->st);
+  };
+  const double* base[5] = {t->xsigtr, t->xsiga, t->xnuf, t->xsigf, t->xsigs};
+  CK(put_set(h->d_fb_base, base));
+  for (int k = 0; k < t->nstate; ++k) CK(put_set(h->d_fb_dsig + k * tq, t->dsig + 5 * k));
+  if (t->nbank > 0) CK(put_set(h->d_fb_rsig, t->rsig));
+  CK(cudaMemcpyAsync(h->d_fb_chi, t->chi, t1 * 8, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->d_fb_mat, t->mat, (size_t)nn * 4, cudaMemcpyHostToDevice, h->st));
+  if (t->nbank > 0) CK(cudaMemcpyAsync(h->d_fb_bank, t->bank, (size_t)nn * 4, cudaMemcpyHostToDevice, h->st));
+  else CK(cudaMemsetAsync(h->d_fb_bank, 0, (size_t)nn * 4, h->st));
+  Xfer X;
+  if ((s = xfer_reserve(h, nmat, X)) != ADP_OK) return s;
+  if ((s = put_dc(h, X, t->dc)) != ADP_OK) return s;
+  CK(cudaStreamSynchronize(h->st));
+  h->fb_chi_neg = chi_negative(h, nmat, t->chi);
+  h->fb_nmat = nmat;
+  h->fb_nst = t->nstate;
+  h->fb_nb = t->nbank;
+  for (int k = 0; k < t->nstate; ++k) {
+    h->fb_kind[k] = t->kind[k];
+    h->fb_ref[k] = t->ref[k];
+  }
+  h->fb_coreh = t->coreh;
+  h->fb_pos0 = t->pos0;
+  h->fb_ssize = t->ssize;
+  h->fb_ready = true;
+  return ADP_OK;
+}
+
+adp_status adp_fb_updt(adp_handle* h, const double* state, const double* bpos) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!h->fb_ready) return fail(h, ADP_ERR_STATE, "adp_fb_updt: no feedback tables (adp_fb_set)");
+  if ((h->fb_nst > 0 && !state) || (h->fb_nb > 0 && !bpos)) return fail(h, ADP_ERR_INPUT, "adp_fb_updt: null state or bank positions");
+  const int G = h->ng, nmat = h->fb_nmat;
+  const long long t1 = (long long)G * nmat;
+  FbParams P;
+  std::memset(&P, 0, sizeof P);
+  P.nmat = nmat;
+  P.G = G;
+  P.nn = h->nnod;
+  P.nst = h->fb_nst;
+  P.nb = h->fb_nb;
+  P.plane = h->plane;
+  P.NB = h->NB;
+  P.tq = 4 * t1 + t1 * G;
+  for (int q = 0; q < 5; ++q) P.off[q] = q * t1;
+  P.base = h->d_fb_base;
+  P.dsig = h->d_fb_dsig;
+  P.rsig = h->d_fb_rsig;
+  P.tab = h->d_fb_tab;
+  P.chi = h->d_fb_chi;
+  P.mat = h->d_fb_mat;
+  P.bank = h->d_fb_bank;
+  P.act = h->d_act;
+  // the state changes of bcon_updt, ftem_updt (square roots), mtem_updt, cden_updt
+  for (int k = 0; k < h->fb_nst; ++k)
+    P.dv[k] = h->fb_kind[k] == ADP_FB_FUEL_TEMP ? std::sqrt(state[k]) - std::sqrt(h->fb_ref[k]) : state[k] - h->fb_ref[k];
+  // crod_updt (mod_xsec.f90:239-263): the rod tip of each bank, walking
+  // down from the top of the core; the plane holding it and its rodded
+  // fraction (no plane: every plane below the top is rodded).  The product
+  // is held apart so that it is rounded on its own, as the reference's is.
+  for (int b = 0; b < h->fb_nb; ++b) {
+    volatile double step = bpos[b] * h->fb_ssize;
+    const double rodh = (h->fb_coreh - h->fb_pos0) - step;
+    double dum = 0.0;
+    P.tip[b] = -1;
+    P.vf[b] = 0.0;
+    for (int k = h->nzz - 1; k >= 0; --k) {
+      if (rodh >= dum && rodh <= dum + h->zdel[k]) {
+        P.tip[b] = k;
+        P.vf[b] = (rodh - dum) / h->zdel[k];
+        break;
+      }
+      dum = dum + h->zdel[k];
+    }
+  }
+  Xfer X;
+  adp_status s = xfer_reserve(h, nmat, X);
+  if (s != ADP_OK) return s;
+  h->fwd_ok = false;
+  CK(cudaMemsetAsync(X.flags, 0, sizeof(int), h->st));
+  P.X = xs_box(h);
+  P.flags = X.flags;
+  CK(launch_fb_updt(P, h->st));
+  h->nmat = nmat;
+  if ((s = xs_flags(h, X, h->fb_chi_neg)) != ADP_OK) return s;
   return xs_finish(h);
 }
 

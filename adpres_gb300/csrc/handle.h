@@ -94,6 +94,16 @@ struct adp_handle {
   double* d_fsa[2] = {nullptr, nullptr};
   adp::OuterCtl* d_ctla = nullptr;
   double *d_sens = nullptr, *d_spart = nullptr;
+  // feedback tables of adp_fb_set, kept until the next call
+  char* fb_base = nullptr;
+  size_t fb_size = 0;
+  bool fb_ready = false, fb_chi_neg = false;
+  int fb_nmat = 0, fb_nst = 0, fb_nb = 0;
+  int fb_kind[4] = {0, 0, 0, 0};
+  double fb_ref[4] = {0, 0, 0, 0};
+  double fb_coreh = 0.0, fb_pos0 = 0.0, fb_ssize = 0.0;
+  double *d_fb_base = nullptr, *d_fb_dsig = nullptr, *d_fb_rsig = nullptr, *d_fb_tab = nullptr, *d_fb_chi = nullptr;
+  int *d_fb_mat = nullptr, *d_fb_bank = nullptr;
   // rod ejection transient (trans.cu), allocated by adp_trans_init
   char* trans_base = nullptr;
   bool trans_ready = false;

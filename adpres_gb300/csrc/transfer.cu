@@ -96,7 +96,77 @@ __global__ void k_base_updt(XsTables T, const int* __restrict__ mat, const int* 
   if (threadIdx.x == 0 && (nuf_bad || sigs_bad)) atomicOr(flags, (nuf_bad ? 1 : 0) | (sigs_bad ? 4 : 0));
 }
 
+// The state changes of XS_updt on the material tables (bcon_updt, ftem_updt,
+// mtem_updt, cden_updt, mod_xsec.f90:394-521), one entry per thread:
+// x = x + dx * dv card by card, each product and sum rounded on its own as
+// the reference's separate statements are.
+__global__ void k_fb_state(FbParams P) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < P.tq;
+       q += (long long)gridDim.x * blockDim.x) {
+    double v = P.base[q];
+    for (int s = 0; s < P.nst; ++s) v = __dadd_rn(v, __dmul_rn(P.dsig[s * P.tq + q], P.dv[s]));
+    P.tab[q] = v;
+  }
+}
+
+// base_updt of the changed tables and crod_updt (mod_xsec.f90:172-195,
+// :230-303), one (node, group) per thread.  A node of bank b in a plane
+// above the rod tip takes x + dx, the plane of the tip x + w dx; in rodded
+// columns negative siga, nuf, sigf and sigs become 0.  flags as
+// k_base_updt: 1 a negative nu*fission, 4 a negative scattering entry.
+__global__ void k_fb_nodes(FbParams P) {
+  const long long total = (long long)P.nn * P.G;
+  const int G = P.G, nmat = P.nmat;
+  int bad = 0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(q % P.nn), g = (int)(q / P.nn);
+    const int m = P.mat[n] - 1;
+    const int a = P.act[n];
+    const long long b = (long long)g * P.NB + a;
+    const int bk = P.bank[n];
+    int mode = 0;   // 0 no rod, 1 fully rodded, 2 the plane of the tip
+    double w = 0.0;
+    if (bk > 0) {
+      const int z = a / P.plane, kt = P.tip[bk - 1];
+      mode = z > kt ? 1 : (z == kt ? 2 : 0);
+      w = P.vf[bk - 1];
+    }
+    auto val = [&](int tq, long long i, bool clamp) -> double {
+      double v = P.tab[P.off[tq] + i];
+      if (mode == 1) v = __dadd_rn(v, P.rsig[P.off[tq] + i]);
+      else if (mode == 2) v = __dadd_rn(v, __dmul_rn(w, P.rsig[P.off[tq] + i]));
+      if (clamp && bk > 0 && v < 0.0) v = 0.0;
+      return v;
+    };
+    const long long t = (long long)g * nmat + m;
+    P.X.chin[b] = P.chi[t];
+    P.X.sigtr[b] = val(0, t, false);
+    P.X.siga[b] = val(1, t, true);
+    const double nf = val(2, t, true);
+    bad |= nf < 0.0 ? 1 : 0;
+    P.X.nuf[b] = nf;
+    P.X.sigf[b] = val(3, t, true);
+    for (int h = 0; h < G; ++h) {
+      const double v = val(4, m + (long long)nmat * (g + (long long)G * h), true);
+      bad |= v < 0.0 ? 4 : 0;
+      P.X.sigs[((long long)g * G + h) * P.NB + a] = v;
+    }
+  }
+  const int nuf_bad = __syncthreads_or(bad & 1);
+  const int sigs_bad = __syncthreads_or(bad & 4);
+  if (threadIdx.x == 0 && (nuf_bad || sigs_bad)) atomicOr(P.flags, (nuf_bad ? 1 : 0) | (sigs_bad ? 4 : 0));
+}
+
 }  // namespace
+
+cudaError_t launch_fb_updt(const FbParams& P, cudaStream_t st) {
+  k_fb_state<<<xfer_blocks(P.tq), kXferThreads, 0, st>>>(P);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_fb_nodes<<<xfer_blocks((long long)P.nn * P.G), kXferThreads, 0, st>>>(P);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_nodes_to_box(const double* src, double* dst, const int* act, int nn, int A, int B,
                                 long long dstride, int chk, int* flags, cudaStream_t st) {

@@ -10,6 +10,12 @@ node holding the tip a volume fraction of them, and negative siga, nuf,
 sigf and sigs of rodded columns become 0.  The result goes to the device
 through adp_xs_updt_nodes, which forms D and sigr and checks them.
 
+``Core.fb_set``/``Core.fb_updt`` run the same update on the device from
+resident tables (adp_fb_set, adp_fb_updt) with the same operations in the
+same order, so both give the same node tables to the bit; the searches and
+the transient use the device form and hand over only the state values and
+the bank positions.
+
 ``cbsearch`` is th::cbsearch (mod_th.f90:752-837): a secant search of the
 boron concentration that makes k = 1, each step an XS update and a
 warm-started outer(0) on the GPU.
@@ -20,9 +26,13 @@ import math
 
 import numpy as np
 
-from ._lib import AdpError, ADP_ERR_INPUT, ADP_ERR_MAXOUTER
+from ._lib import (AdpError, ADP_ERR_INPUT, ADP_ERR_MAXOUTER, ADP_FB_BORON, ADP_FB_COOL_DENS,
+                   ADP_FB_FUEL_TEMP, ADP_FB_MOD_TEMP)
 
 KEYS = ("sigtr", "siga", "nuf", "sigf", "sigs")
+# the state cards in the order XS_updt applies them (mod_xsec.f90:24-40)
+STATE_CARDS = (("bcon", ADP_FB_BORON), ("ftem", ADP_FB_FUEL_TEMP), ("mtem", ADP_FB_MOD_TEMP),
+               ("cden", ADP_FB_COOL_DENS))
 
 
 def _rod_tip(rodh, zdel):
@@ -104,10 +114,10 @@ def cbsearch(core, dk=None, max_steps=20):
     fb = dk.feedback["bcon"]
     steps = []
     core.cbsearch_device_ms = 0.0
+    core.fb_set(dk)
 
     def solve(b):
-        t = xs_update(dk, b)
-        core.xs_updt_nodes(t["sigtr"], t["siga"], t["nuf"], t["sigf"], dk.chi, dk.mat, t["sigs"], dk.dc)
+        core.fb_updt(dk, bcon=b)
         rep = core.outer(popt=0, trace=False)
         core.cbsearch_device_ms += rep.device_ms
         steps.append((b, rep.keff, rep.outers))

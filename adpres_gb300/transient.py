@@ -7,9 +7,10 @@ KNE1 when k is not one (nu*sigf and its rod change divided by k until
 adp_trans_init then forms the precursors, the initial power and the
 reactivity.  Each step of the two phases (tstep1 up to tdiv, tstep2 up to
 ttot) moves the banks as trans_calc does (mod_trans.f90:366-381), recomputes
-the node cross sections at the new positions (adpres_gb300.feedback) and
-runs adp_trans_step: removal of the step, external source, outer_tr on the
-GPU, precursors, power and reactivity.
+the node cross sections at the new positions on the device (adp_fb_updt
+from the tables of adp_fb_set) and runs adp_trans_step: removal of the
+step, external source, outer_tr on the GPU, precursors, power and
+reactivity.
 """
 from __future__ import annotations
 
@@ -19,7 +20,6 @@ import numpy as np
 
 from ._lib import AdpError, ADP_ERR_INPUT
 from .deck import _nint
-from .feedback import xs_update
 
 
 def _working_deck(dk):
@@ -58,9 +58,9 @@ def rod_eject(core, dk=None, max_steps=None):
     bpos = np.array(dk.feedback["crod"]["bpos"], dtype=np.float64)
 
     def set_xs():
-        t = xs_update(w, bpos=bpos)
-        core.xs_updt_nodes(t["sigtr"], t["siga"], t["nuf"], t["sigf"], w.chi, w.mat, t["sigs"], w.dc)
+        core.fb_updt(w, bpos=bpos)
 
+    core.fb_set(w)
     set_xs()
     rep = core.outer(popt=0, trace=False)
     if abs(rep.keff - 1.0) > 1.e-5:
@@ -70,6 +70,7 @@ def rod_eject(core, dk=None, max_steps=None):
             k = rep.keff
             w.xnuf = w.xnuf / k
             w.feedback["crod"]["changes"]["nuf"] = w.feedback["crod"]["changes"]["nuf"] / k
+            core.fb_set(w)
             set_xs()
             rep = core.outer(popt=0, trace=False)
             if abs(rep.keff - 1.0) < 1.e-5:

@@ -189,9 +189,10 @@ def _cbsearch_oracle(text):
 
 def cbsearch_leg(flush, steps=3):
     """th::cbsearch on the 34x34x22-node full core with boron, temperature,
-    density and control-rod feedback cards (seed 0): each search step is the
-    host cross-section update at the iterate, the upload of the node tables
-    and a warm-started outer on the GPU.  Timed end to end (wall clock,
+    density and control-rod feedback cards (seed 0): the feedback tables go
+    to the device once (adp_fb_set); each search step is the cross-section
+    update at the iterate on the device (adp_fb_updt) and a warm-started
+    outer on the GPU.  Timed end to end (wall clock,
     synchronised); device_ms sums the outer calls.  CPU baseline: the
     oracle's whole search on one host core."""
     import multiprocessing as mp
@@ -336,12 +337,13 @@ def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
     t = sum(ms) / len(ms) / 1e3
     conv = sum(r["converged"] for r in res)
     # individual FP64 single-core solves
-    dks = []
+    dks, outs64 = [], []
     t0 = time.perf_counter()
     for i in range(min(fp64_check, len(decks))):
         c = Core.from_deck(decks[i], precision="fp64")
         r = c.outer(trace=False)
         dks.append(abs(res[i]["keff"] - r.keff) / r.keff * 1e5)
+        outs64.append(r.outers)
         c.close()
     t_fp64 = time.perf_counter() - t0
     b.close()
@@ -362,7 +364,12 @@ def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
         "outers_mean": float(np.mean([r["outers"] for r in res])),
         "teams": sorted({r["team"] for r in res}),
         "dk_pcm_vs_fp64_single": {"max": float(max(dks)), "rms": float(np.sqrt(np.mean(np.square(dks)))),
-                                  "checked": len(dks), "fp64_single_s": t_fp64},
+                                  "checked": len(dks), "fp64_single_s": t_fp64,
+                                  "above_1pcm": int(sum(d > 1.0 for d in dks)),
+                                  "worst": {"member": int(np.argmax(dks)),
+                                            "outers_mixed": int(res[int(np.argmax(dks))]["outers"]),
+                                            "outers_fp64": int(outs64[int(np.argmax(dks))])},
+                                  "same_outers": int(sum(res[i]["outers"] == outs64[i] for i in range(len(dks))))},
         "cpu_baseline": {"value": cpu_rate, "unit": "solves/s", "cores": nproc, "kind": "port",
                          "sample": f"oracle full solves of the first {len(sample)} members, one process per host core, "
                                    f"wall {wall:.1f} s (mean {np.mean(tcpu):.1f} s per member)"},

@@ -160,6 +160,55 @@ adp_status adp_xs_updt_nodes(adp_handle* h, int nmat, const double* sigtr, const
                              const double* sigf, const double* chi, const int* mat, const double* sigs,
                              const double* dc);
 
+/* The feedback tables of XS_updt (mod_xsec.f90:11-46) kept on the device,
+ * so that a boron search or a transient step hands over a few numbers
+ * instead of node tables.  Per state variable a change table set for
+ * bcon_updt, ftem_updt, mtem_updt, cden_updt (:394-521) and one for the
+ * control rods (crod_updt, :230-303).  Every table set is sigtr, siga, nuf,
+ * sigf (nmat,ng) and sigs (nmat,ng,ng), in that order. */
+#define ADP_FB_MAX_STATE 4
+#define ADP_FB_MAX_BANKS 64
+typedef enum adp_fb_kind {
+  ADP_FB_BORON = 0,           /* x += dx (bcon - rbcon)                        */
+  ADP_FB_FUEL_TEMP = 1,       /* x += dx (sqrt(ftem) - sqrt(rftem))            */
+  ADP_FB_MOD_TEMP = 2,        /* x += dx (mtem - rmtem)                        */
+  ADP_FB_COOL_DENS = 3        /* x += dx (cden - rcden)                        */
+} adp_fb_kind;
+
+typedef struct adp_fb_tables {
+  int nmat;
+  const double* xsigtr;       /* base material tables (the %XSEC values)      */
+  const double* xsiga;
+  const double* xnuf;
+  const double* xsigf;
+  const double* xsigs;
+  const double* chi;          /* (nmat,ng)                                     */
+  const int* mat;             /* (nnod), 1-based                               */
+  const double* dc;           /* ADFs (nnod,ng,6) or NULL (all 1)              */
+  int nstate;                 /* 0..ADP_FB_MAX_STATE state cards, applied in
+                                 this order (the reference's: boron, fuel
+                                 temperature, moderator temperature, coolant
+                                 density)                                      */
+  const int* kind;            /* [nstate] adp_fb_kind                          */
+  const double* ref;          /* [nstate] reference values                     */
+  const double* const* dsig;  /* [5 * nstate]: state s, table q at 5 s + q     */
+  int nbank;                  /* 0 (no %CROD) .. ADP_FB_MAX_BANKS              */
+  const double* const* rsig;  /* [5] rod change tables                         */
+  const int* bank;            /* (nnod) bank of the node's column, 0 unrodded  */
+  double coreh, pos0, ssize;  /* core height, zero-step position, step size    */
+} adp_fb_tables;
+
+/* Uploads the tables; they stay until the next adp_fb_set or adp_destroy. */
+adp_status adp_fb_set(adp_handle* h, const adp_fb_tables* t);
+
+/* XS_updt at state values state[nstate] (bcon, ftem, ... as the tables'
+ * kinds) and bank positions bpos[nbank] (steps), on the device: the state
+ * changes on the material tables in card order, base_updt, the rods (a
+ * node above the rod tip gets x + dx, the node holding the tip x + w dx
+ * with w its rodded fraction, then negative siga, nuf, sigf and sigs of
+ * rodded columns become 0), then D, sigr and the checks as adp_xs_updt. */
+adp_status adp_fb_updt(adp_handle* h, const double* state, const double* bpos);
+
 /* -- solver --------------------------------------------------------------- */
 
 /* One call of outer(popt) (mode ADP_FORWARD) or outer_ad(popt) (ADP_ADJOINT)

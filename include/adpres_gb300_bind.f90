@@ -40,6 +40,19 @@ module adpres_gb300_bind
     real(c_double) :: device_ms
   end type
 
+  ! feedback tables (mod_xsec.f90:11-46, 230-303, 394-521); the pointers
+  ! are c_loc of the reference's arrays (xsigtr(nmat,ng), ..., the change
+  ! tables of each card, fbmap gathered per node)
+  type, bind(C) :: adp_fb_tables
+    integer(c_int) :: nmat
+    type(c_ptr)    :: xsigtr, xsiga, xnuf, xsigf, xsigs, chi, mat, dc
+    integer(c_int) :: nstate
+    type(c_ptr)    :: kind, ref, dsig          ! int[nstate], double[nstate], c_ptr[5*nstate]
+    integer(c_int) :: nbank
+    type(c_ptr)    :: rsig, bank               ! c_ptr[5], int[nnod]
+    real(c_double) :: coreh, pos0, ssize
+  end type
+
   type, bind(C) :: adp_trans_opts
     integer(c_int) :: nf
     type(c_ptr)    :: beta, lambda, velo   ! double[nf], [nf], [ng]
@@ -92,6 +105,18 @@ module adpres_gb300_bind
       integer(c_int), value :: nmat
       real(c_double), intent(in) :: sigtr(*), siga(*), nuf(*), sigf(*), chi(*), sigs(*), dc(*)
       integer(c_int), intent(in) :: mat(*)
+    end function
+
+    integer(c_int) function adp_fb_set(h, t) bind(C, name="adp_fb_set")
+      import :: c_int, c_ptr, adp_fb_tables
+      type(c_ptr), value :: h
+      type(adp_fb_tables), intent(in) :: t
+    end function
+
+    integer(c_int) function adp_fb_updt(h, state, bpos) bind(C, name="adp_fb_updt")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: state(*), bpos(*)   ! bcon, ftem, mtem, cden as given; bank positions
     end function
 
     integer(c_int) function adp_set_xs(h, nmat, D, sigr, nuf, sigf, chi, mat, sigs, dc) bind(C, name="adp_set_xs")

@@ -1,7 +1,8 @@
 """Critical boron search on the GPU (th::cbsearch, mod_th.f90:752-837)
-against the oracle's search on the sample deck CBCsearch: each step is the
-host XS_updt at the iterate, adp_xs_updt_nodes and a warm-started
-adp_outer(popt = 0) through the C ABI.
+against the oracle's search on the sample deck CBCsearch: each step is
+XS_updt at the iterate on the device (adp_fb_updt) and a warm-started
+adp_outer(popt = 0) through the C ABI.  The device update is checked
+against the host restatement of XS_updt (feedback.xs_update) to the bit.
 
 Bar, FP64 path: the same number of iterates; each iterate's boron within
 0.01 ppm and k within 0.1 pcm of the oracle's; final nodal power within
@@ -77,3 +78,68 @@ def test_cbsearch_synthetic_core_matches_oracle():
     np.testing.assert_allclose([r[0] for r in it], [r[0] for r in ref], rtol=0, atol=0.01)
     np.testing.assert_allclose([r[1] for r in it], [r[1] for r in ref], rtol=1e-6, atol=0)
     assert it[0][2] == ref[0][2]
+
+
+def _solve_pair(dk, bcon, bpos):
+    """The same solve with the node tables of the host restatement
+    (feedback.xs_update + adp_xs_updt_nodes) and of the device update
+    (adp_fb_set + adp_fb_updt)."""
+    a = Core.from_deck(dk, precision="fp64")
+    t = feedback.xs_update(dk, bcon, bpos)
+    a.xs_updt_nodes(t["sigtr"], t["siga"], t["nuf"], t["sigf"], dk.chi, dk.mat, t["sigs"], dk.dc)
+    ra = a.outer(popt=0, trace=False)
+    b = Core.from_deck(dk, precision="fp64")
+    b.fb_set(dk)
+    b.fb_updt(dk, bcon=bcon, bpos=bpos)
+    rb = b.outer(popt=0, trace=False)
+    return ra, a.power(), rb, b.power()
+
+
+@pytest.mark.parametrize("case", ["card", "partial", "all_in", "all_out", "clamped"])
+def test_device_feedback_update_is_bit_identical(case):
+    """adp_fb_updt forms the node tables with the operations of the host
+    restatement in the same order: the solves agree to the bit, at the card's
+    bank positions, with tips inside nodes, fully inserted and withdrawn
+    banks, and with rod changes that drive rodded entries negative (clamped
+    to 0)."""
+    from adpres_gb300 import deck, synth
+    dk = deck.parse(synth.boron_search_3d(1, n=9, planes=6))
+    cr = dk.feedback["crod"]
+    bpos = np.array(cr["bpos"], dtype=np.float64)
+    bcon = 1234.5
+    if case == "partial":
+        bpos = bpos * 0.37 + 3.3
+    elif case == "all_in":
+        bpos[:] = 0.0
+    elif case == "all_out":
+        bpos[:] = float(cr["nstep"])
+    elif case == "clamped":
+        # rodded nodes lose their fission and scattering entirely
+        ch = dict(cr["changes"])
+        ch["nuf"] = ch["nuf"] - 10.0 * np.abs(dk.xnuf).max()
+        ch["sigf"] = ch["sigf"] - 10.0 * np.abs(dk.xsigf).max()
+        ch["sigs"] = ch["sigs"] - 10.0 * np.abs(dk.xsigs).max()
+        cr["changes"] = ch
+        bpos = bpos * 0.5
+    ra, pa, rb, pb = _solve_pair(dk, bcon, bpos)
+    assert ra.outers == rb.outers
+    assert ra.keff == rb.keff
+    assert np.array_equal(pa, pb)
+
+
+def test_device_feedback_update_errors():
+    from adpres_gb300 import deck, synth
+    from adpres_gb300._lib import AdpError, ADP_ERR_INPUT, ADP_ERR_STATE
+    dk = deck.parse(synth.boron_search_3d(0, n=9, planes=6))
+    core = Core.from_deck(dk, precision="fp64")
+    fresh = Core(dk.nxx, dk.nyy, dk.nzz, dk.ix, dk.iy, dk.iz, dk.xdel, dk.ydel, dk.zdel, dk.bc, dk.ng)
+    with pytest.raises(AdpError) as e:
+        fresh.fb_updt(dk)
+    assert e.value.status == ADP_ERR_STATE
+    bad = dict(dk.feedback["crod"])
+    bad["fbmap"] = np.asarray(bad["fbmap"]).copy()
+    bad["fbmap"][0, 0] = int(bad["nb"]) + 1
+    dk.feedback["crod"] = bad
+    with pytest.raises(AdpError) as e:
+        core.fb_set(dk)
+    assert e.value.status == ADP_ERR_INPUT
