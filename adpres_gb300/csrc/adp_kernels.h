@@ -19,6 +19,12 @@ struct OuterParams {
   int ng, nin, nac, nupd, nout, adj, do_nodal, mixed;
   int smem_rows;              // > 0: rows per block of the matrix copy in shared memory
   int trans;                  // 1: outer_tr (mod_cmfd.f90:800-868): source wsrc fs + s0 + exsrc, no k update
+  // Source planes that hold a nonzero value at some node: bit g of src_nz
+  // for wsrc of group g, bit a*ng + c of sc_nz for sigs plane [a][c].  P0
+  // skips the terms of all-zero planes (adding an exact zero changes no
+  // bit of the sum); all ones when unknown.
+  unsigned src_nz;
+  unsigned long long sc_nz;
   const double* exsrc;        // [ng][NB] external source of the transient step (trans only)
   double serc, ferc;
   long long NBH;              // group stride of halo'd arrays
@@ -223,6 +229,11 @@ cudaError_t launch_box_to_nodes(const double* src, double* dst, const int* act, 
                                 long long sstride, cudaStream_t st);
 cudaError_t launch_fill_box(double* dst, const int* act, int nn, int ncomp, long long dstride, double v,
                             cudaStream_t st);
+// Planes of chi, nu*fission and sigs that hold a nonzero value at some
+// active node: out[0] bit g (chi), out[1] bit g (nuf), out[2] | out[3] << 32
+// bit g*G + h (sigs g -> h).  G <= 8; out must be zero on entry.
+cudaError_t launch_xs_nonzero(const double* chin, const double* nuf, const double* sigs, const int* act, int nn,
+                              int G, long long NB, unsigned* out, cudaStream_t st);
 cudaError_t launch_base_updt(const XsTables& T, const int* mat, const int* act, int nn, int nmat, int G, long long NB,
                              const XsBox& X, int* flags, cudaStream_t st);
 // batched solve (batch_k_*.cu): a cooperative launch of `blocks` blocks

@@ -622,6 +622,24 @@ NodalParams adp::nodal_params(adp_handle* h, int cmode) {
 extern "C" {
 
 static adp_status after_xs(adp_handle* h) {
+  h->chi_nz = h->nuf_nz = ~0u;
+  h->sigs_nz = ~0ull;
+  if (h->ng <= 8) {
+    // which source planes hold a nonzero value (the outer kernel skips the
+    // terms of all-zero planes: down-scatter-only cores, chi = 0 groups)
+    Xfer X;
+    adp_status s = xfer_reserve(h, std::max(h->nmat, 1), X);
+    if (s != ADP_OK) return s;
+    unsigned* m = reinterpret_cast<unsigned*>(X.flags) + 4;
+    unsigned hm[4] = {0, 0, 0, 0};
+    CK(cudaMemsetAsync(m, 0, sizeof hm, h->st));
+    CK(launch_xs_nonzero(h->d_chin, h->d_nuf, h->d_sigs, h->d_act, h->nnod, h->ng, h->NB, m, h->st));
+    CK(cudaMemcpyAsync(hm, m, sizeof hm, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->chi_nz = hm[0];
+    h->nuf_nz = hm[1];
+    h->sigs_nz = (unsigned long long)hm[2] | ((unsigned long long)hm[3] << 32);
+  }
   if (h->o.precision == ADP_MIXED) {
     const long long gn = (long long)h->ng * h->NB;
     CK(launch_split(h->d_chin, h->d_chin_h, h->d_chin_l, gn, h->st));
@@ -901,6 +919,8 @@ OuterParams adp::outer_params(adp_handle* h, int adj) {
     P.vv32[t] = h->d_vv32[t];
   }
   P.wsrc = adj ? h->d_nuf : h->d_chin;
+  P.src_nz = adj ? h->nuf_nz : h->chi_nz;
+  P.sc_nz = h->sigs_nz;
   P.wfis = adj ? h->d_chin : h->d_nuf;
   P.sigs = h->d_sigs;
   P.r = h->d_r;

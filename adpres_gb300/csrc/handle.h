@@ -116,6 +116,10 @@ struct adp_handle {
   double *d_c0 = nullptr, *d_omeg = nullptr, *d_ft = nullptr, *d_fst = nullptr, *d_sigrp = nullptr;
   double *d_Lt = nullptr, *d_exsrc = nullptr, *d_wtr = nullptr, *d_wnode = nullptr, *d_af = nullptr;
   double *d_velo = nullptr, *d_tpart = nullptr, *d_s0q = nullptr;
+  // planes of chi, nu*fission and sigs that are nonzero at some node
+  // (after_xs); all ones until known
+  unsigned chi_nz = ~0u, nuf_nz = ~0u;
+  unsigned long long sigs_nz = ~0ull;
   // state
   bool xs_set = false;
   bool fwd_ok = false;        // the flux is a converged forward solution of the current XS

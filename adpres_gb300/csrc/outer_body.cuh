@@ -88,13 +88,20 @@ struct RowsInFlight<true> { static constexpr int R = ADP_ROWS_MIXED; };
 // (barrier), extrapolation every nac outers (barrier), k update and the
 // convergence test, all in the same order as mod_cmfd.f90:479-495.
 //
-// MIXED: P0 is computed in FP64 with the FP64 matrix (the defect of the
-// current flux); the nin Krylov steps for the correction run with the FP32
-// matrix copy and FP32 vectors; each thread sums its rows' products in FP32
-// and the block and grid sums are FP64; the flux x stays FP64 and receives
-// FP32 increments.  Both forms avoid FP64 division in per-row work (the
-// source uses 1/k computed once per outer; RelE/RelEg divide only when a
-// candidate beats the running maximum).
+// MIXED: P0 forms the defect of the current flux in double-float (a
+// compensated dot product over the FP64 matrix as A32 + A32lo and the flux
+// and sources as hi + lo pairs); the nin Krylov steps for the correction run
+// with the FP32 matrix copy and FP32 vectors; the reductions are
+// double-float and the flux x, held as hi + lo, receives the FP32
+// increments.  Both forms avoid FP64 division in per-row work (the source
+// uses 1/k computed once per outer; RelE/RelEg divide only when a candidate
+// beats the running maximum).
+//
+// P0 leaves out the source terms of planes that are zero at every node
+// (P.src_nz, P.sc_nz: the up-scatter planes of a down-scatter-only core,
+// the chi = 0 groups): for finite fluxes a zero term adds an exact zero to
+// sums that are never -0, so the results are the same to the bit and only
+// the loads go.
 // ---------------------------------------------------------------------------
 template <bool MIXED>
 struct KV { using T = double; };
@@ -231,15 +238,18 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
             tid0, nthr, NB,
             [&](int b) -> T {
               Dot2 d;
-              d.add(ff_mul(ff{P.wsrc_h[(size_t)g * NB + b], P.wsrc_l[(size_t)g * NB + b]},
-                           ff{P.fsh[old][b], P.fsl[old][b]}),
-                    invKe_ff);
+              if ((P.src_nz >> g) & 1u)
+                d.add(ff_mul(ff{P.wsrc_h[(size_t)g * NB + b], P.wsrc_l[(size_t)g * NB + b]},
+                             ff{P.fsh[old][b], P.fsl[old][b]}),
+                      invKe_ff);
               for (int h = 0; h < ng; ++h) {
                 if (h == g) continue;
+                const int q = P.adj ? g * ng + h : h * ng + g;
+                if (!((P.sc_nz >> q) & 1ull)) continue;   // an all-zero scattering plane
                 const bool solved = P.adj ? (h > g) : (h < g);
                 const int buf = solved ? nw : old;
                 const size_t ix = (size_t)h * NBH + b;
-                const size_t is = P.adj ? ((size_t)g * ng + h) * NB + b : ((size_t)h * ng + g) * NB + b;
+                const size_t is = (size_t)q * NB + b;
                 d.add(ff{P.sigs_h[is], P.sigs_l[is]}, ff{P.xh[buf][ix], P.xl[buf][ix]});
               }
               const int off[7] = {-plane, -nxx, -1, 0, 1, nxx, plane};
@@ -267,13 +277,13 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
               double s0 = 0.0;
               for (int h = 0; h < ng; ++h) {
                 if (h == g) continue;
+                const int q = P.adj ? g * ng + h : h * ng + g;
+                if (!((P.sc_nz >> q) & 1ull)) continue;   // an all-zero scattering plane
                 const bool solved = P.adj ? (h > g) : (h < g);
                 const double ph = (solved ? phiN : phiO)[(size_t)h * NBH + b];
-                const double sg =
-                    P.adj ? P.sigs[((size_t)g * ng + h) * NB + b] : P.sigs[((size_t)h * ng + g) * NB + b];
-                s0 = fma(sg, ph, s0);
+                s0 = fma(P.sigs[(size_t)q * NB + b], ph, s0);
               }
-              double bs = wsrc[b] * fsO[b] * invKe + s0;
+              double bs = ((P.src_nz >> g) & 1u) ? wsrc[b] * fsO[b] * invKe + s0 : s0;
               if (P.trans) bs = bs + P.exsrc[(size_t)g * NB + b];   // TSrcTr (mod_cmfd.f90:1091-1093)
               double a64[7];
 #pragma unroll

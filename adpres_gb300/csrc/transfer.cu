@@ -158,7 +158,45 @@ __global__ void k_fb_nodes(FbParams P) {
   if (threadIdx.x == 0 && (nuf_bad || sigs_bad)) atomicOr(P.flags, (nuf_bad ? 1 : 0) | (sigs_bad ? 4 : 0));
 }
 
+// Source planes that are nonzero somewhere (launch_xs_nonzero): per thread
+// the masks of its nodes, OR-reduced over the warp, one atomic per warp.
+__global__ void k_xs_nonzero(const double* __restrict__ chin, const double* __restrict__ nuf,
+                             const double* __restrict__ sigs, const int* __restrict__ act, int nn, int G,
+                             long long NB, unsigned* out) {
+  unsigned c = 0, f = 0, s0 = 0, s1 = 0;
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+    const long long b = act[n];
+    for (int g = 0; g < G; ++g) {
+      if (chin[g * NB + b] != 0.0) c |= 1u << g;
+      if (nuf[g * NB + b] != 0.0) f |= 1u << g;
+      for (int h = 0; h < G; ++h) {
+        const int q = g * G + h;
+        if (sigs[(long long)q * NB + b] != 0.0) {
+          if (q < 32) s0 |= 1u << q;
+          else s1 |= 1u << (q - 32);
+        }
+      }
+    }
+  }
+  c = __reduce_or_sync(0xffffffffu, c);
+  f = __reduce_or_sync(0xffffffffu, f);
+  s0 = __reduce_or_sync(0xffffffffu, s0);
+  s1 = __reduce_or_sync(0xffffffffu, s1);
+  if ((threadIdx.x & 31) == 0) {
+    if (c) atomicOr(out, c);
+    if (f) atomicOr(out + 1, f);
+    if (s0) atomicOr(out + 2, s0);
+    if (s1) atomicOr(out + 3, s1);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_xs_nonzero(const double* chin, const double* nuf, const double* sigs, const int* act, int nn,
+                              int G, long long NB, unsigned* out, cudaStream_t st) {
+  k_xs_nonzero<<<xfer_blocks(nn), kXferThreads, 0, st>>>(chin, nuf, sigs, act, nn, G, NB, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_fb_updt(const FbParams& P, cudaStream_t st) {
   k_fb_state<<<xfer_blocks(P.tq), kXferThreads, 0, st>>>(P);

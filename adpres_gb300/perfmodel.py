@@ -41,3 +41,20 @@ def bicg_bytes_per_row_iteration(precision: str) -> float:
     if precision == "fp64":
         return 248.0
     return 4 * (4 + 7) + 4 * 2 + 4 * (2 + 7) + 4 * 2 + (8 + 4 * 4) + (8 + 4)
+
+
+def p0_skipped_bytes_per_row_outer(xsigs, chi, mat) -> float:
+    """Bytes of the P0 terms the kernel leaves out on a given core (forward
+    solve): per outer and box row, 16 B (sigma_s and the other group's flux)
+    for every scattering plane h -> g that is zero in every material in use,
+    and 16 B (the source weight and fs0) for every group whose chi is zero
+    in every material in use.  The canonical count above includes them."""
+    import numpy as np
+    used = np.unique(np.asarray(mat)) - 1
+    xs = np.asarray(xsigs)[used]
+    ch = np.asarray(chi)[used]
+    G = ch.shape[1]
+    zs = sum(1 for h in range(G) for g in range(G) if h != g and not np.any(xs[:, h, g] != 0.0))
+    zc = sum(1 for g in range(G) if not np.any(ch[:, g] != 0.0))
+    return 16.0 * (zs + zc)
+
