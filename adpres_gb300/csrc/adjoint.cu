@@ -24,7 +24,7 @@ namespace adp {
 // A^T in the same 7-slot layout: the coefficient of x[b + off_c] in row b of
 // A^T is the coefficient of x[b] in row b + off_c of A, i.e. that row's
 // opposite slot.
-__global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, float* AT32, float* AT32lo) {
+__global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, float* AT32, float2* AT2) {
   const int NB = G.NB;
   const long long total = (long long)NB * ng;
   const int off[7] = {-G.plane, -G.nxx, -1, 0, 1, G.nxx, G.plane};
@@ -42,18 +42,18 @@ __global__ void k_transpose(BoxGeom G, int ng, const double* A, double* AT, floa
       if (AT32) {
         const float hi = (float)v;
         AT32[(size_t)g * 7 * NB + (size_t)c * NB + b] = hi;
-        if (AT32lo) AT32lo[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)(v - (double)hi);
+        if (AT2) AT2[(size_t)g * 7 * NB + (size_t)c * NB + b] = make_float2(hi, (float)(v - (double)hi));
       }
     }
   }
 }
 
-cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, float* AT32lo,
+cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, float2* AT2,
                              cudaStream_t st) {
   long long total = (long long)G.NB * ng;
   int blocks = (int)((total + 255) / 256);
   if (blocks > 65535 * 4) blocks = 65535 * 4;
-  k_transpose<<<blocks, 256, 0, st>>>(G, ng, A, AT, AT32, AT32lo);
+  k_transpose<<<blocks, 256, 0, st>>>(G, ng, A, AT, AT32, AT2);
   return cudaGetLastError();
 }
 

@@ -50,19 +50,14 @@ struct OuterParams {
   double* red;                // [2][kRedQ][kMaxBlocks]
   // Double-float (hi + lo FP32 pairs) state of the mixed path: the defect
   // correction and the flux and fission-source updates run on these.
-  const float* A32lo;         // [ng][7][NB] A - A32
-  float* xh[2];               // flux [ng][NBH] (halo offset applied)
-  float* xl[2];
-  float* fsh[2];              // fission source [NB]
-  float* fsl[2];
-  const float* wsrc_h;        // [ng][NB]
-  const float* wsrc_l;
-  const float* wfis_h;
-  const float* wfis_l;
-  const float* sigs_h;        // [ng][ng][NB]
-  const float* sigs_l;
-  const float* vdel_h;        // [NB]
-  const float* vdel_l;
+  // Each array holds (hi, lo) pairs.
+  const float2* A2;           // [ng][7][NB] the FP64 matrix as (A32, A - A32)
+  float2* x2[2];              // flux [ng][NBH] (halo offset applied)
+  float2* fs2[2];             // fission source [NB]
+  const float2* wsrc2;        // [ng][NB]
+  const float2* wfis2;
+  const float2* sigs2;        // [ng][ng][NB]
+  const float2* vdel2;        // [NB]
   OuterCtl* ctl;
   double* tr_k;
   double* tr_ser;
@@ -115,7 +110,7 @@ struct AssembleParams {
   const double* dn;
   double* A;
   float* A32;
-  float* A32lo;               // A - A32 (mixed path), may be null
+  float2* A2;                 // (A32, A - A32) pairs (mixed path), may be null
 };
 
 // Contraction of forward and adjoint fluxes into dk/dSigma (adjoint.cu).
@@ -216,10 +211,10 @@ cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st);
 cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, const double* sigtr,
                            const double* siga, const double* sigs, double* D, double* sigr, OuterCtl* ctl,
                            cudaStream_t st);
-cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, float* AT32lo,
+cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* AT, float* AT32, float2* AT2,
                              cudaStream_t st);
-// x = hi + lo with hi = (float)x (double-float copies of the mixed path)
-cudaError_t launch_split(const double* x, float* hi, float* lo, long long n, cudaStream_t st);
+// out = (hi, lo) with hi = (float)x, lo = (float)(x - hi) (double-float copies of the mixed path)
+cudaError_t launch_split(const double* x, float2* out, long long n, cudaStream_t st);
 cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st);
 // node-order <-> box transfers (transfer.cu): host layout a(nn, A, B), node
 // fastest; device planes [A][B] of stride `stride` indexed by act[n]

@@ -334,13 +334,13 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
   add(NB * 8 * 2);                  // fs
   add(NBH * 8 * 8);                 // Krylov FP64
   if (mixed) add(NBH * 4 * 8);      // Krylov FP32
-  if (mixed) {                      // double-float state: A lo, flux, fission source, XS copies
-    add(G * 7 * NB * 4);
-    for (int q = 0; q < 4; ++q) add(G * NBH * 4);
-    for (int q = 0; q < 4; ++q) add(NB * 4);
-    for (int q = 0; q < 4; ++q) add(G * NB * 4);
-    for (int q = 0; q < 2; ++q) add(G * G * NB * 4);
-    for (int q = 0; q < 2; ++q) add(NB * 4);
+  if (mixed) {                      // double-float (hi, lo) pairs: A, flux, fission source, XS copies
+    add(G * 7 * NB * 8);
+    for (int q = 0; q < 2; ++q) add(G * NBH * 8);
+    for (int q = 0; q < 2; ++q) add(NB * 8);
+    for (int q = 0; q < 2; ++q) add(G * NB * 8);
+    add(G * G * NB * 8);
+    add(NB * 8);
   }
   add(2 * kRedQ * kMaxBlocks * 8);
   add(sizeof(OuterCtl));
@@ -388,23 +388,13 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
   }
   h->d_red = (double*)A.take(2 * kRedQ * kMaxBlocks * 8);
   if (mixed) {
-    h->d_A32lo = (float*)A.take(G * 7 * NB * 4);
-    for (int t = 0; t < 2; ++t) {
-      h->d_xh[t] = (float*)A.take(G * NBH * 4) + h->plane;
-      h->d_xl[t] = (float*)A.take(G * NBH * 4) + h->plane;
-    }
-    for (int t = 0; t < 2; ++t) {
-      h->d_fsh[t] = (float*)A.take(NB * 4);
-      h->d_fsl[t] = (float*)A.take(NB * 4);
-    }
-    h->d_chin_h = (float*)A.take(G * NB * 4);
-    h->d_chin_l = (float*)A.take(G * NB * 4);
-    h->d_nuf_h = (float*)A.take(G * NB * 4);
-    h->d_nuf_l = (float*)A.take(G * NB * 4);
-    h->d_sigs_h = (float*)A.take(G * G * NB * 4);
-    h->d_sigs_l = (float*)A.take(G * G * NB * 4);
-    h->d_vdel_h = (float*)A.take(NB * 4);
-    h->d_vdel_l = (float*)A.take(NB * 4);
+    h->d_A2 = (float2*)A.take(G * 7 * NB * 8);
+    for (int t = 0; t < 2; ++t) h->d_x2[t] = (float2*)A.take(G * NBH * 8) + h->plane;
+    for (int t = 0; t < 2; ++t) h->d_fs2[t] = (float2*)A.take(NB * 8);
+    h->d_chin2 = (float2*)A.take(G * NB * 8);
+    h->d_nuf2 = (float2*)A.take(G * NB * 8);
+    h->d_sigs2 = (float2*)A.take(G * G * NB * 8);
+    h->d_vdel2 = (float2*)A.take(NB * 8);
   }
   h->d_ctl = (OuterCtl*)A.take(sizeof(OuterCtl));
   h->d_tr_k = (double*)A.take(nout * 8);
@@ -438,7 +428,7 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
     adp_destroy(h);
     return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
   }
-  if (mixed && (ce = launch_split(h->d_vdel, h->d_vdel_h, h->d_vdel_l, (long long)NB, h->st)) != cudaSuccess) {
+  if (mixed && (ce = launch_split(h->d_vdel, h->d_vdel2, (long long)NB, h->st)) != cudaSuccess) {
     adp_destroy(h);
     return fail(nullptr, ADP_ERR_CUDA, std::string("initial upload: ") + cudaGetErrorString(ce));
   }
@@ -642,9 +632,9 @@ static adp_status after_xs(adp_handle* h) {
   }
   if (h->o.precision == ADP_MIXED) {
     const long long gn = (long long)h->ng * h->NB;
-    CK(launch_split(h->d_chin, h->d_chin_h, h->d_chin_l, gn, h->st));
-    CK(launch_split(h->d_nuf, h->d_nuf_h, h->d_nuf_l, gn, h->st));
-    CK(launch_split(h->d_sigs, h->d_sigs_h, h->d_sigs_l, gn * h->ng, h->st));
+    CK(launch_split(h->d_chin, h->d_chin2, gn, h->st));
+    CK(launch_split(h->d_nuf, h->d_nuf2, gn, h->st));
+    CK(launch_split(h->d_sigs, h->d_sigs2, gn * h->ng, h->st));
   }
   if (h->o.kern == ADP_KERN_SANM) {
     // get_ABEFGH depends on sigr, D and the node sizes only
@@ -932,21 +922,15 @@ OuterParams adp::outer_params(adp_handle* h, int adj) {
   P.s32 = h->d_s32;
   P.t32 = h->d_t32;
   P.red = h->d_red;
-  P.A32lo = h->d_A32lo;
+  P.A2 = h->d_A2;
   for (int t = 0; t < 2; ++t) {
-    P.xh[t] = h->d_xh[t];
-    P.xl[t] = h->d_xl[t];
-    P.fsh[t] = h->d_fsh[t];
-    P.fsl[t] = h->d_fsl[t];
+    P.x2[t] = h->d_x2[t];
+    P.fs2[t] = h->d_fs2[t];
   }
-  P.wsrc_h = adj ? h->d_nuf_h : h->d_chin_h;
-  P.wsrc_l = adj ? h->d_nuf_l : h->d_chin_l;
-  P.wfis_h = adj ? h->d_chin_h : h->d_nuf_h;
-  P.wfis_l = adj ? h->d_chin_l : h->d_nuf_l;
-  P.sigs_h = h->d_sigs_h;
-  P.sigs_l = h->d_sigs_l;
-  P.vdel_h = h->d_vdel_h;
-  P.vdel_l = h->d_vdel_l;
+  P.wsrc2 = adj ? h->d_nuf2 : h->d_chin2;
+  P.wfis2 = adj ? h->d_chin2 : h->d_nuf2;
+  P.sigs2 = h->d_sigs2;
+  P.vdel2 = h->d_vdel2;
   P.ctl = h->d_ctl;
   P.tr_k = h->d_tr_k;
   P.tr_ser = h->d_tr_ser;
@@ -1034,7 +1018,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   AP.dn = h->d_dn;
   AP.A = h->d_A;
   AP.A32 = h->d_A32;
-  AP.A32lo = h->d_A32lo;
+  AP.A2 = h->d_A2;
   CK(launch_assemble(AP, h->st));
   OuterParams P = outer_params(h, adj);
   // first-call start (mod_cmfd.f90:448-454 / :635-641)
@@ -1255,7 +1239,10 @@ static adp_status adj_alloc(adp_handle* h) {
   size_t bytes = 0;
   auto add = [&](size_t b) { bytes += ((b + 255) & ~(size_t)255) + 256; };
   add(G * 7 * NB * 8);
-  if (mixed) add(G * 7 * NB * 4 * 2);
+  if (mixed) {
+    add(G * 7 * NB * 4);
+    add(G * 7 * NB * 8);
+  }
   add(G * NBH * 8 * 2);
   add(NB * 8 * 2);
   add(sizeof(OuterCtl));
@@ -1268,7 +1255,7 @@ static adp_status adj_alloc(adp_handle* h) {
   h->d_AT = (double*)A.take(G * 7 * NB * 8);
   if (mixed) {
     h->d_AT32 = (float*)A.take(G * 7 * NB * 4);
-    h->d_AT32lo = (float*)A.take(G * 7 * NB * 4);
+    h->d_AT2 = (float2*)A.take(G * 7 * NB * 8);
   }
   for (int t = 0; t < 2; ++t) h->d_psi[t] = (double*)A.take(G * NBH * 8) + h->plane;
   for (int t = 0; t < 2; ++t) h->d_fsa[t] = (double*)A.take(NB * 8);
@@ -1293,11 +1280,11 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
   CK(cudaStreamSynchronize(h->st));
   const OuterCtl fwd = *h->h_ctl;
   // A^T of the converged forward matrix (dn frozen)
-  CK(launch_transpose(box_geom(h), h->ng, h->d_A, h->d_AT, h->d_AT32, h->d_AT32lo, h->st));
+  CK(launch_transpose(box_geom(h), h->ng, h->d_A, h->d_AT, h->d_AT32, h->d_AT2, h->st));
   OuterParams P = outer_params(h, 1);
   P.A = h->d_AT;
   P.A32 = h->d_AT32;
-  P.A32lo = h->d_AT32lo;
+  P.A2 = h->d_AT2;
   for (int t = 0; t < 2; ++t) {
     P.phi[t] = h->d_psi[t];
     P.fs[t] = h->d_fsa[t];

@@ -37,20 +37,19 @@ cudaError_t launch_assemble(const AssembleParams& P, cudaStream_t st) {
 
 // First-call start of outer()/outer_ad(): f0 = 1, Ke = 1, fs0 = FSrc(f0)
 // (mod_cmfd.f90:448-454, :635-641).
-__global__ void k_split(const double* x, float* hi, float* lo, long long n) {
+__global__ void k_split(const double* x, float2* out, long long n) {
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
     const double v = x[q];
     const float h = (float)v;
-    hi[q] = h;
-    lo[q] = (float)(v - (double)h);
+    out[q] = make_float2(h, (float)(v - (double)h));
   }
 }
 
-cudaError_t launch_split(const double* x, float* hi, float* lo, long long n, cudaStream_t st) {
+cudaError_t launch_split(const double* x, float2* out, long long n, cudaStream_t st) {
   long long blocks = (n + 255) / 256;
   if (blocks > 65535 * 4) blocks = 65535 * 4;
   if (blocks < 1) blocks = 1;
-  k_split<<<(int)blocks, 256, 0, st>>>(x, hi, lo, n);
+  k_split<<<(int)blocks, 256, 0, st>>>(x, out, n);
   return cudaGetLastError();
 }
 

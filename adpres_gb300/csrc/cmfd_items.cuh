@@ -31,7 +31,7 @@ __device__ __forceinline__ void assemble_items(const AssembleParams& P, long lon
       for (int c = 0; c < 7; ++c) {
         A[(size_t)c * NB + b] = 0.0;
         if (P.A32) P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = 0.0f;
-        if (P.A32lo) P.A32lo[(size_t)g * 7 * NB + (size_t)c * NB + b] = 0.0f;
+        if (P.A2) P.A2[(size_t)g * 7 * NB + (size_t)c * NB + b] = make_float2(0.0f, 0.0f);
       }
       continue;
     }
@@ -73,7 +73,7 @@ __device__ __forceinline__ void assemble_items(const AssembleParams& P, long lon
       if (P.A32) {
         const float hi = (float)a[c];
         P.A32[(size_t)g * 7 * NB + (size_t)c * NB + b] = hi;
-        if (P.A32lo) P.A32lo[(size_t)g * 7 * NB + (size_t)c * NB + b] = (float)(a[c] - (double)hi);
+        if (P.A2) P.A2[(size_t)g * 7 * NB + (size_t)c * NB + b] = make_float2(hi, (float)(a[c] - (double)hi));
       }
     }
   }

@@ -25,6 +25,14 @@ __device__ __forceinline__ ff ff_from_double(double x) {
 
 __device__ __forceinline__ double ff_to_double(ff x) { return (double)x.hi + (double)x.lo; }
 
+// Double-float arrays are stored as float2 (hi, lo) pairs: one 8-byte
+// access per value instead of two 4-byte ones.
+__device__ __forceinline__ ff ld_ff(const float2* p) {
+  const float2 v = *p;
+  return ff{v.x, v.y};
+}
+__device__ __forceinline__ void st_ff(float2* p, ff v) { *p = make_float2(v.hi, v.lo); }
+
 __device__ __forceinline__ ff ff_norm(float s, float e) {   // FastTwoSum, |s| >= |e|
   const float t = __fadd_rn(s, e);
   return ff{t, __fsub_rn(e, __fsub_rn(t, s))};

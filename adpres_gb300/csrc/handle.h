@@ -59,14 +59,12 @@ struct adp_handle {
   float* d_vv32[2] = {nullptr, nullptr};
   double* d_red = nullptr;
   // double-float copies of the mixed path
-  float* d_A32lo = nullptr;
-  float* d_xh[2] = {nullptr, nullptr};
-  float* d_xl[2] = {nullptr, nullptr};
-  float* d_fsh[2] = {nullptr, nullptr};
-  float* d_fsl[2] = {nullptr, nullptr};
-  float *d_chin_h = nullptr, *d_chin_l = nullptr, *d_nuf_h = nullptr, *d_nuf_l = nullptr;
-  float *d_sigs_h = nullptr, *d_sigs_l = nullptr, *d_vdel_h = nullptr, *d_vdel_l = nullptr;
-  float* d_AT32lo = nullptr;
+  // ((hi, lo) pairs)
+  float2* d_A2 = nullptr;
+  float2* d_x2[2] = {nullptr, nullptr};
+  float2* d_fs2[2] = {nullptr, nullptr};
+  float2 *d_chin2 = nullptr, *d_nuf2 = nullptr, *d_sigs2 = nullptr, *d_vdel2 = nullptr;
+  float2* d_AT2 = nullptr;
   adp::OuterCtl* d_ctl = nullptr;
   adp::OuterCtl* h_ctl = nullptr;   // pinned mirror
   double *d_tr_k = nullptr, *d_tr_ser = nullptr, *d_tr_fer = nullptr, *d_tr_ndmax = nullptr;

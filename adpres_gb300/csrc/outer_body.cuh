@@ -89,8 +89,8 @@ struct RowsInFlight<true> { static constexpr int R = ADP_ROWS_MIXED; };
 // convergence test, all in the same order as mod_cmfd.f90:479-495.
 //
 // MIXED: P0 forms the defect of the current flux in double-float (a
-// compensated dot product over the FP64 matrix as A32 + A32lo and the flux
-// and sources as hi + lo pairs); the nin Krylov steps for the correction run
+// compensated dot product over the FP64 matrix as (A32, A - A32) and the
+// flux and sources as (hi, lo) pairs, each pair one float2); the nin Krylov steps for the correction run
 // with the FP32 matrix copy and FP32 vectors; the reductions are
 // double-float and the flux x, held as hi + lo, receives the FP32
 // increments.  Both forms avoid FP64 division in per-row work (the source
@@ -183,14 +183,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
     // the neighbours' rows before the first stencil.
     const double* ph = P.phi[cur];
     for (int b = tid0; b < NB; b += nthr) {
-      for (int g = 0; g < ng; ++g) {
-        const ff v = ff_from_double(ph[(size_t)g * NBH + b]);
-        P.xh[cur][(size_t)g * NBH + b] = v.hi;
-        P.xl[cur][(size_t)g * NBH + b] = v.lo;
-      }
-      const ff v = ff_from_double(P.fs[cur][b]);
-      P.fsh[cur][b] = v.hi;
-      P.fsl[cur][b] = v.lo;
+      for (int g = 0; g < ng; ++g) st_ff(&P.x2[cur][(size_t)g * NBH + b], ff_from_double(ph[(size_t)g * NBH + b]));
+      st_ff(&P.fs2[cur][b], ff_from_double(P.fs[cur][b]));
     }
     if (!team_barrier(C, nblk, rank)) return;
   }
@@ -230,18 +224,15 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
         // (the transient runs the FP64 kernel only)
         // Defect of the current flux in double-float: one compensated dot
         // product over the source and the seven matrix terms (A = A32 + lo).
-        const float* xOh = P.xh[old] + (size_t)g * NBH;
-        const float* xOl = P.xl[old] + (size_t)g * NBH;
-        const float* Alo = P.A32lo + (size_t)g * 7 * NB;
+        const float2* xO2 = P.x2[old] + (size_t)g * NBH;
+        const float2* A2g = P.A2 + (size_t)g * 7 * NB;
         T accT = T(0);
         rows_batched<RowsInFlight<MIXED>::R>(
             tid0, nthr, NB,
             [&](int b) -> T {
               Dot2 d;
               if ((P.src_nz >> g) & 1u)
-                d.add(ff_mul(ff{P.wsrc_h[(size_t)g * NB + b], P.wsrc_l[(size_t)g * NB + b]},
-                             ff{P.fsh[old][b], P.fsl[old][b]}),
-                      invKe_ff);
+                d.add(ff_mul(ld_ff(&P.wsrc2[(size_t)g * NB + b]), ld_ff(&P.fs2[old][b])), invKe_ff);
               for (int h = 0; h < ng; ++h) {
                 if (h == g) continue;
                 const int q = P.adj ? g * ng + h : h * ng + g;
@@ -250,15 +241,15 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 const int buf = solved ? nw : old;
                 const size_t ix = (size_t)h * NBH + b;
                 const size_t is = (size_t)q * NB + b;
-                d.add(ff{P.sigs_h[is], P.sigs_l[is]}, ff{P.xh[buf][ix], P.xl[buf][ix]});
+                d.add(ld_ff(&P.sigs2[is]), ld_ff(&P.x2[buf][ix]));
               }
               const int off[7] = {-plane, -nxx, -1, 0, 1, nxx, plane};
               const int j = SMEMA ? jrow(b) : 0;
 #pragma unroll
               for (int c = 0; c < 7; ++c) {
-                const float ah = Ag[(size_t)c * NB + b];
-                if constexpr (SMEMA) sA[(size_t)c * SR + j] = ah;
-                d.sub(ff{ah, Alo[(size_t)c * NB + b]}, ff{xOh[b + off[c]], xOl[b + off[c]]});
+                const ff a = ld_ff(&A2g[(size_t)c * NB + b]);   // a.hi is the A32 coefficient
+                if constexpr (SMEMA) sA[(size_t)c * SR + j] = a.hi;
+                d.sub(a, ld_ff(&xO2[b + off[c]]));
               }
               return d.value().hi;
             },
@@ -368,10 +359,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 });
           } else {
             const double* xc = (it == 1) ? xO : xN;
-            const float* xch = MIXED ? ((it == 1) ? P.xh[old] : P.xh[nw]) + (size_t)g * NBH : nullptr;
-            const float* xcl = MIXED ? ((it == 1) ? P.xl[old] : P.xl[nw]) + (size_t)g * NBH : nullptr;
-            float* xNh = MIXED ? P.xh[nw] + (size_t)g * NBH : nullptr;
-            float* xNl = MIXED ? P.xl[nw] + (size_t)g * NBH : nullptr;
+            const float2* xc2 = MIXED ? ((it == 1) ? P.x2[old] : P.x2[nw]) + (size_t)g * NBH : nullptr;
+            float2* xN2 = MIXED ? P.x2[nw] + (size_t)g * NBH : nullptr;
             struct RowA { T rb, pb, v, rsb; double xn; ff xf; };
             rows_batched<RowsInFlight<MIXED>::R>(
                 tid0, nthr, NB,
@@ -384,7 +373,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                   if constexpr (MIXED) {
                     // FP32 increment of the correction, added to the double-float flux
                     const T dx = fmav(tom, s[b], tap * pO[b]);
-                    xf = ff_add_f(ff{xch[b], xcl[b]}, dx);
+                    xf = ff_add_f(ld_ff(&xc2[b]), dx);
                   } else {
                     xn = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
                   }
@@ -403,8 +392,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 [&](int b, const RowA& q) {
                   r[b] = q.rb;
                   if constexpr (MIXED) {
-                    xNh[b] = q.xf.hi;
-                    xNl[b] = q.xf.lo;
+                    st_ff(&xN2[b], q.xf);
                   } else {
                     xN[b] = q.xn;
                   }
@@ -502,24 +490,20 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           const T to = MIXED ? (T)s_f[3] : (T)omega;
           const double* xc = (it == 0) ? xO : xN;
           if constexpr (MIXED) {
-            const float* xch = ((it == 0) ? P.xh[old] : P.xh[nw]) + (size_t)g * NBH;
-            const float* xcl = ((it == 0) ? P.xl[old] : P.xl[nw]) + (size_t)g * NBH;
-            const float* xOh = P.xh[old] + (size_t)g * NBH;
-            const float* xOl = P.xl[old] + (size_t)g * NBH;
-            float* xNh = P.xh[nw] + (size_t)g * NBH;
-            float* xNl = P.xl[nw] + (size_t)g * NBH;
+            const float2* xc2 = ((it == 0) ? P.x2[old] : P.x2[nw]) + (size_t)g * NBH;
+            const float2* xO2 = P.x2[old] + (size_t)g * NBH;
+            float2* xN2 = P.x2[nw] + (size_t)g * NBH;
             struct RowCm { ff xn; float d; };
             rows_batched<RowsInFlight<MIXED>::R>(
                 tid0, nthr, NB,
                 [&](int b) -> RowCm {
                   // FP32 increment of the correction, added to the double-float flux
                   const T dx = fmav(to, s[b], ta * pN[b]);
-                  const ff xn = ff_add_f(ff{xch[b], xcl[b]}, dx);
-                  return RowCm{xn, ff_diff(xn, ff{xOh[b], xOl[b]})};
+                  const ff xn = ff_add_f(ld_ff(&xc2[b]), dx);
+                  return RowCm{xn, ff_diff(xn, ld_ff(&xO2[b]))};
                 },
                 [&](int b, const RowCm& q) {
-                  xNh[b] = q.xn.hi;
-                  xNl[b] = q.xn.lo;
+                  st_ff(&xN2[b], q.xn);
                   // RelEg (mod_cmfd.f90:1172-1199): max |x - x0| / |x| over |x| > 1e-10
                   const float ax = fabsf(q.xn.hi), d = fabsf(q.d);
                   if (ax > 1.e-10f && d > fer_f * ax) fer_f = fmaxf(fer_f, d / ax);
@@ -557,13 +541,11 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           [&](int b) -> RowFm {
             Dot2 d;
             for (int g = 0; g < ng; ++g)
-              d.add(ff{P.xh[nw][(size_t)g * NBH + b], P.xl[nw][(size_t)g * NBH + b]},
-                    ff{P.wfis_h[(size_t)g * NB + b], P.wfis_l[(size_t)g * NB + b]});
-            return RowFm{d.value(), ff{P.fsh[old][b], P.fsl[old][b]}, ff{P.vdel_h[b], P.vdel_l[b]}};
+              d.add(ld_ff(&P.x2[nw][(size_t)g * NBH + b]), ld_ff(&P.wfis2[(size_t)g * NB + b]));
+            return RowFm{d.value(), ld_ff(&P.fs2[old][b]), ld_ff(&P.vdel2[b])};
           },
           [&](int b, const RowFm& q) {
-            P.fsh[nw][b] = q.fs.hi;
-            P.fsl[nw][b] = q.fs.lo;
+            st_ff(&P.fs2[nw][b], q.fs);
             const float en = ff_diff(q.fs, q.fo);
             e2f = fmaf(en, en, e2f);
             if (!extrap) {
@@ -626,12 +608,11 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
         float serf = 0.f;
         Dot2 dint;
         for (int b = tid0; b < NB; b += nthr) {
-          const ff fo{P.fsh[old][b], P.fsl[old][b]};
-          ff fs{P.fsh[nw][b], P.fsl[nw][b]};
+          const ff fo = ld_ff(&P.fs2[old][b]);
+          ff fs = ld_ff(&P.fs2[nw][b]);
           fs = ff_add(fs, ff_mul(cf, ff_add(fs, ff{-fo.hi, -fo.lo})));
-          P.fsh[nw][b] = fs.hi;
-          P.fsl[nw][b] = fs.lo;
-          dint.add(ff{P.vdel_h[b], P.vdel_l[b]}, fs);
+          st_ff(&P.fs2[nw][b], fs);
+          dint.add(ld_ff(&P.vdel2[b]), fs);
           const float af = fabsf(fs.hi), d = fabsf(ff_diff(fs, fo));
           if (af > 1.e-10f && d > serf * af) serf = fmaxf(serf, d / af);
         }
@@ -679,8 +660,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
         // back to the FP64 flux and fission source for the host and the nodal update
         for (int b = tid0; b < NB; b += nthr) {
           for (int g = 0; g < ng; ++g)
-            P.phi[cur][(size_t)g * NBH + b] = ff_to_double(ff{P.xh[cur][(size_t)g * NBH + b], P.xl[cur][(size_t)g * NBH + b]});
-          P.fs[cur][b] = ff_to_double(ff{P.fsh[cur][b], P.fsl[cur][b]});
+            P.phi[cur][(size_t)g * NBH + b] = ff_to_double(ld_ff(&P.x2[cur][(size_t)g * NBH + b]));
+          P.fs[cur][b] = ff_to_double(ld_ff(&P.fs2[cur][b]));
         }
       }
       if (lead) {
