@@ -25,6 +25,7 @@ struct OuterParams {
   // bit of the sum); all ones when unknown.
   unsigned src_nz;
   unsigned long long sc_nz;
+  unsigned fis_nz;            // bit g: wfis of group g nonzero somewhere (FSrc)
   const double* exsrc;        // [ng][NB] external source of the transient step (trans only)
   double serc, ferc;
   long long NBH;              // group stride of halo'd arrays

@@ -910,6 +910,7 @@ OuterParams adp::outer_params(adp_handle* h, int adj) {
   }
   P.wsrc = adj ? h->d_nuf : h->d_chin;
   P.src_nz = adj ? h->nuf_nz : h->chi_nz;
+  P.fis_nz = adj ? h->chi_nz : h->nuf_nz;
   P.sc_nz = h->sigs_nz;
   P.wfis = adj ? h->d_chin : h->d_nuf;
   P.sigs = h->d_sigs;

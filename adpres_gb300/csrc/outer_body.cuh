@@ -97,11 +97,11 @@ struct RowsInFlight<true> { static constexpr int R = ADP_ROWS_MIXED; };
 // uses 1/k computed once per outer; RelE/RelEg divide only when a candidate
 // beats the running maximum).
 //
-// P0 leaves out the source terms of planes that are zero at every node
-// (P.src_nz, P.sc_nz: the up-scatter planes of a down-scatter-only core,
-// the chi = 0 groups): for finite fluxes a zero term adds an exact zero to
-// sums that are never -0, so the results are the same to the bit and only
-// the loads go.
+// P0 and FSrc leave out the terms of planes that are zero at every node
+// (P.src_nz, P.sc_nz, P.fis_nz: the up-scatter planes of a down-scatter-only
+// core, the chi = 0 groups of the source and of the adjoint's FSrc): for
+// finite fluxes a zero term adds an exact zero to sums that are never -0,
+// so the results are the same to the bit and only the loads go.
 // ---------------------------------------------------------------------------
 template <bool MIXED>
 struct KV { using T = double; };
@@ -541,7 +541,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           [&](int b) -> RowFm {
             Dot2 d;
             for (int g = 0; g < ng; ++g)
-              d.add(ld_ff(&P.x2[nw][(size_t)g * NBH + b]), ld_ff(&P.wfis2[(size_t)g * NB + b]));
+              if ((P.fis_nz >> g) & 1u)
+                d.add(ld_ff(&P.x2[nw][(size_t)g * NBH + b]), ld_ff(&P.wfis2[(size_t)g * NB + b]));
             return RowFm{d.value(), ld_ff(&P.fs2[old][b]), ld_ff(&P.vdel2[b])};
           },
           [&](int b, const RowFm& q) {
@@ -565,7 +566,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           tid0, nthr, NB,
           [&](int b) -> RowF {
             double fs = 0.0;
-            for (int g = 0; g < ng; ++g) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
+            for (int g = 0; g < ng; ++g)
+              if ((P.fis_nz >> g) & 1u) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
             return RowF{fs, fsO[b], G.vdel[b]};
           },
           [&](int b, const RowF& q) {

@@ -15,6 +15,7 @@ reactivity.
 from __future__ import annotations
 
 import copy
+import time
 
 import numpy as np
 
@@ -51,7 +52,9 @@ def move_banks(bpos, tr, ht, t2):
 
 def rod_eject(core, dk=None, max_steps=None):
     """Records (t, rho, relative power, nout reached, outers, device ms); rho
-    is absolute at t = 0 and in dollars afterwards, as the reference prints."""
+    is absolute at t = 0 and in dollars afterwards, as the reference prints.
+    Sets core.rod_eject_wall = (steady state s, time steps s), host clock."""
+    t_start = time.perf_counter()
     dk = dk if dk is not None else core.deck
     tr = dk.trans
     w = _working_deck(dk)
@@ -83,12 +86,15 @@ def rod_eject(core, dk=None, max_steps=None):
     core.outer(popt=0, trace=False)
     r0 = core.trans_init(tr["beta"], tr["lamb"], tr["velo"], tr["theta"], tr["extr"], af)
     out = [(0.0, r0.rho, 1.0, False, 0, 0.0)]
+    t_steady = time.perf_counter()
+    core.rod_eject_wall = (t_steady - t_start, 0.0)
 
     def step(ht, t2, omeg_mode):
         move_banks(bpos, tr, ht, t2)
         set_xs()
         r = core.trans_step(ht, omeg_mode)
         out.append((t2, r.rho_dollar, r.relpow, bool(r.maxi), r.outers, r.device_ms))
+        core.rod_eject_wall = (t_steady - t_start, time.perf_counter() - t_steady)
 
     n = 0
     for i in range(1, _nint(tr["tdiv"] / tr["tstep1"]) + 1):

@@ -263,13 +263,14 @@ def transient_leg(steps=2):
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
         t_cpu, ref = pool.apply(_transient_oracle, (text,))
-    walls, rec = [], None
+    walls, parts, rec = [], [], None
     for i in range(steps + 1):
         core = Core.from_deck(dk, precision="fp64")
         t0 = time.perf_counter()
         rec = rod_eject(core, dk)
         if i:
             walls.append(time.perf_counter() - t0)
+            parts.append(core.rod_eject_wall)
         core.close()
     t = sum(walls) / len(walls)
     pw = np.array([r[2] for r in ref])
@@ -279,6 +280,8 @@ def transient_leg(steps=2):
                         "(0.01 s to 0.1 s, then 0.05 s), theta 0.5",
             "nodes": int(dk.nnod), "steps": nsteps, "ms_per_transient": t * 1e3, "steps_per_s": nsteps / t,
             "outers": int(sum(r[4] for r in rec[1:])), "device_ms": float(sum(r[5] for r in rec[1:])),
+            "steady_state_ms": 1e3 * sum(p[0] for p in parts) / len(parts),
+            "steps_wall_ms": 1e3 * sum(p[1] for p in parts) / len(parts),
             "peak_relpow": float(got.max()), "max_relpow_diff_vs_oracle": float(np.max(np.abs(got - pw) / pw)),
             "cpu_baseline": {"value": nsteps / t_cpu, "unit": "time steps/s", "cores": 1, "kind": "port",
                              "sample": f"the oracle's whole transient on this core ({t_cpu:.1f} s)"}}
