@@ -413,8 +413,11 @@ adp_status adp_batch_power(adp_batch* b, int i, double* p);
 /* Device timers of the handle. */
 adp_status adp_get_timers(const adp_handle* h, adp_timers* t);
 
-/* Launch shape of the persistent CMFD kernel: blocks (0 = automatic) and
- * threads per block (0 = automatic).  Used by the autotuner. */
+/* Launch shape of the persistent CMFD kernel: blocks (0 = automatic: one
+ * block per SM at most, the same rows for every thread) and threads per
+ * block (0 = automatic: 512, or 256 when 512-thread blocks would leave more
+ * than half of the SMs idle).  Results are reproducible for a fixed shape;
+ * another shape sums the partial products in another grouping. */
 adp_status adp_set_launch(adp_handle* h, int blocks, int threads);
 
 #ifdef __cplusplus
