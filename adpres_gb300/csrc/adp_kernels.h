@@ -25,7 +25,6 @@ struct OuterParams {
   // bit of the sum); all ones when unknown.
   unsigned src_nz;
   unsigned long long sc_nz;
-  unsigned fis_nz;            // bit g: wfis of group g nonzero somewhere (FSrc)
   const double* exsrc;        // [ng][NB] external source of the transient step (trans only)
   double serc, ferc;
   long long NBH;              // group stride of halo'd arrays
@@ -38,16 +37,12 @@ struct OuterParams {
   const double* sigs;         // [ng(from)][ng(to)][NB]
   double* r;                  // Krylov vectors, halo'd [NBH]
   double* rs;
-  double* pv[2];
-  double* vv[2];
-  double* s;
-  double* t;
+  double2* pv2[2];            // (p, v) pairs, halo'd [NBH], double buffered
+  double2* st2;               // (s, t) pairs, halo'd [NBH]
   float* r32;                 // FP32 Krylov vectors (mixed), halo'd [NBH]
   float* rs32;
-  float* pv32[2];
-  float* vv32[2];
-  float* s32;
-  float* t32;
+  float2* pv2f[2];            // FP32 (p, v) and (s, t) pairs (mixed)
+  float2* st2f;
   double* red;                // [2][kRedQ][kMaxBlocks]
   // Double-float (hi + lo FP32 pairs) state of the mixed path: the defect
   // correction and the flux and fission-source updates run on these.

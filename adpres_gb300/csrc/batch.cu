@@ -324,7 +324,6 @@ adp_status adp_batch_create(int n, const adp_geom* geoms, const adp_opts* opts, 
     // the kernel forms each core's cross sections itself: no plane skipped
     I.op.src_nz = ~0u;
     I.op.sc_nz = ~0ull;
-    I.op.fis_nz = ~0u;
     I.op.do_nodal = h->o.kern != ADP_KERN_FDM;
     I.np = adp::nodal_params(h, 1);
     I.np.nd_blocks = 0;

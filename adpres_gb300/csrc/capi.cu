@@ -378,13 +378,19 @@ adp_status adp_create(const adp_geom* geom, const adp_opts* opts, adp_handle** o
   if (mixed) h->d_A32 = (float*)A.take(G * 7 * NB * 4);
   for (int t = 0; t < 2; ++t) h->d_phi[t] = (double*)A.take(G * NBH * 8) + h->plane;
   for (int t = 0; t < 2; ++t) h->d_fs[t] = (double*)A.take(NB * 8);
+  // Krylov vectors: r, rs, then the (p, v) pairs of both buffers and the
+  // (s, t) pairs, each with its halo planes (the arena is zeroed below)
   double* kv = (double*)A.take(NBH * 8 * 8);
-  double** kp[8] = {&h->d_r, &h->d_rs, &h->d_pv[0], &h->d_pv[1], &h->d_vv[0], &h->d_vv[1], &h->d_s, &h->d_t};
-  for (int q = 0; q < 8; ++q) *kp[q] = kv + (size_t)q * NBH + h->plane;
+  h->d_r = kv + h->plane;
+  h->d_rs = kv + NBH + h->plane;
+  for (int t = 0; t < 2; ++t) h->d_pv2[t] = reinterpret_cast<double2*>(kv + (2 + 2 * t) * NBH) + h->plane;
+  h->d_st2 = reinterpret_cast<double2*>(kv + 6 * NBH) + h->plane;
   if (mixed) {
     float* kf = (float*)A.take(NBH * 4 * 8);
-    float** kq[8] = {&h->d_r32, &h->d_rs32, &h->d_pv32[0], &h->d_pv32[1], &h->d_vv32[0], &h->d_vv32[1], &h->d_s32, &h->d_t32};
-    for (int q = 0; q < 8; ++q) *kq[q] = kf + (size_t)q * NBH + h->plane;
+    h->d_r32 = kf + h->plane;
+    h->d_rs32 = kf + NBH + h->plane;
+    for (int t = 0; t < 2; ++t) h->d_pv2f[t] = reinterpret_cast<float2*>(kf + (2 + 2 * t) * NBH) + h->plane;
+    h->d_st2f = reinterpret_cast<float2*>(kf + 6 * NBH) + h->plane;
   }
   h->d_red = (double*)A.take(2 * kRedQ * kMaxBlocks * 8);
   if (mixed) {
@@ -903,25 +909,20 @@ OuterParams adp::outer_params(adp_handle* h, int adj) {
   for (int t = 0; t < 2; ++t) {
     P.phi[t] = h->d_phi[t];
     P.fs[t] = h->d_fs[t];
-    P.pv[t] = h->d_pv[t];
-    P.vv[t] = h->d_vv[t];
-    P.pv32[t] = h->d_pv32[t];
-    P.vv32[t] = h->d_vv32[t];
+    P.pv2[t] = h->d_pv2[t];
+    P.pv2f[t] = h->d_pv2f[t];
   }
   P.wsrc = adj ? h->d_nuf : h->d_chin;
   P.src_nz = adj ? h->nuf_nz : h->chi_nz;
-  P.fis_nz = adj ? h->chi_nz : h->nuf_nz;
   P.sc_nz = h->sigs_nz;
   P.wfis = adj ? h->d_chin : h->d_nuf;
   P.sigs = h->d_sigs;
   P.r = h->d_r;
   P.rs = h->d_rs;
-  P.s = h->d_s;
-  P.t = h->d_t;
+  P.st2 = h->d_st2;
   P.r32 = h->d_r32;
   P.rs32 = h->d_rs32;
-  P.s32 = h->d_s32;
-  P.t32 = h->d_t32;
+  P.st2f = h->d_st2f;
   P.red = h->d_red;
   P.A2 = h->d_A2;
   for (int t = 0; t < 2; ++t) {

@@ -51,12 +51,12 @@ struct adp_handle {
   float* d_A32 = nullptr;
   double* d_phi[2] = {nullptr, nullptr};
   double* d_fs[2] = {nullptr, nullptr};
-  double *d_r = nullptr, *d_rs = nullptr, *d_s = nullptr, *d_t = nullptr;
-  double* d_pv[2] = {nullptr, nullptr};
-  double* d_vv[2] = {nullptr, nullptr};
-  float *d_r32 = nullptr, *d_rs32 = nullptr, *d_s32 = nullptr, *d_t32 = nullptr;
-  float* d_pv32[2] = {nullptr, nullptr};
-  float* d_vv32[2] = {nullptr, nullptr};
+  double *d_r = nullptr, *d_rs = nullptr;
+  double2* d_pv2[2] = {nullptr, nullptr};   // (p, v)
+  double2* d_st2 = nullptr;                 // (s, t)
+  float *d_r32 = nullptr, *d_rs32 = nullptr;
+  float2* d_pv2f[2] = {nullptr, nullptr};
+  float2* d_st2f = nullptr;
   double* d_red = nullptr;
   // double-float copies of the mixed path
   // ((hi, lo) pairs)

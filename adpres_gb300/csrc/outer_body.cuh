@@ -97,16 +97,22 @@ struct RowsInFlight<true> { static constexpr int R = ADP_ROWS_MIXED; };
 // uses 1/k computed once per outer; RelE/RelEg divide only when a candidate
 // beats the running maximum).
 //
-// P0 and FSrc leave out the terms of planes that are zero at every node
-// (P.src_nz, P.sc_nz, P.fis_nz: the up-scatter planes of a down-scatter-only
-// core, the chi = 0 groups of the source and of the adjoint's FSrc): for
-// finite fluxes a zero term adds an exact zero to sums that are never -0,
-// so the results are the same to the bit and only the loads go.
+// P0 leaves out the source terms of planes that are zero at every node
+// (P.src_nz, P.sc_nz: the up-scatter planes of a down-scatter-only core,
+// the chi = 0 groups): for finite fluxes a zero term adds an exact zero to
+// sums that are never -0, so the results are the same to the bit and only
+// the loads go.
+//
+// The Krylov vectors read at neighbours are stored in pairs: (p, v), double
+// buffered, and (s, t), so a neighbour's recomputed p or r costs two loads
+// instead of four.
 // ---------------------------------------------------------------------------
 template <bool MIXED>
-struct KV { using T = double; };
+struct KV { using T = double; using T2 = double2; };
 template <>
-struct KV<true> { using T = float; };
+struct KV<true> { using T = float; using T2 = float2; };
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
 
 // SMEMA: the block keeps its own rows' matrix coefficients of the group
 // being solved in dynamic shared memory (P.smem_rows rows per coefficient,
@@ -116,6 +122,7 @@ struct KV<true> { using T = float; };
 template <bool MIXED, bool SMEMA = false>
 __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, unsigned nteam) {
   using T = typename KV<MIXED>::T;
+  using T2 = typename KV<MIXED>::T2;
   extern __shared__ __align__(16) unsigned char adp_dyn_smem[];
   T* const sA = reinterpret_cast<T*>(adp_dyn_smem);
   const int SR = P.smem_rows;
@@ -157,10 +164,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
   const T* Ab = MIXED ? (const T*)P.A32 : (const T*)P.A;
   T* r = MIXED ? (T*)P.r32 : (T*)P.r;
   T* rs = MIXED ? (T*)P.rs32 : (T*)P.rs;
-  T* s = MIXED ? (T*)P.s32 : (T*)P.s;
-  T* t = MIXED ? (T*)P.t32 : (T*)P.t;
-  T* pv[2] = {MIXED ? (T*)P.pv32[0] : (T*)P.pv[0], MIXED ? (T*)P.pv32[1] : (T*)P.pv[1]};
-  T* vv[2] = {MIXED ? (T*)P.vv32[0] : (T*)P.vv[0], MIXED ? (T*)P.vv32[1] : (T*)P.vv[1]};
+  T2* st = MIXED ? (T2*)P.st2f : (T2*)P.st2;   // (s, t)
+  T2* pv[2] = {MIXED ? (T2*)P.pv2f[0] : (T2*)P.pv2[0], MIXED ? (T2*)P.pv2f[1] : (T2*)P.pv2[1]};   // (p, v)
 
   if (vld(&C->need_prologue)) {
     // f = Integrate(fs0); errn = 1; e1 = Integrate(errn)  (mod_cmfd.f90:457-459)
@@ -326,10 +331,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           if (lead) set_status(C, ADP_ERR_BREAKDOWN);
           return;
         }
-        T* pN = pv[it & 1];
-        const T* pO = pv[(it & 1) ^ 1];
-        T* vN = vv[it & 1];
-        const T* vO = vv[(it & 1) ^ 1];
+        T2* pvN = pv[it & 1];
+        const T2* pvO = pv[(it & 1) ^ 1];
         const T tb = MIXED ? (T)s_f[0] : (T)beta, tom = MIXED ? (T)s_f[1] : (T)omega,
                 tap = MIXED ? (T)s_f[2] : (T)alpha;
         // ---- phase A: (previous step's x and r), p and v = A p -----------
@@ -353,8 +356,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                   return RowA0{pb, v, rs[b]};
                 },
                 [&](int b, const RowA0& q) {
-                  pN[b] = q.pb;
-                  vN[b] = q.v;
+                  pvN[b] = mk2(q.pb, q.v);
                   accT = fmav(q.rsb, q.v, accT);
                 });
           } else {
@@ -365,19 +367,26 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
             rows_batched<RowsInFlight<MIXED>::R>(
                 tid0, nthr, NB,
                 [&](int b) -> RowA {
-                  auto rf = [&](int m) -> T { return fmav(-tom, t[m], s[m]); };
-                  auto pf = [&](int m) -> T { return fmav(tb, fmav(-tom, vO[m], pO[m]), rf(m)); };
-                  const T rb = rf(b);
+                  auto rf = [&](int m) -> T {
+                    const T2 q = st[m];
+                    return fmav(-tom, q.y, q.x);
+                  };
+                  auto pf = [&](int m) -> T {
+                    const T2 o = pvO[m];
+                    return fmav(tb, fmav(-tom, o.y, o.x), rf(m));
+                  };
+                  const T2 stb = st[b], pvb = pvO[b];
+                  const T rb = fmav(-tom, stb.y, stb.x);
                   double xn = 0.0;
                   ff xf{0.f, 0.f};
                   if constexpr (MIXED) {
                     // FP32 increment of the correction, added to the double-float flux
-                    const T dx = fmav(tom, s[b], tap * pO[b]);
+                    const T dx = fmav(tom, stb.x, tap * pvb.x);
                     xf = ff_add_f(ld_ff(&xc2[b]), dx);
                   } else {
-                    xn = fma(omega, (double)s[b], fma(alpha, (double)pO[b], xc[b]));
+                    xn = fma(omega, (double)stb.x, fma(alpha, (double)pvb.x, xc[b]));
                   }
-                  const T pb = fmav(tb, fmav(-tom, vO[b], pO[b]), rb);
+                  const T pb = fmav(tb, fmav(-tom, pvb.y, pvb.x), rb);
                   const int j = SMEMA ? jrow(b) : 0;
                   auto AC = [&](int c) -> T { return SMEMA ? sA[(size_t)c * SR + j] : Ag[(size_t)c * NB + b]; };
                   T v = AC(0) * pf(b - plane);
@@ -396,8 +405,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                   } else {
                     xN[b] = q.xn;
                   }
-                  pN[b] = q.pb;
-                  vN[b] = q.v;
+                  pvN[b] = mk2(q.pb, q.v);
                   accT = fmav(q.rsb, q.v, accT);
                 });
           }
@@ -429,7 +437,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           rows_batched<RowsInFlight<MIXED>::R>(
               tid0, nthr, NB,
               [&](int b) -> RowB {
-                auto sf = [&](int m) -> T { return fmav(-ta, vN[m], r[m]); };
+                auto sf = [&](int m) -> T { return fmav(-ta, pvN[m].y, r[m]); };
                 const T sb = sf(b);
                 const int j = SMEMA ? jrow(b) : 0;
                 auto AC = [&](int c) -> T { return SMEMA ? sA[(size_t)c * SR + j] : Ag[(size_t)c * NB + b]; };
@@ -443,8 +451,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 return RowB{sb, tt, last ? T(0) : rs[b]};
               },
               [&](int b, const RowB& q) {
-                s[b] = q.sb;
-                t[b] = q.tt;
+                st[b] = mk2(q.sb, q.tt);
                 acc0 = fmav(q.tt, q.tt, acc0);
                 acc1 = fmav(q.tt, q.sb, acc1);
                 if (!last) {
@@ -498,7 +505,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
                 tid0, nthr, NB,
                 [&](int b) -> RowCm {
                   // FP32 increment of the correction, added to the double-float flux
-                  const T dx = fmav(to, s[b], ta * pN[b]);
+                  const T dx = fmav(to, st[b].x, ta * pvN[b].x);
                   const ff xn = ff_add_f(ld_ff(&xc2[b]), dx);
                   return RowCm{xn, ff_diff(xn, ld_ff(&xO2[b]))};
                 },
@@ -513,7 +520,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           rows_batched<RowsInFlight<MIXED>::R>(
               tid0, nthr, NB,
               [&](int b) -> RowC {
-                const double xn = fma(omega, (double)s[b], fma(alpha, (double)pN[b], xc[b]));
+                const double xn = fma(omega, (double)st[b].x, fma(alpha, (double)pvN[b].x, xc[b]));
                 return RowC{xn, xO[b]};
               },
               [&](int b, const RowC& q) {
@@ -541,8 +548,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           [&](int b) -> RowFm {
             Dot2 d;
             for (int g = 0; g < ng; ++g)
-              if ((P.fis_nz >> g) & 1u)
-                d.add(ld_ff(&P.x2[nw][(size_t)g * NBH + b]), ld_ff(&P.wfis2[(size_t)g * NB + b]));
+              d.add(ld_ff(&P.x2[nw][(size_t)g * NBH + b]), ld_ff(&P.wfis2[(size_t)g * NB + b]));
             return RowFm{d.value(), ld_ff(&P.fs2[old][b]), ld_ff(&P.vdel2[b])};
           },
           [&](int b, const RowFm& q) {
@@ -566,8 +572,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
           tid0, nthr, NB,
           [&](int b) -> RowF {
             double fs = 0.0;
-            for (int g = 0; g < ng; ++g)
-              if ((P.fis_nz >> g) & 1u) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
+            for (int g = 0; g < ng; ++g) fs = fma(phiN[(size_t)g * NBH + b], P.wfis[(size_t)g * NB + b], fs);
             return RowF{fs, fsO[b], G.vdel[b]};
           },
           [&](int b, const RowF& q) {
