@@ -757,6 +757,8 @@ adp_status adp_fb_set(adp_handle* h, const adp_fb_tables* t) {
   for (int s = 0; s < t->nstate; ++s) {
     if (t->kind[s] < ADP_FB_BORON || t->kind[s] > ADP_FB_COOL_DENS)
       return fail(h, ADP_ERR_INPUT, "adp_fb_set: unknown state kind");
+    if (t->kind[s] == ADP_FB_FUEL_TEMP && !(t->ref[s] >= 0.0))
+      return fail(h, ADP_ERR_INPUT, "adp_fb_set: negative reference fuel temperature");
     for (int q = 0; q < 5; ++q)
       if (!t->dsig[5 * s + q]) return fail(h, ADP_ERR_INPUT, "adp_fb_set: null state change table");
   }
@@ -832,6 +834,13 @@ adp_status adp_fb_updt(adp_handle* h, const double* state, const double* bpos) {
   CK(cudaSetDevice(h->dev));
   if (!h->fb_ready) return fail(h, ADP_ERR_STATE, "adp_fb_updt: no feedback tables (adp_fb_set)");
   if ((h->fb_nst > 0 && !state) || (h->fb_nb > 0 && !bpos)) return fail(h, ADP_ERR_INPUT, "adp_fb_updt: null state or bank positions");
+  for (int k = 0; k < h->fb_nst; ++k) {
+    if (!std::isfinite(state[k])) return fail(h, ADP_ERR_INPUT, "adp_fb_updt: non-finite state value");
+    if (h->fb_kind[k] == ADP_FB_FUEL_TEMP && state[k] < 0.0)
+      return fail(h, ADP_ERR_INPUT, "adp_fb_updt: negative fuel temperature");
+  }
+  for (int b = 0; b < h->fb_nb; ++b)
+    if (!std::isfinite(bpos[b])) return fail(h, ADP_ERR_INPUT, "adp_fb_updt: non-finite bank position");
   const int G = h->ng, nmat = h->fb_nmat;
   const long long t1 = (long long)G * nmat;
   FbParams P;

@@ -12,6 +12,8 @@ last step stops at ser < 1e-5).  Mixed path: the search converges (|k - 1|
 < 1e-5) at a boron within 0.5 ppm of the oracle's (k's slope is about
 10 pcm/ppm here).
 """
+import copy
+
 import numpy as np
 import pytest
 
@@ -136,6 +138,21 @@ def test_device_feedback_update_errors():
     with pytest.raises(AdpError) as e:
         fresh.fb_updt(dk)
     assert e.value.status == ADP_ERR_STATE
+    # a non-finite bank position or a negative fuel temperature is an input error
+    with pytest.raises(AdpError) as e:
+        core.fb_updt(dk, bpos=np.full(int(dk.feedback["crod"]["nb"]), np.nan))
+    assert e.value.status == ADP_ERR_INPUT
+    ft = dict(dk.feedback["ftem"])
+    ft["value"] = -1.0
+    neg = dict(dk.feedback)
+    neg["ftem"] = ft
+    dkn = copy.copy(dk)
+    dkn.feedback = neg
+    with pytest.raises(AdpError) as e:
+        core.fb_updt(dkn)
+    assert e.value.status == ADP_ERR_INPUT
+    core.fb_updt(dk)   # the handle stays usable
+    assert core.outer(popt=0, trace=False).converged
     bad = dict(dk.feedback["crod"])
     bad["fbmap"] = np.asarray(bad["fbmap"]).copy()
     bad["fbmap"][0, 0] = int(bad["nb"]) + 1
