@@ -429,11 +429,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     ck = clocks.stop()
     t_after = core.timers()
-    total_s = sum(dev_ms) / 1e3
-    if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+    total_s = max_over_ranks(dist, sum(dev_ms) / 1e3)
     value = world * args.steps / total_s
     keff_mixed = rep.keff
     p_mixed = core.power()
@@ -506,6 +502,8 @@ def run_ours(args):
     h2d = sum(a.nbytes for a in xin) + mat_p.nbytes + sigs_p.nbytes + dc_p.nbytes
     d2h = dk.nnod * 8 + dk.nnod * dk.ng * 8
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         core.xs_updt(*xin, mat_p, sigs_p, dc_p)
@@ -514,7 +512,7 @@ def run_ours(args):
         core.power()
         core.flux()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
     e2e_value = world * e2e_steps / e2e_s
 
     if rank != 0:
@@ -551,6 +549,19 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+# ---------------------------------------------------- replicas (N > 1) ----
+def max_over_ranks(dist, x):
+    """The largest of every rank's x (the slowest replica's time); x itself
+    when there is one rank.  NCCL reduces a device tensor, gloo a host one."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(x)
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ------------------------------------------------------ reference arm ----
