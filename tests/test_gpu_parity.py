@@ -308,3 +308,29 @@ def test_node_table_uploads_agree_and_check():
     c.xs_updt_nodes(dk.xsigtr[m], dk.xsiga[m], dk.xnuf[m], dk.xsigf[m], dk.chi, dk.mat, dk.xsigs[m], dk.dc)
     c.reset()
     assert c.outer().keff == reps[0].keff
+
+
+def test_core_4g_full_size():
+    """The headline workload at its full size (68x68x80 nodes, 4 groups,
+    1,479,680 unknowns): FP64 against the oracle (k within 0.1 pcm; nodal
+    power within 1e-6 or 4x the oracle's own rounding sensitivity, the
+    distance between its builds with and without multiply-add contraction,
+    since the loosely converged iteration may stop at another outer), and
+    mixed precision against FP64 (1 pcm, 0.1%)."""
+    text = synth.core_4g(0, planes=80)
+    o = _oracle_run(text)
+    of = oracle.Oracle(text=text, variant="fma")
+    of.run()
+    sens = max_rel(of.powdis(), o.powdis())
+    c64, r64 = _gpu_run(text, "fp64")
+    p64 = c64.power()
+    print(f"core_4g: oracle k={o.getd('Ke')!r} outers={o.geti('outers')}, fma build outers={of.geti('outers')} "
+          f"power sens={sens:.2e}; GPU FP64 k={r64.keff!r} outers={r64.outers} "
+          f"dk={pcm(r64.keff, o.getd('Ke')):.2e} pcm dp={max_rel(p64, o.powdis()):.2e}")
+    assert r64.converged
+    assert pcm(r64.keff, o.getd("Ke")) <= KTOL_PCM
+    assert max_rel(p64, o.powdis()) <= max(PTOL, 4.0 * sens)
+    c32, r32 = _gpu_run(text, "mixed")
+    assert r32.converged
+    assert pcm(r32.keff, r64.keff) <= 1.0
+    assert max_rel(c32.power(), p64) <= 1e-3
