@@ -320,10 +320,9 @@ adp_status adp_batch_create(int n, const adp_geom* geoms, const adp_opts* opts, 
     adp_handle* h = b->core[i];
     BatchInst& I = inst[i];
     std::memset(&I, 0, sizeof I);
+    // the kernel forms D and sigr itself; chi, nu*fission and sigs (and
+    // with them the handle's masks of all-zero planes) come from the host
     I.op = adp::outer_params(h, 0);
-    // the kernel forms each core's cross sections itself: no plane skipped
-    I.op.src_nz = ~0u;
-    I.op.sc_nz = ~0ull;
     I.op.do_nodal = h->o.kern != ADP_KERN_FDM;
     I.np = adp::nodal_params(h, 1);
     I.np.nd_blocks = 0;
