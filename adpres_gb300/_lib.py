@@ -113,6 +113,8 @@ SIGNATURES = {
     "adp_xs_updt_nodes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _ip, _dp, _dp]),
     "adp_fb_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpFbTables)]),
     "adp_fb_updt": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp]),
+    "adp_fb_rod_tips": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, _dp, _ip, _dp]),
     "adp_outer": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(AdpReport)]),
     "adp_get_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),
     "adp_set_state": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp]),

@@ -829,6 +829,32 @@ adp_status adp_fb_set(adp_handle* h, const adp_fb_tables* t) {
   return ADP_OK;
 }
 
+// crod_updt (mod_xsec.f90:239-263): the rod tip of each bank, walking down
+// from the top of the core; the plane holding it and its rodded fraction
+// (no plane holds it: every plane of the bank's columns is fully rodded).
+// The product is held apart so that it is rounded on its own, as the
+// reference's is, whether or not the host compiler contracts a - b * c.
+adp_status adp_fb_rod_tips(int nzz, const double* zdel, double coreh, double pos0, double ssize, int nbank,
+                           const double* bpos, int* tip, double* vf) {
+  if (nzz < 1 || nbank < 0 || !zdel || (nbank > 0 && (!bpos || !tip || !vf))) return ADP_ERR_INPUT;
+  for (int b = 0; b < nbank; ++b) {
+    volatile double step = bpos[b] * ssize;
+    const double rodh = (coreh - pos0) - step;
+    double dum = 0.0;
+    tip[b] = -1;
+    vf[b] = 0.0;
+    for (int k = nzz - 1; k >= 0; --k) {
+      if (rodh >= dum && rodh <= dum + zdel[k]) {
+        tip[b] = k;
+        vf[b] = (rodh - dum) / zdel[k];
+        break;
+      }
+      dum = dum + zdel[k];
+    }
+  }
+  return ADP_OK;
+}
+
 adp_status adp_fb_updt(adp_handle* h, const double* state, const double* bpos) {
   if (!h) return ADP_ERR_INPUT;
   CK(cudaSetDevice(h->dev));
@@ -865,25 +891,8 @@ adp_status adp_fb_updt(adp_handle* h, const double* state, const double* bpos) {
   // the state changes of bcon_updt, ftem_updt (square roots), mtem_updt, cden_updt
   for (int k = 0; k < h->fb_nst; ++k)
     P.dv[k] = h->fb_kind[k] == ADP_FB_FUEL_TEMP ? std::sqrt(state[k]) - std::sqrt(h->fb_ref[k]) : state[k] - h->fb_ref[k];
-  // crod_updt (mod_xsec.f90:239-263): the rod tip of each bank, walking
-  // down from the top of the core; the plane holding it and its rodded
-  // fraction (no plane: every plane below the top is rodded).  The product
-  // is held apart so that it is rounded on its own, as the reference's is.
-  for (int b = 0; b < h->fb_nb; ++b) {
-    volatile double step = bpos[b] * h->fb_ssize;
-    const double rodh = (h->fb_coreh - h->fb_pos0) - step;
-    double dum = 0.0;
-    P.tip[b] = -1;
-    P.vf[b] = 0.0;
-    for (int k = h->nzz - 1; k >= 0; --k) {
-      if (rodh >= dum && rodh <= dum + h->zdel[k]) {
-        P.tip[b] = k;
-        P.vf[b] = (rodh - dum) / h->zdel[k];
-        break;
-      }
-      dum = dum + h->zdel[k];
-    }
-  }
+  if (h->fb_nb > 0)
+    adp_fb_rod_tips(h->nzz, h->zdel.data(), h->fb_coreh, h->fb_pos0, h->fb_ssize, h->fb_nb, bpos, P.tip, P.vf);
   Xfer X;
   adp_status s = xfer_reserve(h, nmat, X);
   if (s != ADP_OK) return s;

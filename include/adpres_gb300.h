@@ -209,6 +209,14 @@ adp_status adp_fb_set(adp_handle* h, const adp_fb_tables* t);
  * rodded columns become 0), then D, sigr and the checks as adp_xs_updt. */
 adp_status adp_fb_updt(adp_handle* h, const double* state, const double* bpos);
 
+/* The rod tips adp_fb_updt uses (crod_updt, mod_xsec.f90:239-263): for each
+ * bank position bpos[b] (steps), the plane (0-based, bottom up) holding the
+ * rod tip, walking down from the top of the core, or -1 when none holds it
+ * (every plane of the bank's columns is then fully rodded), and the rodded
+ * fraction vf[b] of that plane.  Host arithmetic only; no device call. */
+adp_status adp_fb_rod_tips(int nzz, const double* zdel, double coreh, double pos0, double ssize, int nbank,
+                           const double* bpos, int* tip, double* vf);
+
 /* -- solver --------------------------------------------------------------- */
 
 /* One call of outer(popt) (mode ADP_FORWARD) or outer_ad(popt) (ADP_ADJOINT)

@@ -112,3 +112,39 @@ def test_deck_feedback_card_errors(case):
         deck.parse(t, "/nonexistent")
     with pytest.raises(oracle.OracleError, match=msg):
         oracle.Oracle(text=t)
+
+
+def test_rod_tips_of_the_abi_match_the_host_restatement():
+    """adp_fb_rod_tips (host arithmetic inside the C library, no device
+    call) gives the plane and rodded fraction of feedback._rod_tip to the bit
+    for bank positions across and beyond the core, on the sample deck's
+    planes and on uneven ones."""
+    import ctypes
+
+    from adpres_gb300 import _lib
+    from adpres_gb300._lib import dptr, iptr
+    from adpres_gb300.feedback import _rod_tip
+    L = _lib.load()
+    rng = np.random.default_rng(7)
+    fx = fixture()
+    dk = deck_from_fixture(fx)
+    cr = dk.feedback["crod"]
+    cases = [([float(z) for z in dk.zdel], float(dk.coreh), float(cr["pos0"]), float(cr["ssize"]))]
+    z = list(rng.uniform(2.0, 30.0, 17))
+    h = 0.0
+    for v in z:
+        h = h + v
+    cases.append((z, h, 7.3, 1.587))
+    for zdel, coreh, pos0, ssize in cases:
+        nstep = (coreh - pos0) / ssize
+        bpos = np.concatenate([rng.uniform(-5.0, nstep + 5.0, 400), [0.0, nstep, np.floor(nstep)]])
+        tip = np.zeros(len(bpos), dtype=np.int32)
+        vf = np.zeros(len(bpos))
+        zd = np.ascontiguousarray(zdel, dtype=np.float64)
+        st = L.adp_fb_rod_tips(len(zdel), dptr(zd), coreh, pos0, ssize, len(bpos), dptr(bpos), iptr(tip), dptr(vf))
+        assert st == 0
+        for b, p in enumerate(bpos):
+            k, w = _rod_tip(coreh - pos0 - p * ssize, zdel)
+            assert tip[b] == k
+            if k >= 0:
+                assert vf[b] == w
