@@ -119,6 +119,17 @@ module adpres_gb300_bind
       real(c_double), intent(in) :: state(*), bpos(*)   ! bcon, ftem, mtem, cden as given; bank positions
     end function
 
+    ! tip(b) is 0-based from the bottom (-1: no plane holds the tip)
+    integer(c_int) function adp_fb_rod_tips(nzz, zdel, coreh, pos0, ssize, nbank, bpos, tip, vf) &
+        bind(C, name="adp_fb_rod_tips")
+      import :: c_int, c_double
+      integer(c_int), value :: nzz, nbank
+      real(c_double), intent(in) :: zdel(*), bpos(*)
+      real(c_double), value :: coreh, pos0, ssize
+      integer(c_int), intent(out) :: tip(*)
+      real(c_double), intent(out) :: vf(*)
+    end function
+
     integer(c_int) function adp_set_xs(h, nmat, D, sigr, nuf, sigf, chi, mat, sigs, dc) bind(C, name="adp_set_xs")
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: h
