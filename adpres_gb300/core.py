@@ -106,22 +106,30 @@ class Core:
             raise AdpError(st, _lib.last_error(self.h))
 
     # -- cross sections -----------------------------------------------------
+    def _xs_args(self, rows, tables, chi, mat, sigs, dc):
+        """Column-major copies of the four (rows, ng) tables, chi (nmat, ng),
+        mat (nnod), sigs (rows, ng, ng) and dc (nnod, ng, 6) or None, after
+        checking their sizes (the library reads exactly these many values)."""
+        nmat = int(np.asarray(chi).shape[0]) if np.ndim(chi) else 0
+        G, nn = self.ng, self.nnod
+        rows = nmat if rows == "mat" else nn
+        want = [(t, rows * G) for t in tables] + [(chi, nmat * G), (mat, nn), (sigs, rows * G * G)]
+        if dc is not None:
+            want.append((dc, nn * G * 6))
+        for a, n in want:
+            if a is None or np.size(a) != n or n == 0:
+                raise AdpError(_lib.ADP_ERR_INPUT, "cross-section array of the wrong size")
+        args = [_fortran(t) for t in tables] + [_fortran(chi)]
+        return (nmat, args, _c(mat, np.int32), _fortran(sigs), None if dc is None else _fortran(dc))
+
     def xs_updt(self, xsigtr, xsiga, xnuf, xsigf, chi, mat, xsigs, dc=None):
         """XS_updt from material tables (nmat,ng) / (nmat,ng,ng) and mat (nnod,)."""
-        nmat = int(np.asarray(chi).shape[0])
-        args = [_fortran(xsigtr), _fortran(xsiga), _fortran(xnuf), _fortran(xsigf), _fortran(chi)]
-        m = _c(mat, np.int32)
-        s = _fortran(xsigs)
-        d = None if dc is None else _fortran(dc)
+        nmat, args, m, s, d = self._xs_args("mat", (xsigtr, xsiga, xnuf, xsigf), chi, mat, xsigs, dc)
         self._check(self.L.adp_xs_updt(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
 
     def xs_updt_nodes(self, sigtr, siga, nuf, sigf, chi, mat, sigs, dc=None):
         """XS_updt from node tables (nnod,ng) / (nnod,ng,ng)."""
-        nmat = int(np.asarray(chi).shape[0])
-        args = [_fortran(sigtr), _fortran(siga), _fortran(nuf), _fortran(sigf), _fortran(chi)]
-        m = _c(mat, np.int32)
-        s = _fortran(sigs)
-        d = None if dc is None else _fortran(dc)
+        nmat, args, m, s, d = self._xs_args("node", (sigtr, siga, nuf, sigf), chi, mat, sigs, dc)
         self._check(self.L.adp_xs_updt_nodes(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
 
     def fb_set(self, dk):
@@ -138,11 +146,19 @@ class Core:
             keep.append(a)
             return a
 
+        nmat, G = int(np.asarray(dk.chi).shape[0]), self.ng
+
         def table_set(tabs):
+            for k in KEYS:
+                if np.size(tabs[k]) != nmat * G * (G if k == "sigs" else 1):
+                    raise AdpError(_lib.ADP_ERR_INPUT, f"feedback table {k} of the wrong size")
             return [dptr(arr(tabs[k])) for k in KEYS]
 
+        if np.size(dk.chi) != nmat * G or np.size(dk.mat) != self.nnod or (
+                dk.dc is not None and np.size(dk.dc) != self.nnod * G * 6):
+            raise AdpError(_lib.ADP_ERR_INPUT, "chi, mat or dc of the wrong size")
         t = _lib.AdpFbTables()
-        t.nmat = int(np.asarray(dk.chi).shape[0])
+        t.nmat = nmat
         base = dict(sigtr=dk.xsigtr, siga=dk.xsiga, nuf=dk.xnuf, sigf=dk.xsigf, sigs=dk.xsigs)
         t.xsigtr, t.xsiga, t.xnuf, t.xsigf, t.xsigs = table_set(base)
         t.chi = dptr(arr(dk.chi))
@@ -175,14 +191,12 @@ class Core:
         bp = None
         if "crod" in fb:
             bp = _c(fb["crod"]["bpos"] if bpos is None else bpos)
+            if bp.size != int(fb["crod"]["nb"]):
+                raise AdpError(_lib.ADP_ERR_INPUT, "one bank position per rod bank")
         self._check(self.L.adp_fb_updt(self.h, dptr(st), dptr(bp)))
 
     def set_xs(self, D, sigr, nuf, sigf, chi, mat, sigs, dc=None):
-        nmat = int(np.asarray(chi).shape[0])
-        args = [_fortran(D), _fortran(sigr), _fortran(nuf), _fortran(sigf), _fortran(chi)]
-        m = _c(mat, np.int32)
-        s = _fortran(sigs)
-        d = None if dc is None else _fortran(dc)
+        nmat, args, m, s, d = self._xs_args("node", (D, sigr, nuf, sigf), chi, mat, sigs, dc)
         self._check(self.L.adp_set_xs(self.h, nmat, *[dptr(a) for a in args], iptr(m), dptr(s), dptr(d)))
 
     # -- solver -------------------------------------------------------------
