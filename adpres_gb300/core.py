@@ -106,6 +106,12 @@ class Core:
             raise AdpError(st, _lib.last_error(self.h))
 
     # -- cross sections -----------------------------------------------------
+    def _sized(self, a, n, what):
+        """a as given when it holds n values, else an input error."""
+        if a is None or np.size(a) != n:
+            raise AdpError(_lib.ADP_ERR_INPUT, f"{what}: expected {n} values")
+        return a
+
     def _xs_args(self, rows, tables, chi, mat, sigs, dc):
         """Column-major copies of the four (rows, ng) tables, chi (nmat, ng),
         mat (nnod), sigs (rows, ng, ng) and dc (nnod, ng, 6) or None, after
@@ -259,9 +265,10 @@ class Core:
         return f0.reshape((self.nnod, self.ng), order="F")
 
     def set_state(self, f0=None, fs0=None, keff=None, dn=None):
-        a = None if f0 is None else _fortran(f0)
-        b = None if fs0 is None else _c(fs0)
-        d = None if dn is None else _fortran(dn)
+        nn, G = self.nnod, self.ng
+        a = None if f0 is None else _fortran(self._sized(f0, nn * G, "f0 (nnod, ng)"))
+        b = None if fs0 is None else _c(self._sized(fs0, nn, "fs0 (nnod)"))
+        d = None if dn is None else _fortran(self._sized(dn, nn * G * 6, "dn (nnod, ng, 6)"))
         k = None if keff is None else ctypes.byref(ctypes.c_double(keff))
         self._check(self.L.adp_set_state(self.h, dptr(a), dptr(b), k, dptr(d)))
 
@@ -283,11 +290,12 @@ class Core:
     def trans_init(self, beta, lamb, velo, theta, extr, af):
         """adp_trans_init after the steady state: af (nnod, ng) adjoint weight.
         Returns the t = 0 record (rho absolute, relative power 1)."""
-        self._trans_keep = [_c(beta), _c(lamb), _c(velo)]
+        self._trans_keep = [_c(beta), _c(lamb), _c(self._sized(velo, self.ng, "velo (ng)"))]
         b, l, v = self._trans_keep
+        self._sized(l, b.size, "one decay constant per delayed family")
         o = _lib.AdpTransOpts(len(b), dptr(b), dptr(l), dptr(v), float(theta), int(bool(extr)))
         r = _lib.AdpTransResult()
-        a = _fortran(af)
+        a = _fortran(self._sized(af, self.nnod * self.ng, "af (nnod, ng)"))
         self._check(self.L.adp_trans_init(self.h, ctypes.byref(o), dptr(a), ctypes.byref(r)))
         return r
 
@@ -303,17 +311,20 @@ class Core:
     # -- adjoint-weighted edits (mod_trans.f90:648-746) ------------------------
     def reactivity(self, af, sigrp=None):
         """reactivity: (src - lea - rem) / fde of the current state weighted by af (nnod, ng)."""
-        a = _fortran(af)
-        s = None if sigrp is None else _fortran(sigrp)
+        nn, G = self.nnod, self.ng
+        a = _fortran(self._sized(af, nn * G, "af (nnod, ng)"))
+        s = None if sigrp is None else _fortran(self._sized(sigrp, nn * G, "sigrp (nnod, ng)"))
         rho = ctypes.c_double()
         self._check(self.L.adp_reactivity(self.h, dptr(a), dptr(s), ctypes.byref(rho)))
         return rho.value
 
     def core_beta(self, af, ibeta, mat):
         """calc_beta: delayed fraction weighted by af, ibeta (nmat, nf), mat (nnod,) 1-based."""
-        a = _fortran(af)
+        a = _fortran(self._sized(af, self.nnod * self.ng, "af (nnod, ng)"))
         ib = np.asfortranarray(ibeta, dtype=np.float64)
-        m = _c(mat, np.int32)
+        if ib.ndim != 2:
+            raise AdpError(_lib.ADP_ERR_INPUT, "ibeta: a (nmat, nf) table")
+        m = _c(self._sized(mat, self.nnod, "mat (nnod)"), np.int32)
         beta = ctypes.c_double()
         self._check(self.L.adp_core_beta(self.h, dptr(a), int(ib.shape[0]), int(ib.shape[1]),
                                          dptr(ib.reshape(-1, order="F")), iptr(m), ctypes.byref(beta)))

@@ -45,3 +45,13 @@ def test_xs_args_rejects_a_wrong_size(bad):
     with pytest.raises(AdpError) as e:
         Core._xs_args(f, "node", tabs, chi, mat, sigs, dc)
     assert e.value.status == ADP_ERR_INPUT
+
+
+def test_sized_checks_the_value_count():
+    f = _fake(nnod=4, ng=2)
+    a = np.ones((4, 2))
+    assert Core._sized(f, a, 8, "af") is a
+    for bad in (np.ones((4, 3)), None, np.ones(7)):
+        with pytest.raises(AdpError) as e:
+            Core._sized(f, bad, 8, "af")
+        assert e.value.status == ADP_ERR_INPUT
