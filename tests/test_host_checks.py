@@ -55,3 +55,37 @@ def test_sized_checks_the_value_count():
         with pytest.raises(AdpError) as e:
             Core._sized(f, bad, 8, "af")
         assert e.value.status == ADP_ERR_INPUT
+
+
+class _StubLib:
+    """Stands in for the C library: every entry point returns ADP_OK, so
+    only the Python side's marshalling runs."""
+
+    def __getattr__(self, name):
+        return lambda *a, **k: 0
+
+
+def test_host_entry_points_marshal_a_deck_without_a_device():
+    from adpres_gb300 import deck, synth
+    dk = deck.parse(synth.rod_ejection_3d(0, n=9, planes=6))
+    c = Core.__new__(Core)
+    c.L, c.h, c.nnod, c.ng, c._fb_cards = _StubLib(), None, dk.nnod, dk.ng, []
+    m = dk.mat - 1
+    c.xs_updt(dk.xsigtr, dk.xsiga, dk.xnuf, dk.xsigf, dk.chi, dk.mat, dk.xsigs, dk.dc)
+    c.xs_updt_nodes(dk.xsigtr[m], dk.xsiga[m], dk.xnuf[m], dk.xsigf[m], dk.chi, dk.mat, dk.xsigs[m], dk.dc)
+    c.set_xs(dk.xsigtr[m], dk.xsiga[m], dk.xnuf[m], dk.xsigf[m], dk.chi, dk.mat, dk.xsigs[m], dk.dc)
+    c.fb_set(dk)
+    assert c._fb_cards == [nm for nm in ("bcon", "ftem", "mtem", "cden") if nm in dk.feedback]
+    c.fb_updt(dk)
+    c.fb_updt(dk, bcon=1000.0, bpos=np.array(dk.feedback["crod"]["bpos"], float))
+    with pytest.raises(AdpError):
+        c.fb_updt(dk, bpos=np.zeros(int(dk.feedback["crod"]["nb"]) + 1))
+    af = np.ones((dk.nnod, dk.ng))
+    tr = dk.trans
+    c.trans_init(tr["beta"], tr["lamb"], tr["velo"], tr["theta"], tr["extr"], af)
+    with pytest.raises(AdpError):
+        c.trans_init(tr["beta"], tr["lamb"], tr["velo"], tr["theta"], tr["extr"], af[:-1])
+    c.set_state(f0=af, fs0=np.ones(dk.nnod), keff=1.0, dn=np.zeros((dk.nnod, dk.ng, 6)))
+    c.reactivity(af)
+    c.reactivity(af, af)
+    c.core_beta(af, np.full((dk.chi.shape[0], 6), 1e-3), dk.mat)
