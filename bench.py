@@ -523,7 +523,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage / f64 reductions" if prec == "mixed" else "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 Krylov steps / double-float (f32 pair) residual and reductions" if prec == "mixed" else "f64",
         "data": "synthetic (seeded core, reference deck format)", "config": workload_config(dk, prec),
         "outers_per_solve": statistics.mean(outers), "nodal_updates_per_solve": statistics.mean(nodal),
         "keff": keff_mixed,
