@@ -308,12 +308,13 @@ def boron_search_3d(seed=0, n=17, planes=20, rbcon=1000.0):
     return text + "\n".join(L) + "\n"
 
 
-def rod_ejection_3d(seed=0, n=17, planes=20, ttot=0.5, tstep1=0.01, tdiv=0.1, tstep2=0.05, theta=0.5):
+def rod_ejection_3d(seed=0, n=17, planes=20, ttot=0.5, tstep1=0.01, tdiv=0.1, tstep2=0.05, theta=0.5, extr=False):
     """Rod ejection (mode RODEJECT) on the core of boron_search_3d: the same
     geometry, cross sections (at its reference boron, no boron card) and two
     rod banks; bank 1 is ejected from step 120 to 228 at 2280 steps/s (0.05 s),
     bank 2 stays.  Six delayed families, 2-group velocities; theta 0.5
-    (Crank-Nicolson); the steady state is brought to k = 1 by KNE1."""
+    (Crank-Nicolson); the steady state is brought to k = 1 by KNE1.  extr
+    adds %EXTR (the exponential flux extrapolation of trans_calc)."""
     text = boron_search_3d(seed, n=n, planes=planes)
     out, skip = [], False
     for ln in text.splitlines():
@@ -331,6 +332,8 @@ def rod_ejection_3d(seed=0, n=17, planes=20, ttot=0.5, tstep1=0.01, tdiv=0.1, ts
          "0.0124 0.0305 0.111 0.301 1.14 3.01",
          "2.0e7 2.2e5",
          "%THET", _fmt(theta)]
+    if extr:
+        L.append("%EXTR")
     return text + "\n".join(L) + "\n"
 
 

@@ -45,9 +45,13 @@ def test_lmw_matches_oracle():
     assert not any(r[3] for r in rec) and not fx["out_maxi"].any()
 
 
-def test_synthetic_ejection_matches_oracle():
+@pytest.mark.parametrize("extr", [False, True])
+def test_synthetic_ejection_matches_oracle(extr):
+    """With %EXTR the steps also carry the exponential flux extrapolation:
+    omega = ln(f0 / ft) / dt from the second step on (rod_eject,
+    mod_trans.f90:120-156), used by trans_calc's removal and sources."""
     import oracle
-    text = synth.rod_ejection_3d(0, n=9, planes=6)
+    text = synth.rod_ejection_3d(0, n=9, planes=6, extr=extr)
     ref = oracle.Oracle(text=text).rodeject()
     sens = oracle.Oracle(text=text, variant="fma").rodeject()
     pw = np.array([r[2] for r in ref])
