@@ -12,9 +12,14 @@
 // gfortran for x86-64 without FMA, so no multiply-add may be fused here.
 //
 // Scope: deck cards %MODE %CASE %XSEC %GEOM %ADF %ITER %KERN %PRNT (+ FILE
-// includes, '!' comments); XS_updt (base + D/sigr + checks); forward `outer`
-// and adjoint `outer_ad` with BiCGSTAB, fission-source extrapolation and the
-// SANM/PNM two-node nodal update; PowDis.  Reference STOPs become error codes.
+// includes, '!' comments), the feedback cards %CROD %CBCS %BCON %FTEM %MTEM
+// %CDEN and the transient cards %EJCT %THET %EXTR; XS_updt (base, state and
+// rod updates, D/sigr, checks); forward `outer` and adjoint `outer_ad` with
+// BiCGSTAB, fission-source extrapolation and the SANM/PNM two-node nodal
+// update; PowDis and the AsmPow/AxiPow/AsmFlux edits; reactivity and
+// calc_beta; the critical boron search cbsearch; the rod ejection transient
+// (rod_eject, trans_calc, outer_tr, KNE1).  Reference STOPs become error
+// codes.
 
 #include <cmath>
 #include <cstdio>
