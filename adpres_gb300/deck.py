@@ -115,7 +115,12 @@ def _split(lines, basedir):
         if "FILE" in text or "file" in text:
             parts = text.strip().split(None, 1)
             fname = parts[1].strip() if len(parts) > 1 else ""
+            # as given, else beside the deck; an absolute path written on
+            # another machine (the sample decks carry their author's) falls
+            # back to the file of that name beside the deck
             path = fname if os.path.exists(fname) else os.path.join(basedir, fname)
+            if not os.path.exists(path) and os.path.isabs(fname):
+                path = os.path.join(basedir, os.path.basename(fname))
             if cur is None:
                 raise DeckError(ADP_ERR_INPUT, f"line {ln}: FILE include outside a card")
             try:

@@ -231,8 +231,10 @@ static void split_cards(const std::vector<Line>& buf, const std::string& basedir
       std::string fname = sp == std::string::npos ? std::string("") : trim(l.substr(sp + 1));
       std::string content;
       std::ifstream t1(fname);
+      std::ifstream t2(basedir + "/" + fname);
       if (t1) content = read_file(fname);
-      else content = read_file(basedir + "/" + fname);
+      else if (t2 || fname.empty() || fname[0] != '/') content = read_file(basedir + "/" + fname);
+      else content = read_file(basedir + "/" + fname.substr(fname.rfind('/') + 1));   // another machine's absolute path
       std::vector<Line> inc;
       strip_comments(content, inc);
       if (!cur) throw OraError(ORA_ERR_INPUT, "FILE include outside a card");

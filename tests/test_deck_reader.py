@@ -29,7 +29,9 @@ def _compare(dk, o):
     assert int(dk.adjoint) == o.geti("adjoint")
 
 
-@pytest.mark.parametrize("name", ["IAEA3Ds", "adjoint", "PNM", "FDM", "FDM-1D", "DVP", "IAEA2D", "BIBLIS", "KOEBERG"])
+@pytest.mark.parametrize("name", ["IAEA3Ds", "adjoint", "PNM", "FDM", "FDM-1D", "DVP", "IAEA2D", "BIBLIS", "KOEBERG",
+                                  "MOX/part1_ari_helios", "MOX/part1_ari_serpent", "MOX/part1_aro_helios",
+                                  "MOX/part1_aro_serpent"])
 def test_reference_decks_match_oracle(name):
     path = reference_deck(name)
     _compare(deck.load(path), oracle.Oracle(path))
@@ -63,6 +65,16 @@ def test_out_of_scope_and_bad_cards():
     with pytest.raises(deck.DeckError) as e:
         deck.load(reference_deck("fixed_source"))
     assert e.value.status == ADP_ERR_UNSUPPORTED
+    # the NEACRP decks include their cards by the author's absolute paths;
+    # the include falls back to the file beside the deck, and both readers
+    # then stop at the thermal-hydraulics card, outside this path
+    path = reference_deck("NEACRP/A1")
+    with pytest.raises(deck.DeckError) as e:
+        deck.load(path)
+    assert e.value.status == ADP_ERR_UNSUPPORTED and "THER" in str(e.value)
+    with pytest.raises(oracle.OracleError) as e:
+        oracle.Oracle(path)
+    assert "THER" in str(e.value)
     bad = synth.small_core(seed=0).replace("%KERN", "%KERNEL")
     with pytest.raises(deck.DeckError) as e:
         deck.parse(bad)
