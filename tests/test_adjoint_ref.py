@@ -4,9 +4,8 @@ The dense restatement (tests/adjoint_ref.py) contracts the left and right
 eigenvectors of the oracle's assembled CMFD operators; here it is checked
 against central differences of the dense eigenvalue with dn frozen, and,
 for the FDM kernel (dn = 0), against differences of the oracle's full
-solve.  For SANM the frozen-dn derivative is compared with differences of
-the full nodal solve to record how far the frozen coupling is from the
-nonlinear fixed point's derivative (signs agree; magnitudes do not).
+solve.  The derivative through the nodal update (SANM/PNM), which the
+frozen-dn formula leaves out, is checked in tests/test_adjoint_full_ref.py.
 """
 import numpy as np
 import pytest
@@ -79,25 +78,3 @@ def test_fdm_formula_matches_fd_of_full_solve():
                        (int(np.argmax(phi[:, 0])), 0, "sigtr")):
         fd = _full_fd(d, kind, n, g, 1e-3, base, k0)
         assert abs(S[n, g, KINDS.index(kind)] - fd) <= 1e-3 * abs(fd), kind
-
-
-def test_sanm_frozen_dn_against_full_nodal_fd():
-    """The full nodal solve re-converges dn, which depends on the node's cross
-    sections through the two-node problems; the frozen-dn derivative omits
-    that path.  On these 7.5 cm nodes the two differ by several percent up to
-    tens of percent per node (printed); their signs agree."""
-    d = _dense("SANM", 1, 2)
-    k, phi, psi = d.eig()
-    S = d.analytic_sens(k, phi, psi)
-    base = {a: d.o.array(a).copy() for a in ("f0", "fs0", "dn", "D", "sigr", "siga", "sigtr", "nuf", "sigs")}
-    k0 = d.o.getd("Ke")
-    d.o.seti("nupd", 1)          # re-converge dn at every outer: the nonlinear fixed point
-    gaps = []
-    for n, g, kind in ((int(np.argmax(phi[:, 1])), 1, "siga"), (int(np.argmax(phi[:, 0])), 0, "nuf"),
-                       (int(np.argmax(phi[:, 1])), 1, "sigtr")):
-        fd = _full_fd(d, kind, n, g, 1e-3, base, k0)
-        an = S[n, g, KINDS.index(kind)]
-        assert np.sign(fd) == np.sign(an)
-        gaps.append(abs(an - fd) / abs(fd))
-    print("SANM frozen-dn vs full nodal FD, relative gaps:", ["%.2e" % x for x in gaps])
-    assert max(gaps) < 1.0
