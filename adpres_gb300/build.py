@@ -16,7 +16,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libadpres_gb300.so")
-SOURCES = ["batch_k32.cu", "batch_k64.cu", "cmfd.cu", "nodal.cu", "capi.cu", "noalloc.cu", "adjoint.cu", "batch.cu", "edits.cu", "reactivity.cu", "transfer.cu", "trans.cu"]
+SOURCES = ["batch_k32.cu", "batch_k64.cu", "cmfd.cu", "nodal.cu", "capi.cu", "noalloc.cu", "adjoint.cu", "batch.cu", "edits.cu", "reactivity.cu", "transfer.cu", "trans.cu", "nodal_adj.cu"]
 HEADERS = ["adp_device.cuh", "ff.cuh", "adp_kernels.h", "outer_body.cuh", "nodal_body.cuh", "cmfd_items.cuh", "host_geom.h", "handle.h", "batch_kernel.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -232,21 +232,42 @@ class Core:
         self._check(st)
         return self.last_report
 
-    def adjoint_sens(self, tol=0.0, trace=False):
-        """Discrete adjoint at frozen dn and dk/dSigma after a converged forward outer.
+    def adjoint_sens(self, tol=0.0, trace=False, frozen_dn=False):
+        """dk/dSigma after a converged forward outer.
 
-        Returns (dkdp (nnod, ng, 4 + ng), psi (nnod, ng), Report of the adjoint
-        solve); dkdp[:, g, c] for c = 0 D, 1 siga, 2 nuf, 3 sigtr, 4 + h sigs(g->h).
+        The derivative of k at the fixed point of the CMFD eigenproblem and
+        the nodal update (adp_adjoint_sens), or with the coupling
+        coefficients dn held at the forward solution (frozen_dn=True,
+        adp_adjoint_sens_frozen).  Returns (dkdp (nnod, ng, 4 + ng),
+        psi (nnod, ng), Report); dkdp[:, g, c] for c = 0 D, 1 siga, 2 nuf,
+        3 sigtr, 4 + h sigs(g->h).
         """
         nn, G = self.nnod, self.ng
         dk = np.zeros(nn * G * (4 + G))
         psi = np.zeros(nn * G)
         rep, bufs = self._report(trace)
-        st = self.L.adp_adjoint_sens(self.h, float(tol), dptr(dk), dptr(psi), ctypes.byref(rep))
+        fn = self.L.adp_adjoint_sens_frozen if frozen_dn else self.L.adp_adjoint_sens
+        st = fn(self.h, float(tol), dptr(dk), dptr(psi), ctypes.byref(rep))
         r = self._to_report(rep, bufs)
         self.last_adjoint_ms = rep.device_ms
         self._check(st)
         return dk.reshape((nn, G, 4 + G), order="F"), psi.reshape((nn, G), order="F"), r
+
+    def nodal_vjp(self, lam):
+        """adp_nodal_vjp: lam (nnod, ng, 6) -> (phibar (nnod, ng), dnbar
+        (nnod, ng, 6), kbar, sigbar (nnod, ng, 4 + ng), residual)."""
+        nn, G = self.nnod, self.ng
+        lam = np.asfortranarray(lam, dtype=np.float64).reshape(-1, order="F")
+        if lam.size != nn * G * 6:
+            raise ValueError("lam must hold nnod * ng * 6 values")
+        pb = np.zeros(nn * G)
+        db = np.zeros(nn * G * 6)
+        sb = np.zeros(nn * G * (4 + G))
+        kb, rs = ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.adp_nodal_vjp(self.h, dptr(lam), dptr(pb), dptr(db), ctypes.byref(kb), dptr(sb),
+                                         ctypes.byref(rs)))
+        return (pb.reshape((nn, G), order="F"), db.reshape((nn, G, 6), order="F"), kb.value,
+                sb.reshape((nn, G, 4 + G), order="F"), rs.value)
 
     def state(self):
         """(f0 (nnod,ng), fs0 (nnod,), keff, dn (nnod,ng,6)) in the reference layouts."""

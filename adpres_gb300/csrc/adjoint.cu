@@ -93,61 +93,92 @@ __device__ __forceinline__ double ddf_dD(bool interior, int bc, double Dn, doubl
   return 0.0;
 }
 
-// Per node and group: out[(c * ng + g) * nnod + n], the Fortran array
-// dkdp(nnod, ng, 4 + ng) with c = 0 D, 1 siga, 2 nuf, 3 sigtr (through
-// D = 1/(3 sigtr), dD/dsigtr = -3 D^2, mod_xsec.f90:199-226) and 4 + h the
-// g -> h scattering (through sigr and the scattering source).
+// The contraction w^T (lambda dF/dp - dM/dp) phi of one node and group for
+// every parameter p of the column layout of dkdp(nnod, ng, 4 + ng):
+// c = 0 D, 1 siga, 2 nuf, 3 sigtr (through D = 1/(3 sigtr),
+// dD/dsigtr = -3 D^2, mod_xsec.f90:199-226) and 4 + h the g -> h scattering
+// (through sigr and the scattering source).  P.psi is the weight w.
+__device__ __forceinline__ void sens_raw(const SensParams& P, int n, int g, double* v) {
+  const BoxGeom& G = P.G;
+  const int NB = G.NB, ng = P.ng;
+  const double lam = 1.0 / P.keff;
+  const int b = P.act[n];
+  const unsigned m = G.nbm[b];
+  double fsa = 0.0;   // sum_g chi_g w_g at this node
+  for (int h = 0; h < ng; ++h) fsa = fma(P.chin[(size_t)h * NB + b], P.psi[(size_t)h * P.NBH + b], fsa);
+  const double ph = P.phi[(size_t)g * P.NBH + b], ps = P.psi[(size_t)g * P.NBH + b];
+  const double Dn = P.D[(size_t)g * NB + b];
+  // D: every face of the node; an interior face enters its own row and
+  // the neighbour's row with the same (harmonic-mean) coefficient.
+  double nD = 0.0;
+  for (int f = 0; f < 6; ++f) {
+    const int u = f >> 1;
+    const double hn = hdir(G, u, b);
+    if (m & (1u << f)) {
+      const int bm = b + face_off(G, f);
+      const double Dm = P.D[(size_t)g * NB + bm], hm = hdir(G, u, bm);
+      const double phm = P.phi[(size_t)g * P.NBH + bm], psm = P.psi[(size_t)g * P.NBH + bm];
+      const double d = ddf_dD(true, 0, Dn, Dm, hn, hm);
+      nD += d * (ps * (ph - phm) / hn + psm * (phm - ph) / hm);
+    } else {
+      const double d = ddf_dD(false, G.bcf[f], Dn, 0.0, hn, 0.0);
+      nD += d * ps * ph / hn;
+    }
+  }
+  v[0] = -nD;
+  v[1] = -ps * ph;          // siga (through sigr)
+  v[2] = lam * fsa * ph;    // nuf of group g
+  v[3] = -3.0 * Dn * Dn * v[0];
+  for (int h = 0; h < ng; ++h) v[4 + h] = (h != g) ? -(ps - P.psi[(size_t)h * P.NBH + b]) * ph : 0.0;
+}
+
+// Per node and group: out[(c * ng + g) * nnod + n] =
+// k^2 / (psi^T F phi) * psi^T (lambda dF/dp - dM/dp) phi, the derivative at
+// frozen dn.
 __global__ void k_sens(SensParams P, const double* part, int nblk, double* out) {
   double tot[1];
   grid_totals<1, 0u>(part, nblk, tot);
   const double den = tot[0];
-  const BoxGeom& G = P.G;
-  const int NB = G.NB, ng = P.ng, nn = P.nnod;
-  const double k = P.keff, lam = 1.0 / k, scale = k * k / den;
-  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
-    const int b = P.act[n];
-    const unsigned m = G.nbm[b];
-    double fsa = 0.0;   // sum_g chi_g psi_g at this node
-    for (int g = 0; g < ng; ++g) fsa = fma(P.chin[(size_t)g * NB + b], P.psi[(size_t)g * P.NBH + b], fsa);
-    for (int g = 0; g < ng; ++g) {
-      const double ph = P.phi[(size_t)g * P.NBH + b], ps = P.psi[(size_t)g * P.NBH + b];
-      const double Dn = P.D[(size_t)g * NB + b];
-      // D: every face of the node; an interior face enters its own row and
-      // the neighbour's row with the same (harmonic-mean) coefficient.
-      double nD = 0.0;
-      for (int f = 0; f < 6; ++f) {
-        const int u = f >> 1;
-        const double hn = hdir(G, u, b);
-        if (m & (1u << f)) {
-          const int bm = b + face_off(G, f);
-          const double Dm = P.D[(size_t)g * NB + bm], hm = hdir(G, u, bm);
-          const double phm = P.phi[(size_t)g * P.NBH + bm], psm = P.psi[(size_t)g * P.NBH + bm];
-          const double d = ddf_dD(true, 0, Dn, Dm, hn, hm);
-          nD += d * (ps * (ph - phm) / hn + psm * (phm - ph) / hm);
-        } else {
-          const double d = ddf_dD(false, G.bcf[f], Dn, 0.0, hn, 0.0);
-          nD += d * ps * ph / hn;
-        }
-      }
-      const double sD = -nD * scale;
-      out[((size_t)0 * ng + g) * nn + n] = sD;
-      out[((size_t)1 * ng + g) * nn + n] = -ps * ph * scale;        // siga (through sigr)
-      out[((size_t)2 * ng + g) * nn + n] = lam * fsa * ph * scale;   // nuf of group g
-      out[((size_t)3 * ng + g) * nn + n] = -3.0 * Dn * Dn * sD;      // sigtr
-      for (int h = 0; h < ng; ++h) {
-        double v = 0.0;
-        if (h != g) v = -(ps - P.psi[(size_t)h * P.NBH + b]) * ph * scale;
-        out[((size_t)(4 + h) * ng + g) * nn + n] = v;
-      }
+  const int ng = P.ng, nn = P.nnod;
+  const double k = P.keff, scale = k * k / den;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nn * ng; q += gridDim.x * blockDim.x) {
+    const int n = q % nn, g = q / nn;
+    double v[4 + kMaxGroups];
+    sens_raw(P, n, g, v);
+    for (int c = 0; c < 4 + ng; ++c) out[((size_t)c * ng + g) * nn + n] = scale * v[c];
+  }
+}
+
+// The derivative through the nodal update: out = KS (1 + s) + NS +
+// Gam^T (lambda dF/dp - dM/dp) phi, with KS the frozen-dn derivative, s =
+// lam^T dN/dk (scal[0]), NS = lam^T dN/dp and P.psi = Gam.
+__global__ void k_sens_total(SensParams P, const double* KS, const double* NS, const double* scal, double* out) {
+  const int ng = P.ng, nn = P.nnod;
+  const double s1 = 1.0 + scal[0];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nn * ng; q += gridDim.x * blockDim.x) {
+    const int n = q % nn, g = q / nn;
+    double v[4 + kMaxGroups];
+    sens_raw(P, n, g, v);
+    for (int c = 0; c < 4 + ng; ++c) {
+      const size_t i = ((size_t)c * ng + g) * nn + n;
+      out[i] = KS[i] * s1 + NS[i] + v[c];
     }
   }
+}
+
+cudaError_t launch_sens_total(const SensParams& P, const double* KS, const double* NS, const double* scal, double* out,
+                              cudaStream_t st) {
+  int b2 = (P.nnod * P.ng + 255) / 256;
+  if (b2 > 4096) b2 = 4096;
+  k_sens_total<<<b2, 256, 0, st>>>(P, KS, NS, scal, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st) {
   int blocks = (P.G.NB + 255) / 256;
   if (blocks > kMaxBlocks) blocks = kMaxBlocks;
   k_sens_den<<<blocks, 256, 0, st>>>(P, part);
-  int b2 = (P.nnod + 255) / 256;
+  int b2 = (P.nnod * P.ng + 255) / 256;
   if (b2 > 4096) b2 = 4096;
   k_sens<<<b2, 256, 0, st>>>(P, part, blocks, out);
   return cudaGetLastError();

@@ -123,6 +123,24 @@ struct SensParams {
   const double* chin;
 };
 
+// Reverse-mode derivative of the nodal update (nodal_adj.cu).  Face arrays
+// use the [g][6][NB] layout at canonical slots (the minus face of every
+// node, the plus face of a node ending its line).
+struct NadjParams {
+  NodalParams N;              // the forward state being differentiated (cmode 1)
+  const double* lam;          // adjoint of the new coupling coefficients
+  double* side;               // [2][3][9G + G^2][NB] per-side adjoints of the face stage
+  double* nodeu;              // [3][7G + G^2][NB] per-direction adjoints of the node stage
+  double* Lbar;               // [3][G][NB] adjoints of the leakages L1..L3
+  double* dfbar;              // adjoint of df
+  double* dnbar;              // out: lam^T dN/dd
+  double* phibar;             // out: lam^T dN/dphi, [G][NB]
+  double* kpart;              // [kMaxBlocks] partials of lam^T dN/dk
+  double* rpart;              // [kMaxBlocks] partial maxima of |N(state) - d|
+  double* scal;               // out: [0] lam^T dN/dk, [1] max |N(state) - d|
+  double* out;                // out: lam^T dN/dSigma in the dkdp layout (nnod, G, 4 + G)
+};
+
 // One core of a batch (batch.cu): the parameter blocks of its handle plus the
 // inputs of the in-kernel cross-section update and power edit.
 struct BatchInst {
@@ -204,6 +222,7 @@ cudaError_t launch_power(const BoxGeom& G, int ng, long long NBH, const double* 
                          double* pbox, double* red, OuterCtl* ctl, cudaStream_t st);
 cudaError_t launch_sanm_consts(const NodalParams& P, cudaStream_t st);
 cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st);
+cudaError_t launch_nodal_prep(const NodalParams& P, cudaStream_t st);   // G <= 4
 cudaError_t launch_xs_updt(const BoxGeom& G, int ng, const int* act, int nnod, const double* sigtr,
                            const double* siga, const double* sigs, double* D, double* sigr, OuterCtl* ctl,
                            cudaStream_t st);
@@ -212,6 +231,25 @@ cudaError_t launch_transpose(const BoxGeom& G, int ng, const double* A, double* 
 // out = (hi, lo) with hi = (float)x, lo = (float)(x - hi) (double-float copies of the mixed path)
 cudaError_t launch_split(const double* x, float2* out, long long n, cudaStream_t st);
 cudaError_t launch_sens(const SensParams& P, double* part, double* out, cudaStream_t st);
+// out = KS (1 + scal[0]) + NS + P.psi^T (lambda dF/dp - dM/dp) phi
+cudaError_t launch_sens_total(const SensParams& P, const double* KS, const double* NS, const double* scal,
+                              double* out, cudaStream_t st);
+// derivative through the nodal update (nodal_adj.cu); G <= 4
+cudaError_t launch_nodal_adjoint(const NadjParams& Q, cudaStream_t st);
+size_t nadj_side_doubles(int ng, long long NB);
+size_t nadj_nodeu_doubles(int ng, long long NB);
+cudaError_t launch_face_contract(const BoxGeom& G, int ng, int nnod, long long NBH, const int* act,
+                                 const double* phi, const double* w, double scale, double* out, cudaStream_t st);
+cudaError_t launch_lam_update(const BoxGeom& G, int ng, int nnod, const int* act, const double* Kd,
+                              const double* dnbar, const double* cG, const double* scal, double* lam, double* part,
+                              cudaStream_t st);
+int lam_update_blocks(int ng, int nnod);
+cudaError_t launch_gpt_source(const BoxGeom& G, int ng, int nnod, long long NBH, const int* act, const double* phi,
+                              const double* v, double* part, double* src, cudaStream_t st);
+cudaError_t launch_gpt_project(const BoxGeom& G, int ng, int nnod, long long NBH, const int* act,
+                               const double* chin, const double* nuf, const double* phi, const double* psi,
+                               double* part, double* gam, double* fsg, cudaStream_t st);
+cudaError_t launch_scale_planes(const double* in, double s, double* out, long long n, cudaStream_t st);
 // node-order <-> box transfers (transfer.cu): host layout a(nn, A, B), node
 // fastest; device planes [A][B] of stride `stride` indexed by act[n]
 cudaError_t launch_nodes_to_box(const double* src, double* dst, const int* act, int nn, int A, int B,

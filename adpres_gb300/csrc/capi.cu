@@ -238,6 +238,7 @@ adp_status adp_destroy(adp_handle* h) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->ar.base) cudaFree(h->ar.base);
   if (h->adj_base) cudaFree(h->adj_base);
+  if (h->nadj_base) cudaFree(h->nadj_base);
   if (h->edit_base) cudaFree(h->edit_base);
   if (h->react_base) cudaFree(h->react_base);
   if (h->trans_base) cudaFree(h->trans_base);
@@ -1252,6 +1253,22 @@ adp_status adp_power(adp_handle* h, double* p) {
 }
 
 // Device state of the discrete adjoint, allocated once per handle.
+static SensParams sens_params(adp_handle* h, double keff, const double* phi, const double* w) {
+  SensParams S;
+  S.G = box_geom(h);
+  S.ng = h->ng;
+  S.nnod = h->nnod;
+  S.NBH = h->NBH;
+  S.keff = keff;
+  S.act = h->d_act;
+  S.phi = phi;
+  S.psi = w;
+  S.D = h->d_D;
+  S.nuf = h->d_nuf;
+  S.chin = h->d_chin;
+  return S;
+}
+
 static adp_status adj_alloc(adp_handle* h) {
   if (h->adj_base) return ADP_OK;
   const size_t NB = h->NB, G = h->ng, NBH = h->NBH, nn = h->nnod;
@@ -1288,17 +1305,12 @@ static adp_status adj_alloc(adp_handle* h) {
   return ADP_OK;
 }
 
-adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* rep) {
-  if (!h) return ADP_ERR_INPUT;
-  CK(cudaSetDevice(h->dev));
-  if (!h->fwd_ok)
-    return fail(h, ADP_ERR_STATE, "adp_adjoint_sens: needs a converged forward adp_outer on the current cross sections");
-  adp_status s = adj_alloc(h);
-  if (s != ADP_OK) return s;
-  CK(cudaEventRecord(h->e0, h->st));
+// The adjoint eigen-solve at frozen dn and the frozen-dn derivative into
+// d_sens.  fwd: the forward control block; c: the adjoint's.
+static adp_status adjoint_frozen(adp_handle* h, double tol, OuterCtl& fwd, OuterCtl& c) {
   CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  const OuterCtl fwd = *h->h_ctl;
+  fwd = *h->h_ctl;
   // A^T of the converged forward matrix (dn frozen)
   CK(launch_transpose(box_geom(h), h->ng, h->d_A, h->d_AT, h->d_AT32, h->d_AT2, h->st));
   OuterParams P = outer_params(h, 1);
@@ -1313,7 +1325,6 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
   P.do_nodal = 0;
   if (tol > 0) P.serc = P.ferc = tol;
   CK(launch_init_flux(P, h->st));
-  OuterCtl c;
   std::memset(&c, 0, sizeof c);
   c.Ke = 1.0;
   c.need_prologue = 1;
@@ -1339,37 +1350,205 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
   }
   if (result == ADP_OK && !c.converged)
     result = fail(h, ADP_ERR_MAXOUTER, "adp_adjoint_sens: the adjoint solve did not converge");
-  if (result == ADP_OK) {
-    SensParams S;
-    S.G = box_geom(h);
-    S.ng = h->ng;
-    S.nnod = h->nnod;
-    S.NBH = h->NBH;
-    S.keff = fwd.Ke;
-    S.act = h->d_act;
-    S.phi = h->d_phi[fwd.cur];
-    S.psi = h->d_psi[c.cur];
-    S.D = h->d_D;
-    S.nuf = h->d_nuf;
-    S.chin = h->d_chin;
-    CK(launch_sens(S, h->d_spart, h->d_sens, h->st));
+  if (result != ADP_OK) return result;
+  SensParams S = sens_params(h, fwd.Ke, h->d_phi[fwd.cur], h->d_psi[c.cur]);
+  CK(launch_sens(S, h->d_spart, h->d_sens, h->st));
+  return ADP_OK;
+}
+
+static adp_status nadj_alloc(adp_handle* h) {
+  if (h->nadj_base) return ADP_OK;
+  const size_t NB = h->NB, G = h->ng, NBH = h->NBH, nn = h->nnod;
+  const size_t face = G * 6 * NB * 8, sens = nn * G * (4 + G) * 8;
+  const size_t pieces[] = {nadj_side_doubles(h->ng, h->NB) * 8, nadj_nodeu_doubles(h->ng, h->NB) * 8,
+                           3 * G * NB * 8, face, face, G * NB * 8, face, face, face, kMaxBlocks * 8, kMaxBlocks * 8,
+                           4 * 8, sens, sens, G * NBH * 8, G * NBH * 8, NB * 8, NB * 8, G * NB * 8, G * NB * 8,
+                           2 * kMaxBlocks * 8, 2 * kMaxBlocks * 8, sizeof(OuterCtl)};
+  size_t bytes = 0;
+  for (size_t b : pieces) bytes += ((b + 255) & ~(size_t)255) + 256;
+  DevArena A;
+  A.size = bytes;
+  CK(cudaMalloc((void**)&A.base, bytes));
+  h->nadj_base = A.base;
+  int i = 0;
+  h->d_nside = (double*)A.take(pieces[i++]);
+  h->d_nnodeu = (double*)A.take(pieces[i++]);
+  h->d_nLbar = (double*)A.take(pieces[i++]);
+  h->d_ndfbar = (double*)A.take(pieces[i++]);
+  h->d_ndnbar = (double*)A.take(pieces[i++]);
+  h->d_nphibar = (double*)A.take(pieces[i++]);
+  h->d_lam = (double*)A.take(pieces[i++]);
+  h->d_Kd = (double*)A.take(pieces[i++]);
+  h->d_cG = (double*)A.take(pieces[i++]);
+  h->d_nkpart = (double*)A.take(pieces[i++]);
+  h->d_nrpart = (double*)A.take(pieces[i++]);
+  h->d_nscal = (double*)A.take(pieces[i++]);
+  h->d_NS = (double*)A.take(pieces[i++]);
+  h->d_sens_full = (double*)A.take(pieces[i++]);
+  for (int t = 0; t < 2; ++t) h->d_gam[t] = (double*)A.take(pieces[i++]) + h->plane;
+  for (int t = 0; t < 2; ++t) h->d_fsg[t] = (double*)A.take(pieces[i++]);
+  h->d_gsrc = (double*)A.take(pieces[i++]);
+  h->d_nufk = (double*)A.take(pieces[i++]);
+  h->d_lpart = (double*)A.take(pieces[i++]);
+  h->d_gpart = (double*)A.take(pieces[i++]);
+  h->d_ctlg = (OuterCtl*)A.take(pieces[i++]);
+  if (A.used > A.size) return fail(h, ADP_ERR_CUDA, "internal: nodal adjoint arena overflow");
+  CK(cudaMemsetAsync(A.base, 0, A.size, h->st));   // halos, inactive positions and non-canonical slots stay 0
+  CK(cudaStreamSynchronize(h->st));
+  return ADP_OK;
+}
+
+// The derivative of k at the nonlinear fixed point of the CMFD eigenproblem
+// M(d) phi = (1/k) F phi and the nodal update d = N(phi, d, k):
+//   dk/dSigma = KS (1 + s) + lam^T N_Sigma + Gam^T (F_Sigma / k - M_Sigma) phi,
+//   lam = Kd (1 + s) + N_d^T lam - Gam^T M_d phi        (per face, canonical slots)
+//   (M - F/k)^T Gam = N_phi^T lam,   Gam^T F phi = 0,   s = N_k^T lam,
+// with KS, Kd the frozen-dn derivatives -k^2 psi^T (M_x - F_x/k) phi / (psi^T F phi).
+// Solved like the forward problem it is the adjoint of: rounds of `K` outer
+// iterations of the generalized adjoint Gam (the persistent kernel on the
+// transposed stencil with the eigenvalue held, nu*fission/k as the fission
+// weight and N_phi^T lam as the external source, its fundamental-mode
+// component removed after every round), each followed by the update of
+// lam, until lam's relative change is below tol.
+static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, const OuterCtl& ca, int& rounds,
+                                int& gouters, double& resid, double& lrel) {
+  adp_status s = nadj_alloc(h);
+  if (s != ADP_OK) return s;
+  const BoxGeom G = box_geom(h);
+  const int ng = h->ng, nn = h->nnod;
+  const double* phi = h->d_phi[fwd.cur];
+  const double* psi = h->d_psi[ca.cur];
+  // forward intermediates of the update at the converged state
+  NodalParams NP = nodal_params(h, 1);
+  CK(launch_nodal_prep(NP, h->st));
+  // the generalized adjoint starts at 0 with the eigenvalue held
+  const size_t gbytes = (size_t)ng * h->NBH * 8;
+  for (int t = 0; t < 2; ++t) {
+    CK(cudaMemsetAsync(h->d_gam[t] - h->plane, 0, gbytes, h->st));
+    CK(cudaMemsetAsync(h->d_fsg[t], 0, (size_t)h->NB * 8, h->st));
   }
-  CK(cudaEventRecord(h->e1, h->st));
-  CK(cudaEventSynchronize(h->e1));
-  float total_ms = 0.f;
-  cudaEventElapsedTime(&total_ms, h->e0, h->e1);
-  h->tm.adjoint_ms += total_ms;
-  h->tm.adjoint_outers += c.p;
+  // psi^T F phi (the projection of Gam = 0 changes nothing)
+  CK(launch_gpt_project(G, ng, nn, h->NBH, h->d_act, h->d_chin, h->d_nuf, phi, psi, h->d_gpart, h->d_gam[0],
+                        h->d_fsg[0], h->st));
+  std::vector<double> part(2 * kMaxBlocks);
+  CK(cudaMemcpyAsync(part.data(), h->d_gpart, part.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const int nbp = std::max(1, std::min((nn + 255) / 256, kMaxBlocks));
+  double den = 0.0;
+  for (int b = 0; b < nbp; ++b) den += part[kMaxBlocks + b];
+  const double k = fwd.Ke;
+  if (!(den != 0.0) || !std::isfinite(den)) return fail(h, ADP_ERR_NAN, "adp_adjoint_sens: psi^T F phi is zero");
+  CK(launch_face_contract(G, ng, nn, h->NBH, h->d_act, phi, psi, -k * k / den, h->d_Kd, h->st));
+  CK(cudaMemcpyAsync(h->d_lam, h->d_Kd, (size_t)ng * 6 * h->NB * 8, cudaMemcpyDeviceToDevice, h->st));
+  CK(launch_scale_planes(h->d_nuf, 1.0 / k, h->d_nufk, (long long)ng * h->NB, h->st));
+  NadjParams Q;
+  std::memset(&Q, 0, sizeof Q);
+  Q.N = NP;
+  Q.lam = h->d_lam;
+  Q.side = h->d_nside;
+  Q.nodeu = h->d_nnodeu;
+  Q.Lbar = h->d_nLbar;
+  Q.dfbar = h->d_ndfbar;
+  Q.dnbar = h->d_ndnbar;
+  Q.phibar = h->d_nphibar;
+  Q.kpart = h->d_nkpart;
+  Q.rpart = h->d_nrpart;
+  Q.scal = h->d_nscal;
+  Q.out = h->d_NS;
+  OuterParams P = outer_params(h, 1);
+  P.mixed = 0;
+  P.trans = 1;
+  P.A = h->d_AT;
+  for (int t = 0; t < 2; ++t) {
+    P.phi[t] = h->d_gam[t];
+    P.fs[t] = h->d_fsg[t];
+  }
+  P.wsrc = h->d_nufk;
+  P.exsrc = h->d_gsrc;
+  P.ctl = h->d_ctlg;
+  P.do_nodal = 1;
+  const int K = std::min(std::max(h->o.nupd, 2 * h->o.nac), std::max(h->o.nout, 1));
+  P.nupd = K;
+  P.serc = P.ferc = 0.0;   // rounds end on the count; convergence is lam's
+  int blocks, threads;
+  launch_shape(h, blocks, threads);
+  P.smem_rows = 0;
+  OuterCtl c;
+  std::memset(&c, 0, sizeof c);
+  c.Ke = k;
+  c.need_prologue = 1;
+  c.err_node = -1;
+  *h->h_ctl = c;
+  CK(cudaMemcpyAsync(h->d_ctlg, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
+  const double ltol = std::max(tol > 0 ? tol : std::min(h->o.serc, h->o.ferc), 1e-13);
+  const int max_rounds = std::max(4, 4 * h->o.nout / K);
+  const int lblk = lam_update_blocks(ng, nn);
+  std::vector<double> lp(2 * kMaxBlocks);
+  double scal[2] = {0.0, 0.0};
+  rounds = 0;
+  gouters = 0;
+  lrel = 1.0;
+  bool conv = false;
+  for (int r = 0; r < max_rounds; ++r) {
+    CK(launch_nodal_adjoint(Q, h->st));
+    CK(launch_gpt_source(G, ng, nn, h->NBH, h->d_act, phi, h->d_nphibar, h->d_gpart, h->d_gsrc, h->st));
+    CK(cudaMemsetAsync(&h->d_ctlg->p, 0, sizeof(int), h->st));
+    CK(cudaMemsetAsync(&h->d_ctlg->nodal_due, 0, sizeof(int), h->st));
+    CK(cudaMemsetAsync(&h->d_ctlg->bar_count, 0, sizeof(unsigned), h->st));
+    CK(launch_outer(P, blocks, threads, h->st));
+    CK(cudaMemcpyAsync(h->h_ctl, h->d_ctlg, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    c = *h->h_ctl;
+    if (c.status) return ctl_error(h, c);
+    gouters += c.p;
+    double* gam = h->d_gam[c.cur];
+    CK(launch_gpt_project(G, ng, nn, h->NBH, h->d_act, h->d_chin, h->d_nuf, phi, psi, h->d_gpart, gam,
+                          h->d_fsg[c.cur], h->st));
+    CK(launch_face_contract(G, ng, nn, h->NBH, h->d_act, phi, gam, 1.0, h->d_cG, h->st));
+    CK(launch_lam_update(G, ng, nn, h->d_act, h->d_Kd, h->d_ndnbar, h->d_cG, h->d_nscal, h->d_lam, h->d_lpart,
+                         h->st));
+    CK(cudaMemcpyAsync(lp.data(), h->d_lpart, lp.size() * 8, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(scal, h->d_nscal, 2 * 8, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    double d2 = 0.0, n2 = 0.0;
+    for (int b = 0; b < lblk; ++b) {
+      d2 += lp[b];
+      n2 += lp[kMaxBlocks + b];
+    }
+    ++rounds;
+    if (r == 0) resid = scal[1];
+    if (!std::isfinite(d2) || !std::isfinite(n2) || !std::isfinite(scal[0]))
+      return fail(h, ADP_ERR_NAN, "adp_adjoint_sens: non-finite adjoint of the nodal update");
+    lrel = n2 > 0.0 ? std::sqrt(d2 / n2) : 0.0;
+    if (r >= 2 && lrel < ltol) {
+      conv = true;
+      break;
+    }
+  }
+  if (!conv) return fail(h, ADP_ERR_MAXOUTER, "adp_adjoint_sens: the adjoint of the nodal update did not converge");
+  // the derivative at the final lam
+  CK(launch_nodal_adjoint(Q, h->st));
+  SensParams S = sens_params(h, k, phi, h->d_gam[c.cur]);
+  CK(launch_sens_total(S, h->d_sens, h->d_NS, h->d_nscal, h->d_sens_full, h->st));
+  return ADP_OK;
+}
+
+static adp_status adjoint_entry(adp_handle* h, double tol, bool through_nodal, double* dkdp, double* psi,
+                                adp_report* rep) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!h->fwd_ok)
+    return fail(h, ADP_ERR_STATE, "adp_adjoint_sens: needs a converged forward adp_outer on the current cross sections");
+  through_nodal = through_nodal && h->o.kern != ADP_KERN_FDM;
+  if (through_nodal && h->ng > 4)
+    return fail(h, ADP_ERR_UNSUPPORTED, "adp_adjoint_sens: the derivative through the nodal update supports ng <= 4");
+  adp_status s = adj_alloc(h);
+  if (s != ADP_OK) return s;
+  CK(cudaEventRecord(h->e0, h->st));
+  OuterCtl fwd, c;
+  adp_status result = adjoint_frozen(h, tol, fwd, c);
   if (rep) {
-    rep->outers = c.p;
-    rep->converged = c.converged;
-    rep->nodal_updates = 0;
-    rep->keff = c.Ke;
-    rep->ser = c.ser;
-    rep->fer = c.fer;
-    rep->ndmax = 0.0;
-    rep->im = rep->jm = rep->km = 0;
-    rep->device_ms = total_ms;
+    // the trace of the adjoint eigen-solve
     int n = std::min(std::min(c.p, rep->trace_cap), h->o.nout);
     if (n > 0) {
       if (rep->trace_k) CK(cudaMemcpy(rep->trace_k, h->d_tr_k, n * 8, cudaMemcpyDeviceToHost));
@@ -1379,15 +1558,100 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
       if (rep->trace_ndmax) CK(cudaMemcpy(rep->trace_ndmax, h->d_tr_ndmax, n * 8, cudaMemcpyDeviceToHost));
     }
   }
+  int rounds = 0, gouters = 0;
+  double resid = 0.0, lrel = 0.0;
+  if (result == ADP_OK && through_nodal) result = adjoint_nodal(h, tol, fwd, c, rounds, gouters, resid, lrel);
+  CK(cudaEventRecord(h->e1, h->st));
+  CK(cudaEventSynchronize(h->e1));
+  float total_ms = 0.f;
+  cudaEventElapsedTime(&total_ms, h->e0, h->e1);
+  h->tm.adjoint_ms += total_ms;
+  h->tm.adjoint_outers += c.p + gouters;
+  if (rep) {
+    rep->outers = c.p + gouters;
+    rep->converged = result == ADP_OK;
+    rep->nodal_updates = rounds;
+    rep->keff = c.Ke;
+    rep->ser = through_nodal ? lrel : c.ser;
+    rep->fer = c.fer;
+    rep->ndmax = resid;
+    rep->im = rep->jm = rep->km = 0;
+    rep->device_ms = total_ms;
+  }
   if (result != ADP_OK) return result;
   const int nn = h->nnod, G = h->ng;
-  if (dkdp) CK(cudaMemcpy(dkdp, h->d_sens, (size_t)nn * G * (4 + G) * 8, cudaMemcpyDeviceToHost));
+  const double* src = through_nodal ? h->d_sens_full : h->d_sens;
+  if (dkdp) CK(cudaMemcpy(dkdp, src, (size_t)nn * G * (4 + G) * 8, cudaMemcpyDeviceToHost));
   if (psi) {
     Xfer X;
-    adp_status s = xfer_reserve(h, h->nmat, X);
-    if (s != ADP_OK) return s;
+    adp_status s2 = xfer_reserve(h, h->nmat, X);
+    if (s2 != ADP_OK) return s2;
     return get_nodes(h, X, h->d_psi[c.cur], G, 1, h->NBH, psi);
   }
+  return ADP_OK;
+}
+
+adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* rep) {
+  return adjoint_entry(h, tol, true, dkdp, psi, rep);
+}
+
+adp_status adp_adjoint_sens_frozen(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* rep) {
+  return adjoint_entry(h, tol, false, dkdp, psi, rep);
+}
+
+adp_status adp_nodal_vjp(adp_handle* h, const double* lam, double* phibar, double* dnbar, double* kbar,
+                         double* sigbar, double* resid) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!lam) return fail(h, ADP_ERR_INPUT, "adp_nodal_vjp: null lam");
+  if (!h->xs_set || !h->started[0])
+    return fail(h, ADP_ERR_STATE, "adp_nodal_vjp: needs cross sections and a forward state");
+  if (h->o.kern == ADP_KERN_FDM) return fail(h, ADP_ERR_INPUT, "adp_nodal_vjp: the FDM kernel has no nodal update");
+  if (h->ng > 4) return fail(h, ADP_ERR_UNSUPPORTED, "adp_nodal_vjp: supports ng <= 4");
+  adp_status s = nadj_alloc(h);
+  if (s != ADP_OK) return s;
+  Xfer X;
+  if ((s = xfer_reserve(h, h->nmat, X)) != ADP_OK) return s;
+  if ((s = put_nodes(h, X, lam, h->ng, 6, h->d_lam, h->NB, 0)) != ADP_OK) return s;
+  // df of the current cross sections (matrix_setup(1), as adp_outer starts)
+  AssembleParams AP;
+  AP.G = box_geom(h);
+  AP.ng = h->ng;
+  AP.with_coupling = 1;
+  AP.D = h->d_D;
+  AP.sigr = h->d_sigr;
+  AP.df = h->d_df;
+  AP.dn = h->d_dn;
+  AP.A = h->d_A;
+  AP.A32 = h->d_A32;
+  AP.A2 = h->d_A2;
+  CK(launch_assemble(AP, h->st));
+  NodalParams NP = nodal_params(h, 1);
+  CK(launch_nodal_prep(NP, h->st));
+  NadjParams Q;
+  std::memset(&Q, 0, sizeof Q);
+  Q.N = NP;
+  Q.lam = h->d_lam;
+  Q.side = h->d_nside;
+  Q.nodeu = h->d_nnodeu;
+  Q.Lbar = h->d_nLbar;
+  Q.dfbar = h->d_ndfbar;
+  Q.dnbar = h->d_ndnbar;
+  Q.phibar = h->d_nphibar;
+  Q.kpart = h->d_nkpart;
+  Q.rpart = h->d_nrpart;
+  Q.scal = h->d_nscal;
+  Q.out = h->d_NS;
+  CK(launch_nodal_adjoint(Q, h->st));
+  double scal[2];
+  CK(cudaMemcpyAsync(scal, h->d_nscal, 16, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (kbar) *kbar = scal[0];
+  if (resid) *resid = scal[1];
+  if (phibar && (s = get_nodes(h, X, h->d_nphibar, h->ng, 1, h->NB, phibar)) != ADP_OK) return s;
+  if (dnbar && (s = get_nodes(h, X, h->d_ndnbar, h->ng, 6, h->NB, dnbar)) != ADP_OK) return s;
+  if (sigbar)
+    CK(cudaMemcpy(sigbar, h->d_NS, (size_t)h->nnod * h->ng * (4 + h->ng) * 8, cudaMemcpyDeviceToHost));
   return ADP_OK;
 }
 

@@ -112,7 +112,10 @@ cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStre
 __global__ void k_power_nodes(BoxGeom G, int ng, long long NBH, const double* phi, const double* sigf, double* pbox,
                               double* part) {
   double acc[1] = {0.0};
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < G.NB; b += gridDim.x * blockDim.x) {
+  // 64-bit index: the stride is added after the last row, so an int could
+  // wrap when NB is within one stride of 2^31
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < G.NB;
+       b += (long long)gridDim.x * blockDim.x) {
     double pw = 0.0;
     for (int g = 0; g < ng; ++g) {
       double q = phi[(size_t)g * NBH + b] * sigf[(size_t)g * G.NB + b] * G.vdel[b];
@@ -133,7 +136,9 @@ __global__ void k_power_norm(BoxGeom G, double* pbox, const double* part, int nb
     if (blockIdx.x == 0 && threadIdx.x == 0) set_status(C, ADP_ERR_ZEROPOWER);
     return;
   }
-  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < G.NB; b += gridDim.x * blockDim.x) pbox[b] = pbox[b] / tpow;
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < G.NB;
+       b += (long long)gridDim.x * blockDim.x)
+    pbox[b] = pbox[b] / tpow;
 }
 
 cudaError_t launch_power(const BoxGeom& G, int ng, long long NBH, const double* phi, const double* sigf, double* pbox,

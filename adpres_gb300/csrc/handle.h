@@ -92,6 +92,16 @@ struct adp_handle {
   double* d_fsa[2] = {nullptr, nullptr};
   adp::OuterCtl* d_ctla = nullptr;
   double *d_sens = nullptr, *d_spart = nullptr;
+  // derivative through the nodal update (adp_adjoint_sens, SANM/PNM),
+  // allocated on its first call
+  char* nadj_base = nullptr;
+  double *d_nside = nullptr, *d_nnodeu = nullptr, *d_nLbar = nullptr, *d_ndfbar = nullptr, *d_ndnbar = nullptr;
+  double *d_nphibar = nullptr, *d_lam = nullptr, *d_Kd = nullptr, *d_cG = nullptr, *d_nkpart = nullptr;
+  double *d_nrpart = nullptr, *d_nscal = nullptr, *d_NS = nullptr, *d_sens_full = nullptr;
+  double* d_gam[2] = {nullptr, nullptr};
+  double* d_fsg[2] = {nullptr, nullptr};
+  double *d_gsrc = nullptr, *d_nufk = nullptr, *d_lpart = nullptr, *d_gpart = nullptr;
+  adp::OuterCtl* d_ctlg = nullptr;
   // feedback tables of adp_fb_set, kept until the next call
   char* fb_base = nullptr;
   size_t fb_size = 0;

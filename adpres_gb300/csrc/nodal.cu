@@ -57,6 +57,30 @@ static cudaError_t nodal_ng(const NodalParams& P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// The stages of the update before the faces (get_source, then per node and
+// direction get_B, a2, a4, L1) at the current state, leaving dn unchanged:
+// the forward quantities the derivative of the update reads.
+template <int NG>
+static cudaError_t nodal_prep_ng(const NodalParams& P, cudaStream_t st) {
+  int blocks1 = (P.nnod * NG + 255) / 256;
+  if (blocks1 > 8192) blocks1 = 8192;
+  k_tl_source<<<blocks1, 256, 0, st>>>(P);
+  int blocks2 = (P.nnod * 3 + 127) / 128;
+  if (blocks2 > 8192) blocks2 = 8192;
+  k_node_prep<NG><<<blocks2, 128, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_nodal_prep(const NodalParams& P, cudaStream_t st) {
+  switch (P.ng) {
+    case 1: return nodal_prep_ng<1>(P, st);
+    case 2: return nodal_prep_ng<2>(P, st);
+    case 3: return nodal_prep_ng<3>(P, st);
+    case 4: return nodal_prep_ng<4>(P, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_nodal(const NodalParams& P, cudaStream_t st) {
   switch (P.ng) {
     case 1: return nodal_ng<1>(P, st);

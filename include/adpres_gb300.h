@@ -258,30 +258,79 @@ adp_status adp_power(adp_handle* h, double* p);
  * fixed 8,448-byte array of device memory inside the library, held on every
  * GPU that loads the library until the process exits.  The first call on a
  * device looks up that array's device address (cudaGetSymbolAddress), so
- * make the first call on each device before any stream capture.  All calls
- * share the array: calls that overlap on the GPU race; serialise them.
- * Errors: message through adp_last_error(NULL). */
+ * make the first call on each device before any stream capture; the
+ * address is kept for the life of the process, so a cudaDeviceReset (or
+ * any re-creation of the device's primary context) between calls is not
+ * supported.  All calls share the array: calls that overlap on the GPU
+ * race; serialise them.  On an error the contents of p are unspecified (on
+ * ADP_ERR_ZEROPOWER it holds the unnormalised per-node powers).  Errors:
+ * message through adp_last_error(NULL). */
 adp_status adp_power_noalloc(int nnod, int ng, const double* f0, const double* sigf, const double* vdel, double* p,
                              void* stream);
 
 /* Discrete adjoint and dk/dSigma; no counterpart in the reference (its
  * outer_ad, mod_cmfd.f90:602-699, solves the physical adjoint with its own
  * adjoint nodal update and the untransposed matrix).  Needs a converged
- * forward adp_outer on the current cross sections.  With dn frozen at the
- * forward solution the CMFD problem is M phi = (1/k) F phi; this call
- * solves M^T psi = (1/k) F^T psi with the persistent kernel on the
- * transposed stencil (source weights and group sweep of outer_ad), starting
- * from psi = 1, until ser < tol and fer < tol (tol <= 0: the handle's serc
- * and ferc), then
- *   dk/dp = k^2 psi^T ((1/k) dF/dp - dM/dp) phi / (psi^T F phi)
- * for every node parameter.  dkdp (nnod, ng, 4 + ng), node index fastest:
+ * forward adp_outer on the current cross sections.
+ *
+ * The converged state is the fixed point of the CMFD eigenproblem
+ * M(d) phi = (1/k) F phi (matrix_setup + TSrc, mod_cmfd.f90:217-304,
+ * :1006-1033) and of the nodal update d = N(phi, d, k) of the faces'
+ * coupling coefficients (nodal_update, mod_nodal.f90:18-278).  This call
+ * returns the derivative of k at that fixed point:
+ *   dk/dp = KS_p (1 + s) + lam^T dN/dp + Gam^T ((1/k) dF/dp - dM/dp) phi,
+ * where KS_p = k^2 psi^T ((1/k) dF/dp - dM/dp) phi / (psi^T F phi) is the
+ * derivative at frozen d with psi the adjoint of M^T psi = (1/k) F^T psi
+ * (solved with the persistent kernel on the transposed stencil, source
+ * weights and group sweep of outer_ad, from psi = 1 until ser < tol and
+ * fer < tol; tol <= 0: the handle's serc and ferc), lam the adjoint of the
+ * face coefficients, s = lam^T dN/dk, and Gam the generalized adjoint of
+ * the flux: (M - F/k)^T Gam = lam^T dN/dphi with Gam^T F phi = 0.  lam and
+ * Gam are iterated together as the forward iteration is (rounds of
+ * max(nupd, 2 nac) outers of Gam, each followed by the reverse-mode
+ * derivative of the nodal update at the converged state and an update of
+ * lam) until lam's relative change is below tol (at least 1e-13).  For the
+ * FDM kernel (d = 0) the frozen-d derivative is the whole derivative.  The
+ * result is the derivative of the fixed point the forward state sits at:
+ * converge the forward solve tightly (small serc, ferc) for a tight result.
+ * report->ndmax is the fixed-point residual max |N(phi, d, k) - d| at the
+ * state, report->nodal_updates the rounds, report->ser lam's last relative
+ * change.  Needs ng <= 4 for SANM/PNM (ADP_ERR_UNSUPPORTED otherwise).
+ *
+ * dkdp (nnod, ng, 4 + ng), node index fastest:
  * [:,g,1] dk/dD_g, [:,g,2] dk/dsiga_g, [:,g,3] dk/dnuf_g, [:,g,4]
  * dk/dsigtr_g (= -3 D_g^2 dk/dD_g, the chain rule of D = 1/(3 sigtr)),
  * [:,g,4+h] dk/dsigs(g->h) (through sigr and the scattering source; 0 for
  * h = g).  psi (nnod, ng) receives the adjoint flux (unnormalised); either
  * output may be NULL.  report (may be NULL) describes the adjoint solve
- * (keff is its eigenvalue).  The forward state is left unchanged. */
+ * (keff is its eigenvalue; outers count the adjoint and Gam outers).  The
+ * forward state is left unchanged. */
 adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* report);
+
+/* The derivative with the faces' coupling coefficients d held at the
+ * forward solution (KS_p above): the derivative of the CMFD eigenvalue at
+ * fixed d, which adp_outer(ADP_FORWARD | ADP_FROZEN_DN) solves for.  Same
+ * arguments and outputs as adp_adjoint_sens.  No counterpart in the
+ * reference. */
+adp_status adp_adjoint_sens_frozen(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* report);
+
+/* Reverse-mode derivative of one nodal update (nodal_update /
+ * nodal_update_pnm, mod_nodal.f90:18-278, static form) at the handle's
+ * current state (flux, coupling coefficients dn, eigenvalue, cross
+ * sections): the update is a function N(phi, d, k; Sigma) of the flux, the
+ * faces' coupling coefficients d, k and the cross sections, and for an
+ * adjoint lam of its new coefficients this returns lam^T dN/dphi in phibar
+ * (nnod, ng), lam^T dN/dd in dnbar (nnod, ng, 6), lam^T dN/dk in *kbar and
+ * lam^T dN/dp in sigbar (nnod, ng, 4 + ng), the dkdp layout of
+ * adp_adjoint_sens.  Face arrays use the reference's nod%dn layout; an
+ * interior face's coefficient is one variable, held in the slot of the
+ * face's plus-side node (its minus face; a boundary face in its own slot):
+ * lam is read there and dnbar written there, other slots are ignored on
+ * input and 0 on output.  *resid receives max |N(phi, d, k) - d| at the
+ * state.  The building block of adp_adjoint_sens; no counterpart in the
+ * reference.  Any output may be NULL.  ng <= 4; not for FDM. */
+adp_status adp_nodal_vjp(adp_handle* h, const double* lam, double* phibar, double* dnbar, double* kbar,
+                         double* sigbar, double* resid);
 
 /* -- output edits of control::forward (mod_control.f90:33-44) -------------- */
 

@@ -177,6 +177,24 @@ module adpres_gb300_bind
       type(adp_report), intent(inout) :: rep
     end function
 
+    ! the same with nod%dn held at the forward solution
+    integer(c_int) function adp_adjoint_sens_frozen(h, tol, dkdp, psi, rep) bind(C, name="adp_adjoint_sens_frozen")
+      import :: c_int, c_ptr, c_double, adp_report
+      type(c_ptr), value :: h
+      real(c_double), value :: tol
+      real(c_double), intent(out) :: dkdp(*), psi(*)
+      type(adp_report), intent(inout) :: rep
+    end function
+
+    ! reverse-mode derivative of one nodal update at the current state
+    integer(c_int) function adp_nodal_vjp(h, lam, phibar, dnbar, kbar, sigbar, resid) bind(C, name="adp_nodal_vjp")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(in) :: lam(*)
+      real(c_double), intent(out) :: phibar(*), dnbar(*), sigbar(*)
+      real(c_double), intent(out) :: kbar, resid
+    end function
+
     ! output edits of control::forward (mod_io.f90:3267-3644)
     integer(c_int) function adp_edit_asmpow(h, nx, ny, xdiv, ydiv, fasm, imax, jmax) bind(C, name="adp_edit_asmpow")
       import :: c_int, c_ptr, c_double

@@ -149,19 +149,25 @@ class FullAdjoint:
         return self.layout(tot), self.layout(KS), lam
 
     def layout(self, g):
-        nn, ng = self.nn, self.ng
-        out = np.zeros((nn, ng, 4 + ng))
-        D = self.p["D"].numpy()
-        out[:, :, 0] = g["D"].numpy()
-        out[:, :, 1] = g["siga"].numpy()
-        out[:, :, 2] = g["nuf"].numpy()
-        out[:, :, 3] = -3.0 * D * D * out[:, :, 0]
-        sg = g["sigs"].numpy()
-        for h in range(ng):
-            col = sg[:, :, h].copy()
-            col[:, h] = 0.0
-            out[:, :, 4 + h] = col
-        return out
+        return dkdp_layout(self.p["D"], g)
+
+
+def dkdp_layout(D, g):
+    """Gradients with respect to D, siga, nuf (nn, ng) and sigs (nn, ng, ng)
+    in the dkdp layout (nn, ng, 4 + ng) of adp_adjoint_sens."""
+    D = D.numpy()
+    nn, ng = D.shape
+    out = np.zeros((nn, ng, 4 + ng))
+    out[:, :, 0] = g["D"].numpy()
+    out[:, :, 1] = g["siga"].numpy()
+    out[:, :, 2] = g["nuf"].numpy()
+    out[:, :, 3] = -3.0 * D * D * out[:, :, 0]
+    sg = g["sigs"].numpy()
+    for h in range(ng):
+        col = sg[:, :, h].copy()
+        col[:, h] = 0.0
+        out[:, :, 4 + h] = col
+    return out
 
 
 def converge_fixed_point(o, tol=1e-12, nupd=None):

@@ -1,7 +1,7 @@
 """Discrete adjoint and dk/dSigma on the GPU, through the C ABI.
 
 Checks, on the same inputs:
-  * dk/dp of adp_adjoint_sens against the dense restatement (tests/adjoint_ref.py)
+  * dk/dp at frozen dn (adp_adjoint_sens_frozen) against the dense restatement (tests/adjoint_ref.py)
     built from the oracle's assembled operators: every entry, 1e-6 of the
     largest entry of its kind;
   * against central finite differences of k at dn frozen (relative step
@@ -55,7 +55,7 @@ CASES = [("FDM", 6, 2, False), ("SANM", 1, 2, False), ("PNM", 4, 2, True), ("SAN
 def test_sens_matches_dense_restatement(kern, seed, ng, adf):
     text = synth.small_core(seed=seed, ng=ng, kern=kern, adf=adf)
     dk, c, rep = _gpu(text)
-    S, psi, arep = c.adjoint_sens(tol=TIGHT)
+    S, psi, arep = c.adjoint_sens(tol=TIGHT, frozen_dn=True)
     assert arep.converged
     # the discrete adjoint has the forward eigenvalue
     assert abs(arep.keff - rep.keff) <= 1e-10 * rep.keff
@@ -82,7 +82,7 @@ def test_sens_matches_dense_fd_frozen_dn(kern, seed, ng, adf):
     compared."""
     text = synth.small_core(seed=seed, ng=ng, kern=kern, adf=adf)
     dk, c, rep = _gpu(text)
-    S, _, _ = c.adjoint_sens(tol=TIGHT)
+    S, _, _ = c.adjoint_sens(tol=TIGHT, frozen_dn=True)
     d = Dense(_oracle(text))
     rng = np.random.default_rng(100 + seed)
     checked, worst = 0, 0.0
@@ -183,7 +183,7 @@ def test_full_core_3d_sens_matches_frozen_fd():
     step 1e-4 of warm-started GPU FP64 solves with dn frozen, <= 1e-3."""
     text = synth.full_core_3d(0)
     dk, c, rep = _gpu(text, tol=1e-13)
-    S, psi, arep = c.adjoint_sens(tol=1e-13)
+    S, psi, arep = c.adjoint_sens(tol=1e-13, frozen_dn=True)
     assert arep.converged
     state = c.state()
     tabs = _node_tables(dk)
@@ -218,9 +218,9 @@ def test_full_core_3d_sens_matches_frozen_fd():
 def test_mixed_precision_sens_close_to_fp64():
     text = synth.quarter_core_2d(1)
     _, c64, _ = _gpu(text, "fp64", tol=1e-10)
-    S64, _, _ = c64.adjoint_sens(tol=1e-10)
+    S64, _, _ = c64.adjoint_sens(tol=1e-10, frozen_dn=True)
     _, c32, _ = _gpu(text, "mixed", tol=1e-10)
-    S32, _, _ = c32.adjoint_sens(tol=1e-10)
+    S32, _, _ = c32.adjoint_sens(tol=1e-10, frozen_dn=True)
     for ci in range(S64.shape[2]):
         scale = np.max(np.abs(S64[:, :, ci]))
         if scale:

@@ -98,7 +98,7 @@ def test_reactivity_static_identity_on_gpu_solution():
     from adpres_gb300.core import Core
     c = Core.from_deck(deck.parse(synth.quarter_core_2d(0)), serc=1e-12, ferc=1e-12)
     rep = c.outer(trace=False)
-    S, psi, _ = c.adjoint_sens(tol=1e-12)
+    S, psi, _ = c.adjoint_sens(tol=1e-12, frozen_dn=True)
     nn, ng = c.nnod, c.ng
     for af in (np.ones((nn, ng)), psi):
         assert abs(c.reactivity(af) - (1 - 1 / rep.keff)) < 1e-9

@@ -63,9 +63,42 @@ def test_power_noalloc_rejects_sizes_and_zero_power():
     st = L.adp_power_noalloc(4, 2, ctypes.c_void_p(z.data_ptr()), ctypes.c_void_p(z.data_ptr()),
                              ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(out.data_ptr()), nul)
     assert st == _lib.ADP_ERR_ZEROPOWER
+    # on that error p holds the unnormalised per-node powers (all zero here)
+    assert np.all(out.cpu().numpy() == 0.0)
     # the status word is cleared per call: a valid call afterwards succeeds
     f = torch.ones(8, dtype=torch.float64, device="cuda")
     st = L.adp_power_noalloc(4, 2, ctypes.c_void_p(f.data_ptr()), ctypes.c_void_p(f.data_ptr()),
                              ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(out.data_ptr()), nul)
     assert st == _lib.ADP_OK
     np.testing.assert_allclose(out.cpu().numpy(), np.full(4, 0.25))
+
+
+def test_power_noalloc_many_blocks_matches_adp_power():
+    """A core of more than 262,144 nodes (the 68x68x80 four-group core,
+    369,920 nodes): more blocks than the scratch holds partial sums for, so
+    the launch is capped at that many blocks and each block sums several
+    rows per thread.  A seeded positive flux, through adp_power on a handle
+    and through the allocation-free call twice."""
+    torch = pytest.importorskip("torch")
+    from adpres_gb300 import _lib, deck, synth
+    from adpres_gb300.core import Core
+    dk = deck.parse(synth.core_4g(0))
+    assert dk.nnod > 1024 * 256
+    c = Core.from_deck(dk)
+    rng = np.random.default_rng(5)
+    f0 = rng.uniform(0.1, 2.0, (dk.nnod, dk.ng))
+    c.set_state(f0=f0, fs0=np.ones(dk.nnod), keff=1.0)
+    p_ref = c.power()
+    c.close()
+    L = _lib.load()
+    vdel = dk.xdel[dk.ix - 1] * dk.ydel[dk.iy - 1] * dk.zdel[dk.iz - 1]
+    sigf = dk.xsigf[dk.mat - 1]
+    d_f0 = torch.tensor(np.asfortranarray(f0).reshape(-1, order="F"), dtype=torch.float64, device="cuda")
+    d_sf = torch.tensor(np.asfortranarray(sigf).reshape(-1, order="F"), dtype=torch.float64, device="cuda")
+    d_v = torch.tensor(vdel, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        d_p = torch.full((dk.nnod,), -1.0, dtype=torch.float64, device="cuda")
+        st = L.adp_power_noalloc(dk.nnod, dk.ng, ctypes.c_void_p(d_f0.data_ptr()), ctypes.c_void_p(d_sf.data_ptr()),
+                                 ctypes.c_void_p(d_v.data_ptr()), ctypes.c_void_p(d_p.data_ptr()), ctypes.c_void_p(0))
+        assert st == _lib.ADP_OK, _lib.last_error(None)
+        np.testing.assert_allclose(d_p.cpu().numpy(), p_ref, rtol=PTOL, atol=0)
