@@ -253,6 +253,15 @@ class Core:
         self._check(st)
         return dk.reshape((nn, G, 4 + G), order="F"), psi.reshape((nn, G), order="F"), r
 
+    def set_wait_limit(self, seconds):
+        """adp_set_wait_limit: time limit of a grid-barrier wait (0: 2 s)."""
+        self._check(self.L.adp_set_wait_limit(self.h, float(seconds)))
+
+    def test_missing_block(self, on=True):
+        """adp_test_missing_block: make every barrier wait of the next forward
+        outers run out (ADP_ERR_TIMEOUT), for tests of the timeout path."""
+        self._check(self.L.adp_test_missing_block(self.h, int(bool(on))))
+
     def nodal_vjp(self, lam):
         """adp_nodal_vjp: lam (nnod, ng, 6) -> (phibar (nnod, ng), dnbar
         (nnod, ng, 6), kbar, sigbar (nnod, ng, 4 + ng), residual)."""

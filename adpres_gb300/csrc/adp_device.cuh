@@ -45,7 +45,8 @@ struct OuterCtl {
   int pad0;
   unsigned bar_count; // grid barrier state
   unsigned bar_gen;
-  unsigned pad1[14];
+  unsigned long long wait_ns;  // time limit of a barrier wait; 0: kBarrierTimeoutNs
+  unsigned pad1[12];
 };
 
 // Box geometry shared by all kernels.  Box index b = i + nxx*(j + nyy*k),
@@ -113,9 +114,10 @@ __device__ __forceinline__ void set_status(OuterCtl* C, int code) {
 // block adds 1, so the top bit flips exactly when the last block arrives
 // and the low bits return to zero; each block waits until the top bit
 // differs from the value its own add returned.  The word must be 0 when the
-// team first uses it.  The wait is bounded: after kBarrierTimeoutNs the
-// block records ADP_ERR_TIMEOUT and returns false, so a fault elsewhere can
-// never leave the kernel spinning.  Called by lane 0 of one warp.
+// team first uses it.  The wait is bounded: after C->wait_ns (when 0,
+// kBarrierTimeoutNs) the block records ADP_ERR_TIMEOUT and returns false, so
+// a fault elsewhere can never leave the kernel spinning.  Called by lane 0
+// of one warp.
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 // The arrival is an acquire-release add (it publishes this block's writes,
@@ -127,6 +129,8 @@ constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 // of the team runs out of time too and the kernel ends.
 __device__ __forceinline__ int team_arrive_wait(OuterCtl* C, unsigned nblocks, unsigned rank) {
   int ok = 1;
+  const unsigned long long lim0 = *(const volatile unsigned long long*)&C->wait_ns;
+  const unsigned long long lim = lim0 ? lim0 : kBarrierTimeoutNs;
   const unsigned add = (rank == 0) ? (0x80000000u - (nblocks - 1u)) : 1u;
   const unsigned old = atom_add_acqrel_gpu(&C->bar_count, add);
   if (!(((old + add) ^ old) & 0x80000000u)) {
@@ -136,7 +140,7 @@ __device__ __forceinline__ int team_arrive_wait(OuterCtl* C, unsigned nblocks, u
       if ((++spins & 63u) == 0) {
         const unsigned long long t = globaltimer_ns();
         if (t0 == 0) t0 = t;
-        else if (t - t0 > kBarrierTimeoutNs) {
+        else if (t - t0 > lim) {
           set_status(C, ADP_ERR_TIMEOUT);
           ok = 0;
           break;

@@ -19,6 +19,8 @@ struct OuterParams {
   int ng, nin, nac, nupd, nout, adj, do_nodal, mixed;
   int smem_rows;              // > 0: rows per block of the matrix copy in shared memory
   int trans;                  // 1: outer_tr (mod_cmfd.f90:800-868): source wsrc fs + s0 + exsrc, no k update
+  int phantom;                // team members counted by the barriers beyond the launched blocks (0; 1 makes
+                              // every barrier wait run out: the host-side test of ADP_ERR_TIMEOUT)
   // Source planes that hold a nonzero value at some node: bit g of src_nz
   // for wsrc of group g, bit a*ng + c of sc_nz for sigs plane [a][c].  P0
   // skips the terms of all-zero planes (adding an exact zero changes no

@@ -1018,6 +1018,19 @@ adp_status adp_set_launch(adp_handle* h, int blocks, int threads) {
   return ADP_OK;
 }
 
+adp_status adp_set_wait_limit(adp_handle* h, double seconds) {
+  if (!h) return ADP_ERR_INPUT;
+  if (!(seconds >= 0.0) || seconds > 60.0) return fail(h, ADP_ERR_INPUT, "adp_set_wait_limit: seconds must be in [0, 60]");
+  h->wait_ns = (unsigned long long)(seconds * 1e9);
+  return ADP_OK;
+}
+
+adp_status adp_test_missing_block(adp_handle* h, int on) {
+  if (!h) return ADP_ERR_INPUT;
+  h->phantom = on ? 1 : 0;
+  return ADP_OK;
+}
+
 adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   if (!h) return ADP_ERR_INPUT;
   CK(cudaSetDevice(h->dev));
@@ -1062,6 +1075,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   c.need_prologue = 1;
   c.err_node = -1;
   c.bar_count = 0;
+  c.wait_ns = h->wait_ns;
   if (frozen) c.ndmax = 0.0;
   const int nod0 = c.nodal_updates;
   const long outers0 = c.p_total;
@@ -1069,6 +1083,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
   const int do_nodal = !frozen && (h->o.kern != ADP_KERN_FDM) && (!adj || popt > 0);
   P.do_nodal = do_nodal;
+  P.phantom = h->phantom;
   NodalParams NP = nodal_params(h, adj ? 0 : (h->trans_on ? 2 : 1));
   if (h->trans_on) {
     // outer_tr (mod_cmfd.f90:800-868): the FP64 kernel with the step's
@@ -1329,6 +1344,7 @@ static adp_status adjoint_frozen(adp_handle* h, double tol, OuterCtl& fwd, Outer
   c.Ke = 1.0;
   c.need_prologue = 1;
   c.err_node = -1;
+  c.wait_ns = h->wait_ns;
   *h->h_ctl = c;
   CK(cudaMemcpyAsync(h->d_ctla, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
   int blocks, threads;
@@ -1478,6 +1494,7 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
   c.Ke = k;
   c.need_prologue = 1;
   c.err_node = -1;
+  c.wait_ns = h->wait_ns;
   *h->h_ctl = c;
   CK(cudaMemcpyAsync(h->d_ctlg, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
   const double ltol = std::max(tol > 0 ? tol : std::min(h->o.serc, h->o.ferc), 1e-13);

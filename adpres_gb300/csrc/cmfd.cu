@@ -64,7 +64,7 @@ cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
 
 template <bool MIXED, bool SMEMA>
 __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
-  outer_body<MIXED, SMEMA>(P, blockIdx.x, gridDim.x);
+  outer_body<MIXED, SMEMA>(P, blockIdx.x, gridDim.x + P.phantom);
 }
 
 int outer_max_blocks_per_sm(int threads, int mixed) {

@@ -133,6 +133,8 @@ struct adp_handle {
   bool fwd_ok = false;        // the flux is a converged forward solution of the current XS
   bool started[2] = {false, false};
   int launch_blocks = 0, launch_threads = 0;
+  unsigned long long wait_ns = 0;   // barrier wait limit of the persistent kernels (0: the default 2 s)
+  int phantom = 0;                  // adp_test_missing_block
   int sms = 0;
   adp_timers tm{};
 };

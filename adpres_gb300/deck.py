@@ -3,9 +3,12 @@
 Cards handled as in src/mod_io.f90: %MODE (:580-640), %CASE, %XSEC
 (:683-805), %GEOM (:809-1289 with the node ordering of misc, :1293-1365),
 %ADF with rotations (:1732-2144), %ITER (:1522-1569), %KERN (:1593-1646)
-and %PRNT (:1693-1728); comments after '!' (:452-492) and the FILE include
-keyword (:519-535).  Cards that belong to feedback, transient or
-fixed-source calculations raise DeckError with ADP_ERR_UNSUPPORTED.
+and %PRNT (:1693-1728); the feedback cards %CROD, %CBCS, %BCON, %FTEM,
+%MTEM, %CDEN (:2148-2954) and the transient cards %EJCT, %THET, %EXTR
+(:1650-1689, :2332-2482); comments after '!' (:452-492) and the FILE
+include keyword (:519-535).  %ESRC (fixed source), %THER (thermal
+hydraulics) and %XTAB (branch tables) raise DeckError with
+ADP_ERR_UNSUPPORTED.
 
 The result is the reference's sdata state for this path: geometry and node
 order, material cross sections, ADFs per node, iteration control.

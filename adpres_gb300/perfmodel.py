@@ -58,3 +58,12 @@ def p0_skipped_bytes_per_row_outer(xsigs, chi, mat) -> float:
     zc = sum(1 for g in range(G) if not np.any(ch[:, g] != 0.0))
     return 16.0 * (zs + zc)
 
+
+def canonical_bytes_per_node_outer(ng: int, nin: int, w: int) -> float:
+    """Canonical algorithmic bytes of one outer per node: w-byte words, 31
+    per BiCGSTAB step (fused in three phases), 2G + 11 for each group's
+    source and initial residual, 3G + 3 for the fission source and the norms:
+    w [G (31 nin + 2G + 11) + 3G + 3].  w = 8 for FP64 storage, 4 for the
+    FP32-storage form of the mixed path."""
+    G = ng
+    return float(w * (G * (31 * nin + 2 * G + 11) + 3 * G + 3))

@@ -36,11 +36,10 @@ METRIC = "k-eig solves/s (mixed FP32/FP64, |dk| <= 1 pcm vs FP64)"
 UNIT = "solves/s"
 CONFIG_NAME = "core_4g"
 SEED = 0
-# Outer iterations and nodal updates of one full solve of this core by the
-# oracle (FP64, measured: 234 outers, 2 nodal updates, k = 1.232556358).
-ORACLE_OUTERS = 234
-ORACLE_NODAL = 2
-CPU_SAMPLE_OUTERS = 12
+# Outers timed per process by the reference arm's bounded sample; the
+# sample is scaled by the outers and nodal updates of a full solve of the
+# same core that the arm times in its warm-up.
+CPU_SAMPLE_OUTERS = 4
 
 
 def log(*a):
@@ -121,59 +120,75 @@ def cpu_sample(text, outers):
     return t_outer, t_nodal
 
 
+def cpu_full_solve(text):
+    """One full solve of the oracle from a cold start: (seconds, outers,
+    nodal updates, k)."""
+    import oracle
+    o = oracle.Oracle(text=text)
+    t0 = time.perf_counter()
+    o.run()
+    t = time.perf_counter() - t0
+    nodal = sum(1 for r in o.trace() if r.nodal)
+    return t, o.geti("outers"), nodal, o.getd("Ke")
+
+
 def _worker(args):
     text, outers = args
     return cpu_sample(text, outers)
 
 
-def est_solve_seconds(t_outer, t_nodal):
-    return ORACLE_OUTERS * t_outer + ORACLE_NODAL * t_nodal
+def _full_worker(text):
+    return cpu_full_solve(text)
 
 
 def cpu_baseline_single(text):
-    t_outer, t_nodal = cpu_sample(text, CPU_SAMPLE_OUTERS)
-    est = est_solve_seconds(t_outer, t_nodal)
-    return {"value": 1.0 / est, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"oracle (CPU restatement of the reference loops, -O2, 1 core): {CPU_SAMPLE_OUTERS} outer "
-                      f"iterations ({t_outer * 1e3:.1f} ms each) and one nodal update ({t_nodal * 1e3:.0f} ms) of this "
-                      f"core, scaled to its full solve of {ORACLE_OUTERS} outers and {ORACLE_NODAL} nodal updates "
-                      f"({est:.1f} s)"}
+    t, outers, nodal, k = cpu_full_solve(text)
+    return {"value": 1.0 / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle (CPU restatement of the reference loops, -O2, 1 core): one full solve of this core "
+                      f"from a cold start, {t:.1f} s ({outers} outers, {nodal} nodal updates, k = {k:.9f})",
+            "outers": outers, "nodal_updates": nodal, "seconds": t}
 
 
 # ------------------------------------------------ dk/dSigma leg ----
 def adjoint_leg(flush, steps=3):
-    """Forward solve + discrete adjoint + contraction on the 34x34x22-node
-    two-group full core (seed 0), mixed precision and FP64; gradients/s
-    counts D, siga, nuf per group and the 1->2 scattering per node."""
+    """Forward solve + adjoint + dk/dSigma on the 34x34x22-node two-group
+    full core (seed 0), mixed precision and FP64, with the deck's iteration
+    control: the derivative at frozen dn (adp_adjoint_sens_frozen) and the
+    derivative of the fixed point through the nodal update
+    (adp_adjoint_sens).  gradients/s counts D, siga, nuf per group and the
+    1->2 scattering per node."""
     import torch
 
     from adpres_gb300 import deck, synth
     from adpres_gb300.core import Core
 
     dk = deck.parse(synth.full_core_3d(0))
-    out = {"workload": "full_core_3d seed 0: 34x34 radial nodes x 22 planes, 2 groups, SANM",
+    out = {"workload": "full_core_3d seed 0: 34x34 radial nodes x 22 planes, 2 groups, SANM, serc = ferc = 1e-5",
            "params_per_solve": int(dk.nnod * (3 * dk.ng + dk.ng * (dk.ng - 1) // 2))}
     for prec in ("mixed", "fp64"):
         c = Core.from_deck(dk, precision=prec)
+        for mode in ("frozen_dn", "fixed_point"):
+            def run():
+                c.reset()
+                r = c.outer(trace=False)
+                _, _, a = c.adjoint_sens(frozen_dn=(mode == "frozen_dn"))
+                return r.device_ms, c.last_adjoint_ms, a
 
-        def run():
-            c.reset()
-            r = c.outer(trace=False)
-            c.adjoint_sens()
-            return r.device_ms, c.last_adjoint_ms
-
-        for _ in range(2):
-            run()
-        fwd, adj = [], []
-        for _ in range(steps):
-            flush.zero_()
-            torch.cuda.synchronize()
-            f, a = run()
-            fwd.append(f)
-            adj.append(a)
-        t = (sum(fwd) + sum(adj)) / steps / 1e3
-        out[prec] = {"grads_per_s": out["params_per_solve"] / t, "ms_per_solve": t * 1e3,
-                     "forward_ms": sum(fwd) / steps, "adjoint_ms": sum(adj) / steps}
+            for _ in range(2):
+                run()
+            fwd, adj = [], []
+            for _ in range(steps):
+                flush.zero_()
+                torch.cuda.synchronize()
+                f, a, rep = run()
+                fwd.append(f)
+                adj.append(a)
+            t = (sum(fwd) + sum(adj)) / steps / 1e3
+            out["%s_%s" % (prec, mode)] = {
+                "grads_per_s": out["params_per_solve"] / t, "ms_per_solve": t * 1e3,
+                "forward_ms": sum(fwd) / steps, "adjoint_ms": sum(adj) / steps,
+                "adjoint_outers": rep.outers, "rounds": rep.nodal_updates,
+                "fixed_point_residual": rep.ndmax if mode == "fixed_point" else None}
         c.close()
     return out
 
@@ -439,10 +454,15 @@ def run_ours(args):
     kms = t_after["outer_kernel_ms"] - t_before["outer_kernel_ms"]
     n_outers = sum(outers)
     NB = dk.nxx * dk.nyy * dk.nzz
-    bytes_per_outer = NB * perfmodel.bytes_per_row_outer(dk.ng, dk.nin, dk.nac, prec)
-    bytes_per_launch = bytes_per_outer * n_outers / launches
+    # canonical algorithmic bytes (w = 4 for the FP32-storage form, 8 FP64)
+    w = 4 if prec == "mixed" else 8
+    canon_per_outer = dk.nnod * perfmodel.canonical_bytes_per_node_outer(dk.ng, dk.nin, w)
+    bytes_per_launch = canon_per_outer * n_outers / launches
     avg_launch_s = kms / 1e3 / launches
     achieved = bytes_per_launch / avg_launch_s / 1e9
+    # the kernel's own count: the words it moves at their stored widths (the
+    # FP64 / double-float P0 operands at 8 bytes)
+    kernel_bytes_per_launch = NB * perfmodel.bytes_per_row_outer(dk.ng, dk.nin, dk.nac, prec) * n_outers / launches
     # the all-zero source planes P0 leaves out (counted by the canonical figure)
     skipped_per_launch = NB * perfmodel.p0_skipped_bytes_per_row_outer(dk.xsigs, dk.chi, dk.mat) * n_outers / launches
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -455,25 +475,27 @@ def run_ours(args):
     # DRAM traffic of one launch: the ncu capture of the 68x68x40 core's first
     # launch gives the bytes per box row and outer; scaled to this launch by
     # box rows x outers per launch (the same kernel on twice the planes)
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "k_outer_mixed_core_4g.json")
+    traffic, traffic_src = None, None
+    prof = os.path.join(ROOT, "profiles", "k_outer_mixed_core_4g_planes80_dram.json")
     if os.path.exists(prof) and prec == "mixed":
         with open(prof) as f:
             pj = json.load(f)
-        traffic = pj["dram_bytes_per_row_outer"] * NB * n_outers / launches
+        traffic = pj["dram_bytes_per_outer"] * n_outers / launches
+        traffic_src = pj["capture"]
     gpu_launches = int(sum(2 + 0 for _ in outers) + launches + 5 * sum(nodal))
 
     # FP64 path on the same core: solves/s and the mixed-precision error
     core64 = Core.from_deck(dk, precision="fp64")
-    step(core64)
+    for _ in range(args.warmup):
+        step(core64)
     d64 = []
-    for _ in range(2):
+    for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         r64 = step(core64)
         d64.append(r64.device_ms)
     p64 = core64.power()
-    fp64_value = 2 / (sum(d64) / 1e3)
+    fp64_value = args.steps / (sum(d64) / 1e3)
     dk_pcm = abs(keff_mixed - r64.keff) / r64.keff * 1e5
     m = p64 > 0
     perr = np.abs(p_mixed[m] - p64[m]) / p64[m]
@@ -528,15 +550,20 @@ def run_ours(args):
         "outers_per_solve": statistics.mean(outers), "nodal_updates_per_solve": statistics.mean(nodal),
         "keff": keff_mixed,
         "fp64": {"value": fp64_value, "unit": UNIT, "keff": r64.keff, "outers": r64.outers,
-                 "mixed_speedup": value / fp64_value},
+                 "steps": args.steps, "mixed_speedup": value / fp64_value},
         "accuracy_vs_fp64": {"dk_pcm": dk_pcm, "power_max_rel": float(perr.max()),
                              "power_rms_rel": float(np.sqrt(np.mean(perr ** 2)))},
         "roofline": {"kernel": "k_outer<mixed>" if prec == "mixed" else "k_outer<fp64>", "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_src, "traffic": traffic,
+                     "peak_source": peak_src, "traffic": traffic, "traffic_source": traffic_src,
+                     "bytes": "canonical: nodes x %d B per outer (w = %d)" % (
+                         perfmodel.canonical_bytes_per_node_outer(dk.ng, dk.nin, w), w),
                      "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
-                     "launches": launches, "p0_zero_plane_bytes_skipped_per_launch": skipped_per_launch,
-                     "achieved_without_skipped": (bytes_per_launch - skipped_per_launch) / avg_launch_s / 1e9},
+                     "launches": launches, "outers_per_launch": n_outers / launches,
+                     "kernel_count_bytes_per_launch": kernel_bytes_per_launch,
+                     "kernel_count_achieved": kernel_bytes_per_launch / avg_launch_s / 1e9,
+                     "kernel_count_frac": kernel_bytes_per_launch / avg_launch_s / 1e9 / peak,
+                     "p0_zero_plane_bytes_skipped_per_launch": skipped_per_launch},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "adjoint": adjoint,
         "cbsearch": boron,
@@ -566,6 +593,14 @@ def max_over_ranks(dist, x):
 
 # ------------------------------------------------------ reference arm ----
 def run_reference(args):
+    """The reference arm: the oracle (CPU restatement of the reference's
+    loops; no Fortran compiler exists here) on all host cores, one process
+    per core.  Warm-up: every process times one full solve of the workload
+    from a cold start, which gives the solve's outers and nodal updates.
+    Each timed step: every process times a bounded sample (CPU_SAMPLE_OUTERS
+    outers and one nodal update); solves/s = processes / (outers x t_outer +
+    nodal x t_nodal).  The line also reports the warm-up's measured full
+    solves/s, which the sampled figure must agree with."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -576,10 +611,13 @@ def run_reference(args):
     text = workload_text()
     dk = deck.parse(text)
     cores = os.cpu_count() or 1
-    outers = 4
+    outers = CPU_SAMPLE_OUTERS
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        for _ in range(args.warmup):
+        t0 = time.perf_counter()
+        full = pool.map(_full_worker, [text] * cores)
+        full_wall = time.perf_counter() - t0
+        for _ in range(max(0, args.warmup - 1)):
             pool.map(_worker, [(text, outers)] * cores)
         times = []
         per = []
@@ -588,10 +626,12 @@ def run_reference(args):
             res = pool.map(_worker, [(text, outers)] * cores)
             times.append(time.perf_counter() - t0)
             per.extend(res)
+    n_out, n_nod = full[0][1], full[0][2]
     t_outer = statistics.mean(r[0] for r in per)
     t_nodal = statistics.mean(r[1] for r in per)
-    est = est_solve_seconds(t_outer, t_nodal)
+    est = n_out * t_outer + n_nod * t_nodal
     value = cores / est
+    measured = cores / full_wall
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": statistics.mean(times) * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -600,8 +640,12 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"each step: {cores} independent processes, each timing {outers} outer iterations "
                                    f"and one nodal update of the oracle (CPU restatement of the reference loops) on "
-                                   f"this core; solves/s = processes / ({ORACLE_OUTERS} x t_outer + {ORACLE_NODAL} x "
-                                   f"t_nodal) = {cores} / {est:.1f} s"},
+                                   f"this core; solves/s = processes / ({n_out} x t_outer + {n_nod} x t_nodal) = "
+                                   f"{cores} / {est:.1f} s, with {n_out} outers and {n_nod} nodal updates from the "
+                                   f"warm-up's full solves"},
+        "full_solves_in_warmup": {"value": measured, "unit": UNIT, "processes": cores, "wall_s": full_wall,
+                                  "per_process_s": [round(f[0], 2) for f in full], "outers": n_out,
+                                  "nodal_updates": n_nod, "sample_over_measured": value / measured},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

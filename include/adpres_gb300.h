@@ -219,6 +219,20 @@ adp_status adp_fb_rod_tips(int nzz, const double* zdel, double coreh, double pos
 
 /* -- solver --------------------------------------------------------------- */
 
+/* Time limit of every grid-barrier wait of the persistent kernels of this
+ * handle, in seconds (0: the default, 2 s; at most 60).  A wait that runs
+ * out records ADP_ERR_TIMEOUT, the kernel returns and the call returns that
+ * status; the handle stays usable.  No counterpart in the reference. */
+adp_status adp_set_wait_limit(adp_handle* h, double seconds);
+
+/* Failure injection for tests, on the host side: with on != 0 the forward
+ * adp_outer launches count one block more than they launch, so no grid
+ * barrier can complete and every wait runs out after the wait limit
+ * (ADP_ERR_TIMEOUT) -- the way to exercise the timeout path without a GPU
+ * fault.  on = 0 restores normal launches.  No counterpart in the
+ * reference. */
+adp_status adp_test_missing_block(adp_handle* h, int on);
+
 /* One call of outer(popt) (mode ADP_FORWARD) or outer_ad(popt) (ADP_ADJOINT)
  * on the state held by the handle: matrix_setup(1), the first-call start
  * f0 = 1, k = 1 (mod_cmfd.f90:448-454, :635-641), then outer iterations with

@@ -186,6 +186,20 @@ module adpres_gb300_bind
       type(adp_report), intent(inout) :: rep
     end function
 
+    ! time limit of a grid-barrier wait in seconds (0: 2 s)
+    integer(c_int) function adp_set_wait_limit(h, seconds) bind(C, name="adp_set_wait_limit")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), value :: seconds
+    end function
+
+    ! failure injection for tests: every barrier wait of the next outers runs out
+    integer(c_int) function adp_test_missing_block(h, on) bind(C, name="adp_test_missing_block")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: h
+      integer(c_int), value :: on
+    end function
+
     ! reverse-mode derivative of one nodal update at the current state
     integer(c_int) function adp_nodal_vjp(h, lam, phibar, dnbar, kbar, sigbar, resid) bind(C, name="adp_nodal_vjp")
       import :: c_int, c_ptr, c_double

@@ -2,9 +2,9 @@
 fixture, from the ADPRES sample deck smpl/static/CBCsearch.
 
 Run from the repository root where the reference project is mounted
-(default /root/reference):
+(--ref):
 
-    python tests/golden/make_feedback.py [--ref /root/reference]
+    python tests/golden/make_feedback.py --ref <reference project root>
 
 The fixture holds
   * the deck's input state as the oracle reads it (as make_golden.py);
@@ -61,7 +61,7 @@ def feedback_arrays(dk) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the reference project tree")
     args = ap.parse_args()
     path = os.path.join(args.ref, "smpl", "static", "CBCsearch")
     dk = deck.load(path)

@@ -1,9 +1,9 @@
 """Regenerate the golden fixtures under tests/golden/ from the ADPRES sources.
 
 Run from the repository root in a container where the reference project is
-mounted (default /root/reference):
+mounted (--ref):
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <reference project root>
 
 It writes
   * iaea3d_trace.json -- the reference's own printed IAEA3D convergence trace,
@@ -125,7 +125,7 @@ def deck_fixture(path: str) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the reference project tree")
     args = ap.parse_args()
     trace = parse_trace(os.path.join(args.ref, "docs", "quick-guides.md"))
     with open(os.path.join(HERE, "iaea3d_trace.json"), "w") as f:

@@ -2,7 +2,7 @@
 ADPRES sample deck smpl/transient/LMW (a rod-movement transient: bank 2
 withdrawn from t = 0, bank 1 inserted from 7.5 s, theta 0.5, 240 steps).
 
-    python tests/golden/make_transient.py [--ref /root/reference]
+    python tests/golden/make_transient.py --ref <reference project root>
 
 The fixture holds the deck's input state as the oracle reads it (as
 make_golden.py), its %CROD card as adpres_gb300.deck reads it (as
@@ -48,7 +48,7 @@ def records(rec, prefix) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the reference project tree")
     args = ap.parse_args()
     path = os.path.join(args.ref, "smpl", "transient", "LMW")
     dk = deck.load(path)

@@ -27,6 +27,17 @@ def test_reference_arm_prints_one_json_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # the warm-up's measured full solves calibrate the sampled figure
+    fw = d["full_solves_in_warmup"]
+    assert fw["outers"] > 0 and fw["nodal_updates"] > 0 and fw["value"] > 0
+    assert 0.5 < fw["sample_over_measured"] < 2.0
+
+
+def test_canonical_bytes():
+    from adpres_gb300 import perfmodel
+    # 4 groups, nin = 2: 339 words per node and outer
+    assert perfmodel.canonical_bytes_per_node_outer(4, 2, 8) == 8 * 339
+    assert perfmodel.canonical_bytes_per_node_outer(2, 2, 8) == 8 * 163
 
 
 def test_skipped_source_planes_in_the_byte_model():
