@@ -126,6 +126,9 @@ SIGNATURES = {
     "adp_adjoint_sens_frozen": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, _dp, _dp, ctypes.POINTER(AdpReport)]),
     "adp_nodal_vjp": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp]),
     "adp_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "adp_get_matrix": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "adp_nodal_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpReport)]),
+    "adp_get_nodal_sources": (ctypes.c_int, [ctypes.c_void_p, _dp]),
     "adp_test_missing_block": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "adp_get_timers": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpTimers)]),
     "adp_reactivity": (ctypes.c_int, [ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_double)]),

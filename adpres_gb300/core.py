@@ -253,6 +253,26 @@ class Core:
         self._check(st)
         return dk.reshape((nn, G, 4 + G), order="F"), psi.reshape((nn, G), order="F"), r
 
+    def matrix(self):
+        """adp_get_matrix: the CMFD matrix (nnod, ng, 7), columns z-, y-, x-, diag, x+, y+, z+."""
+        a = np.zeros(self.nnod * self.ng * 7)
+        self._check(self.L.adp_get_matrix(self.h, dptr(a)))
+        return a.reshape((self.nnod, self.ng, 7), order="F")
+
+    def nodal_step(self):
+        """adp_nodal_step: one nodal update at the current state; Report with ndmax and loc."""
+        rep, bufs = self._report(False)
+        st = self.L.adp_nodal_step(self.h, ctypes.byref(rep))
+        r = self._to_report(rep, bufs)
+        self._check(st)
+        return r
+
+    def nodal_sources(self):
+        """adp_get_nodal_sources: S1..S3 of the last nodal update, (nnod, ng, 3)."""
+        s = np.zeros(self.nnod * self.ng * 3)
+        self._check(self.L.adp_get_nodal_sources(self.h, dptr(s)))
+        return s.reshape((self.nnod, self.ng, 3), order="F")
+
     def set_wait_limit(self, seconds):
         """adp_set_wait_limit: time limit of a grid-barrier wait (0: 2 s)."""
         self._check(self.L.adp_set_wait_limit(self.h, float(seconds)))

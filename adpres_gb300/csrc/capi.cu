@@ -1616,6 +1616,80 @@ adp_status adp_adjoint_sens_frozen(adp_handle* h, double tol, double* dkdp, doub
   return adjoint_entry(h, tol, false, dkdp, psi, rep);
 }
 
+static AssembleParams assemble_params(adp_handle* h, int with_coupling) {
+  AssembleParams AP;
+  AP.G = box_geom(h);
+  AP.ng = h->ng;
+  AP.with_coupling = with_coupling;
+  AP.D = h->d_D;
+  AP.sigr = h->d_sigr;
+  AP.df = h->d_df;
+  AP.dn = h->d_dn;
+  AP.A = h->d_A;
+  AP.A32 = h->d_A32;
+  AP.A2 = h->d_A2;
+  return AP;
+}
+
+adp_status adp_get_matrix(adp_handle* h, double* A7) {
+  if (!h || !A7) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!h->xs_set) return fail(h, ADP_ERR_STATE, "adp_get_matrix: cross sections not set");
+  CK(launch_assemble(assemble_params(h, 1), h->st));
+  Xfer X;
+  adp_status s = xfer_reserve(h, h->nmat, X);
+  if (s != ADP_OK) return s;
+  return get_nodes(h, X, h->d_A, h->ng, 7, h->NB, A7);
+}
+
+adp_status adp_nodal_step(adp_handle* h, adp_report* rep) {
+  if (!h) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  if (!h->xs_set || !h->started[0])
+    return fail(h, ADP_ERR_STATE, "adp_nodal_step: needs cross sections and a forward state");
+  if (h->o.kern == ADP_KERN_FDM) return fail(h, ADP_ERR_INPUT, "adp_nodal_step: the FDM kernel has no nodal update");
+  CK(launch_assemble(assemble_params(h, 1), h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  OuterCtl c = *h->h_ctl;
+  c.status = 0;
+  c.err_node = -1;
+  c.converged = c.max_reached = c.nodal_due = 0;
+  c.p = 0;                       // no trace row is written for this update
+  *h->h_ctl = c;
+  CK(cudaMemcpyAsync(h->d_ctl, h->h_ctl, sizeof(OuterCtl), cudaMemcpyHostToDevice, h->st));
+  CK(launch_nodal(nodal_params(h, 1), h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, h->d_ctl, sizeof(OuterCtl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  c = *h->h_ctl;
+  h->fwd_ok = false;
+  if (rep) {
+    rep->ndmax = c.ndmax;
+    rep->im = c.im;
+    rep->jm = c.jm;
+    rep->km = c.km;
+    rep->keff = c.Ke;
+    rep->nodal_updates = 1;
+  }
+  if (c.status) return ctl_error(h, c);
+  return ADP_OK;
+}
+
+adp_status adp_get_nodal_sources(adp_handle* h, double* S) {
+  if (!h || !S) return ADP_ERR_INPUT;
+  CK(cudaSetDevice(h->dev));
+  Xfer X;
+  adp_status s = xfer_reserve(h, h->nmat, X);
+  if (s != ADP_OK) return s;
+  // box [u][g][NB] -> host (nnod, ng, 3): one direction at a time
+  std::vector<double> tmp((size_t)h->nnod * h->ng);
+  for (int u = 0; u < 3; ++u) {
+    if ((s = get_nodes(h, X, h->d_S + (size_t)u * h->ng * h->NB, h->ng, 1, h->NB, tmp.data())) != ADP_OK) return s;
+    std::memcpy(S + (size_t)u * h->nnod * h->ng, tmp.data(), tmp.size() * 8);
+  }
+  return ADP_OK;
+}
+
 adp_status adp_nodal_vjp(adp_handle* h, const double* lam, double* phibar, double* dnbar, double* kbar,
                          double* sigbar, double* resid) {
   if (!h) return ADP_ERR_INPUT;

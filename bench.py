@@ -313,23 +313,26 @@ def _batch_oracle_member(args):
     return time.perf_counter() - t0
 
 
-def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
+def batch_leg(flush, dist=None, steps=3, warmup=3, ncores=256, fp64_check=256):
     """256 independent two-group cores (radial 20..68, axial 10..40 nodes,
     config-1 cross sections with 1% lognormal perturbations) in one
     persistent launch replayed from a CUDA graph, mixed precision, schedule
     from the autotuner (cached per batch shape).  Members are those of the
     seeded draw that the reference algorithm converges on
-    (tests/golden/batch_members.json).  Per-instance |dk| against individual
-    single-core FP64 solves; CPU baseline: the oracle on a sample of members,
-    one process per host core."""
+    (tests/golden/batch_members.json).  With N > 1 ranks the members are
+    split over the GPUs (adpres_gb300/partition.py: balanced by box rows x
+    groups, no data-path collective, results gathered on rank 0) and the
+    time of a step is the slowest rank's.  Per-instance |dk| against
+    individual single-core FP64 solves; CPU baseline: the oracle on a sample
+    of members, one process per host core (both with one rank only)."""
     import multiprocessing as mp
 
     import numpy as np
     import torch
 
     from adpres_gb300 import deck, synth
-    from adpres_gb300.batch import Batch
     from adpres_gb300.core import Core
+    from adpres_gb300.partition import DistributedBatch, loads
 
     with open(os.path.join(ROOT, "tests", "golden", "batch_members.json")) as f:
         acc = json.load(f)
@@ -338,21 +341,38 @@ def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
     decks = [deck.parse(t) for t in texts]
     nodes = int(sum(len(d.ix) for d in decks))
     t0 = time.perf_counter()
-    b = Batch(decks, precision="mixed")
+    db = DistributedBatch(decks, dist=dist, precision="mixed")
     t_create = time.perf_counter() - t0
     cache = os.path.join(os.path.expanduser("~"), ".cache", "adpres_gb300", "batch_tune.json")
     t0 = time.perf_counter()
-    cfg, tune_ms, hit = b.autotune(cache)
+    tuned = db.autotune(cache)
+    cfg, tune_ms, hit = tuned if tuned else (None, 0.0, False)
     t_tune = time.perf_counter() - t0
+
+    def one_step():
+        if dist is not None:
+            dist.barrier()
+        return db.solve()
+
     for _ in range(warmup):
-        b.solve()
+        one_step()
     ms = []
     for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
-        res, m = b.solve()
-        ms.append(m)
+        res, _, secs = one_step()
+        ms.append(secs * 1e3)
     t = sum(ms) / len(ms) / 1e3
+    part = {"ranks": db.world, "members_per_rank": [len(p) for p in db.parts],
+            "load_max_over_mean": max(loads(db.weights, db.parts)) / (sum(db.weights) / db.world)}
+    db.close()
+    if db.rank != 0:
+        return None
+    if db.world > 1:
+        return {"workload": f"{len(decks)} two-group cores, {nodes} nodes in all, split over {db.world} GPUs",
+                "value": len(decks) / t, "unit": "solves/s", "ms_per_batch": t * 1e3, "steps": steps,
+                "warmup": warmup, "scaling": "strong", "partition": part,
+                "converged": sum(r["converged"] for r in res), "config_rank0": cfg}
     conv = sum(r["converged"] for r in res)
     # individual FP64 single-core solves
     dks, outs64 = [], []
@@ -364,7 +384,6 @@ def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
         outs64.append(r.outers)
         c.close()
     t_fp64 = time.perf_counter() - t0
-    b.close()
     # CPU baseline: the oracle on a sample, all host cores
     nproc = os.cpu_count() or 1
     sample = [(seed, i) for i in idx[:nproc]]
@@ -391,7 +410,7 @@ def batch_leg(flush, steps=3, warmup=3, ncores=256, fp64_check=256):
         "cpu_baseline": {"value": cpu_rate, "unit": "solves/s", "cores": nproc, "kind": "port",
                          "sample": f"oracle full solves of the first {len(sample)} members, one process per host core, "
                                    f"wall {wall:.1f} s (mean {np.mean(tcpu):.1f} s per member)"},
-        "l2_flush": "256 MiB written between steps",
+        "l2_flush": "256 MiB written between steps", "partition": part,
     }
 
 
@@ -504,7 +523,7 @@ def run_ours(args):
     adjoint = adjoint_leg(flush)
     boron = cbsearch_leg(flush)
     transient = transient_leg()
-    batched = batch_leg(flush) if not args.no_batch else None
+    batched = batch_leg(flush, dist) if not args.no_batch else None
 
     # e2e through the C ABI from host buffers: the inputs sit in pinned host
     # memory in the reference's column-major layouts (set up before timing)

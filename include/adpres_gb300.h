@@ -328,6 +328,27 @@ adp_status adp_adjoint_sens(adp_handle* h, double tol, double* dkdp, double* psi
  * reference. */
 adp_status adp_adjoint_sens_frozen(adp_handle* h, double tol, double* dkdp, double* psi, adp_report* report);
 
+/* -- single stages, for per-stage parity checks ---------------------------- */
+
+/* The CMFD matrix of matrix_setup(1) (mod_cmfd.f90:217-304; coup_coef
+ * first, :11-137) at the current cross sections and dn: A7 (nnod, ng, 7),
+ * node index fastest, columns in the reference's order z-, y-, x-,
+ * diagonal, x+, y+, z+ (0 where a node has no neighbour).  No counterpart
+ * in the reference (its A is module state). */
+adp_status adp_get_matrix(adp_handle* h, double* A7);
+
+/* One nodal update (nodal_upd with the static cal_mode 1: nodal_update or
+ * nodal_update_pnm, mod_nodal.f90:18-278) at the current flux, k and dn,
+ * which it overwrites with the new coupling coefficients; report->ndmax and
+ * im, jm, km give the maximum change and its location (first maximum in
+ * the reference's sweep order).  Statuses as adp_outer's (PIVOT,
+ * DIVERGED).  Clears the converged flag that adp_adjoint_sens needs. */
+adp_status adp_nodal_step(adp_handle* h, adp_report* report);
+
+/* The zeroth-order transverse-leakage sources S1, S2, S3 of the last nodal
+ * update (get_source, mod_nodal.f90:1009-1043): S (nnod, ng, 3). */
+adp_status adp_get_nodal_sources(adp_handle* h, double* S);
+
 /* Reverse-mode derivative of one nodal update (nodal_update /
  * nodal_update_pnm, mod_nodal.f90:18-278, static form) at the handle's
  * current state (flux, coupling coefficients dn, eigenvalue, cross

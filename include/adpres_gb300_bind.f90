@@ -186,6 +186,23 @@ module adpres_gb300_bind
       type(adp_report), intent(inout) :: rep
     end function
 
+    ! single stages: the CMFD matrix A7(nnod, ng, 7), one nodal update, S1..S3
+    integer(c_int) function adp_get_matrix(h, A7) bind(C, name="adp_get_matrix")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: A7(*)
+    end function
+    integer(c_int) function adp_nodal_step(h, rep) bind(C, name="adp_nodal_step")
+      import :: c_int, c_ptr, adp_report
+      type(c_ptr), value :: h
+      type(adp_report), intent(inout) :: rep
+    end function
+    integer(c_int) function adp_get_nodal_sources(h, S) bind(C, name="adp_get_nodal_sources")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: h
+      real(c_double), intent(out) :: S(*)
+    end function
+
     ! time limit of a grid-barrier wait in seconds (0: 2 s)
     integer(c_int) function adp_set_wait_limit(h, seconds) bind(C, name="adp_set_wait_limit")
       import :: c_int, c_ptr, c_double
