@@ -242,6 +242,58 @@ def batch_member(seed, index, zref=True, zsize=10.0, nupd=100):
                  planars, zpln, (1, 1, 1, 1, 1, 1), iter_=it)
 
 
+def batch_member_stated(seed, index):
+    """A member of the batched workload with the config-1 cross-section sets
+    as stated for it, and the reference's default nodal-update interval.
+
+    Radial nodes U{20..68} (assemblies of 2 or 3 nodes, corner reflector by
+    the circle test as the full core), axial nodes U{10..40} of 20 cm with a
+    reflector node at the bottom and top; the materials of full_core_3d
+    (reflector, three fuel types, their rodded variants with sigma_a2 +
+    0.02) each scaled per parameter by an independent lognormal factor
+    (sigma 1%); the rodded region is 8 seeded fuel assemblies over the top
+    40% of the fuel planes; nupd = ceil((nxx + nyy + nzz) / 2.5)
+    (mod_io.f90:1363).  No draw is filtered: members on which the
+    reference's two-node iteration diverges stay in the batch."""
+    rng = np.random.default_rng([5000 + seed, index])
+    nr = int(rng.integers(20, 69))
+    nzn = int(rng.integers(10, 41))
+    base = np.random.default_rng(1000 + seed)
+    fuels = [_fuel2(base) for _ in range(3)]
+
+    def pert(f):
+        return dict(D=tuple(d * rng.lognormal(0, 0.01) for d in f["D"]),
+                    sa=[s * rng.lognormal(0, 0.01) for s in f["sa"]],
+                    nuf=tuple(s * rng.lognormal(0, 0.01) for s in f["nuf"]),
+                    s12=f["s12"] * rng.lognormal(0, 0.01))
+
+    rodded = []
+    for f in fuels:
+        g = dict(f)
+        g["sa"] = [f["sa"][0], f["sa"][1] + 0.02]
+        rodded.append(g)
+    mats = [_mat2(**pert(REFL2))] + [_mat2(**pert(f)) for f in fuels] + [_mat2(**pert(f)) for f in rodded]
+    div = _split_nodes(nr)
+    n = len(div)
+    fuel = _circle_outline(n, 7.2 / 17.0 * n)
+    types = rng.integers(0, 3, size=(n, n))
+    fuel_pos = np.argwhere(fuel)
+    nrod = min(8, len(fuel_pos))
+    rods = fuel_pos[rng.choice(len(fuel_pos), size=nrod, replace=False)]
+    rodmask = np.zeros((n, n), dtype=bool)
+    rodmask[rods[:, 0], rods[:, 1]] = True
+    refl = np.ones((n, n), dtype=int)
+    unrod = np.where(fuel, 2 + types, 1)
+    rod = np.where(fuel & rodmask, 5 + types, unrod)
+    nfuel = nzn - 2
+    ntop = int(round(0.4 * nfuel))
+    zpln = [1] + [2] * (nfuel - ntop) + [3] * ntop + [1]
+    size = [10.0 * d for d in div]
+    it = [2000, 2, "1.0e-5", "1.0e-5", 5, _nupd(sum(div), sum(div), nzn), 30, 20]
+    return _deck(f"BATCHS{index}", 2, mats, n, n, nzn, size, div, size, div, [20.0] * nzn, [1] * nzn,
+                 [refl, unrod, rod], zpln, (1, 1, 1, 1, 1, 1), iter_=it)
+
+
 def _changes2(rows):
     """Feedback-card records of 2-group materials: per material two rows
     sigtr siga nuf sigf sigs(g->1) sigs(g->2)."""

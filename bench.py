@@ -375,15 +375,25 @@ def batch_leg(flush, dist=None, steps=3, warmup=3, ncores=256, fp64_check=256):
                 "converged": sum(r["converged"] for r in res), "config_rank0": cfg}
     conv = sum(r["converged"] for r in res)
     # individual FP64 single-core solves
-    dks, outs64 = [], []
+    dks, outs64, k64 = [], [], []
     t0 = time.perf_counter()
     for i in range(min(fp64_check, len(decks))):
         c = Core.from_deck(decks[i], precision="fp64")
         r = c.outer(trace=False)
         dks.append(abs(res[i]["keff"] - r.keff) / r.keff * 1e5)
         outs64.append(r.outers)
+        k64.append(r.keff)
         c.close()
     t_fp64 = time.perf_counter() - t0
+    # the worst member against its fixed point: a tight FP64 solve (criteria
+    # 1e-10) tells how far the loosely converged end points (ser, fer < 1e-5,
+    # ndmax < 1e-2) of the batch and of the single solve each sit from it
+    wi = int(np.argmax(dks))
+    c = Core.from_deck(decks[wi], precision="fp64", serc=1e-10, ferc=1e-10)
+    rt = c.outer(trace=False)
+    c.close()
+    worst_tight = {"k_tight": rt.keff, "outers_tight": rt.outers,
+                   "batch_pcm_from_tight": abs(res[wi]["keff"] - rt.keff) / rt.keff * 1e5}
     # CPU baseline: the oracle on a sample, all host cores
     nproc = os.cpu_count() or 1
     sample = [(seed, i) for i in idx[:nproc]]
@@ -403,15 +413,74 @@ def batch_leg(flush, dist=None, steps=3, warmup=3, ncores=256, fp64_check=256):
         "dk_pcm_vs_fp64_single": {"max": float(max(dks)), "rms": float(np.sqrt(np.mean(np.square(dks)))),
                                   "checked": len(dks), "fp64_single_s": t_fp64,
                                   "above_1pcm": int(sum(d > 1.0 for d in dks)),
-                                  "worst": {"member": int(np.argmax(dks)),
-                                            "outers_mixed": int(res[int(np.argmax(dks))]["outers"]),
-                                            "outers_fp64": int(outs64[int(np.argmax(dks))])},
+                                  "worst": {"member": wi, "outers_mixed": int(res[wi]["outers"]),
+                                            "outers_fp64": int(outs64[wi]), "fp64_single_pcm_from_tight":
+                                                abs(k64[wi] - worst_tight["k_tight"]) / worst_tight["k_tight"] * 1e5,
+                                            **worst_tight},
                                   "same_outers": int(sum(res[i]["outers"] == outs64[i] for i in range(len(dks))))},
         "cpu_baseline": {"value": cpu_rate, "unit": "solves/s", "cores": nproc, "kind": "port",
                          "sample": f"oracle full solves of the first {len(sample)} members, one process per host core, "
                                    f"wall {wall:.1f} s (mean {np.mean(tcpu):.1f} s per member)"},
         "l2_flush": "256 MiB written between steps", "partition": part,
     }
+
+
+def batch_stated_leg(flush, cfg, steps=2, warmup=1, ncores=256):
+    """The batched workload as stated for it, unfiltered: 256 draws of
+    synth.batch_member_stated (config-1 cross-section sets including the
+    rodded region, 1% lognormal factors, the default nodal-update interval),
+    solved in one launch with the first leg's tuned configuration, mixed
+    precision.  Counts the members whose two-node iteration diverges (in the
+    batch and in single FP64 solves) and those more than 1 pcm from their
+    single FP64 solve."""
+    import numpy as np
+    import torch
+
+    from adpres_gb300 import _lib, deck, synth
+    from adpres_gb300._lib import AdpError
+    from adpres_gb300.batch import Batch
+    from adpres_gb300.core import Core
+
+    decks = [deck.parse(synth.batch_member_stated(0, i)) for i in range(ncores)]
+    nodes = int(sum(len(d.ix) for d in decks))
+    b = Batch(decks, precision="mixed")
+    if cfg:
+        b.set_config(**cfg)
+    for _ in range(warmup):
+        b.solve(check=False)
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        res, m = b.solve(check=False)
+        ms.append(m)
+    b.close()
+    t = sum(ms) / len(ms) / 1e3
+    single = []
+    for dk in decks:
+        c = Core.from_deck(dk, precision="fp64")
+        try:
+            r = c.outer(trace=False)
+            single.append((0, r.keff, r.outers))
+        except AdpError as e:
+            single.append((e.status, None, None))
+        c.close()
+    div_b = [i for i, r in enumerate(res) if r["status"] == _lib.ADP_ERR_DIVERGED]
+    div_s = [i for i, r in enumerate(single) if r[0] == _lib.ADP_ERR_DIVERGED]
+    both = [i for i in range(ncores) if res[i]["status"] == 0 and res[i]["converged"] and single[i][0] == 0]
+    dpcm = np.array([abs(res[i]["keff"] - single[i][1]) / single[i][1] * 1e5 for i in both])
+    return {"workload": f"{ncores} unfiltered draws of synth.batch_member_stated, {nodes} nodes in all, "
+                        "config-1 sets with the rodded region, default nupd, mixed precision",
+            "value": ncores / t, "unit": "solves/s (every member, diverged ones included)", "ms_per_batch": t * 1e3,
+            "steps": steps, "warmup": warmup, "config": cfg,
+            "converged": int(sum(1 for r in res if r["status"] == 0 and r["converged"])),
+            "diverged_batch": len(div_b), "diverged_fp64_single": len(div_s),
+            "diverged_both": len(set(div_b) & set(div_s)),
+            "other_status": sorted({int(r["status"]) for r in res if r["status"] not in (0, _lib.ADP_ERR_DIVERGED)}),
+            "dk_pcm_vs_fp64_single": {"compared": len(both), "max": float(dpcm.max()) if len(dpcm) else None,
+                                      "rms": float(np.sqrt(np.mean(dpcm ** 2))) if len(dpcm) else None,
+                                      "above_1pcm": int(np.sum(dpcm > 1.0))},
+            "outers_mean": float(np.mean([r["outers"] for r in res]))}
 
 
 # ------------------------------------------------------------ our arm ----
@@ -524,6 +593,7 @@ def run_ours(args):
     boron = cbsearch_leg(flush)
     transient = transient_leg()
     batched = batch_leg(flush, dist) if not args.no_batch else None
+    batched_stated = (batch_stated_leg(flush, batched.get("config")) if batched and world == 1 else None)
 
     # e2e through the C ABI from host buffers: the inputs sit in pinned host
     # memory in the reference's column-major layouts (set up before timing)
@@ -588,6 +658,7 @@ def run_ours(args):
         "cbsearch": boron,
         "transient": transient,
         "batched": batched,
+        "batched_stated": batched_stated,
         "gpu_launches": gpu_launches,
         "clocks": ck,
         "cpu_baseline": cpu,
