@@ -10,7 +10,9 @@ import ctypes
 import os
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libadpres_gb300.so")
+# ADPRES_LIB selects another build of the library (the variants of
+# adpres_gb300/build.py); by default the in-tree one.
+LIB_PATH = os.environ.get("ADPRES_LIB") or os.path.join(PKG, "libadpres_gb300.so")
 
 ADP_OK = 0
 ADP_ERR_INPUT = 1

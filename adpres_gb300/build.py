@@ -36,17 +36,27 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+# Variants for measurements only: "nofmad" compiles with -fmad=false (no
+# contraction of a separate multiply and add into an FMA by the compiler;
+# the kernels' explicit fma() calls stay).  A variant builds under
+# _build/<variant>/ and is loaded by setting ADPRES_LIB to its library.
+VARIANTS = {"default": [], "nofmad": ["-fmad=false"]}
+
+
+def build(force: bool = False, verbose: bool = False, variant: str = "default") -> str:
+    extra = VARIANTS[variant]
+    build_dir = BUILD if variant == "default" else os.path.join(BUILD, variant)
+    lib = LIB if variant == "default" else os.path.join(build_dir, "libadpres_gb300.so")
+    os.makedirs(build_dir, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "adpres_gb300.h")]
     objs = []
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(build_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            cmd = [nvcc()] + ARCH + FLAGS + ["-c", s, "-o", o]
+            cmd = [nvcc()] + ARCH + FLAGS + extra + ["-c", s, "-o", o]
             jobs.append(cmd)
 
     def run(cmd):
@@ -59,12 +69,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + ".tmp.%d" % os.getpid()
+    if force or jobs or _stale(lib, objs):
+        tmp = lib + ".tmp.%d" % os.getpid()
         run([nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", tmp] + objs)
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    import sys
+    print(build(verbose=True, variant=sys.argv[1] if len(sys.argv) > 1 else "default"))

@@ -99,6 +99,9 @@ def test_sample_decks_match_oracle(name):
         np.testing.assert_allclose(rep.trace_k[:n], fx["out_trace_k"][:n], rtol=rtol)
         np.testing.assert_array_equal(rep.trace_flags[:n], fx["out_trace_flags"][:n])
     p = c.power()
+    print("parity %s: dk %.2e pcm, power %.2e (bar %.1e), outers %d vs %d" % (
+        name, pcm(rep.keff, float(fx["out_k"])), max_rel(p, fx["out_power"]),
+        max(PTOL, 4.0 * float(fx["sens_power_rel"])), rep.outers, int(fx["out_outers"])))
     assert max_rel(p, fx["out_power"]) <= max(PTOL, 4.0 * float(fx["sens_power_rel"]))
 
 
@@ -153,6 +156,9 @@ def test_small_cores_match_oracle(seed, ng, kern, adf):
     text = synth.small_core(seed=seed, ng=ng, kern=kern, adf=adf)
     o = _oracle_run(text)
     c, rep = _gpu_run(text)
+    print("parity %s: dk %.2e pcm, power %.2e, outers %d vs %d" % (
+        os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0], pcm(rep.keff, o.getd("Ke")), max_rel(c.power(), o.powdis()), rep.outers,
+        o.geti("outers")))
     assert rep.outers == o.geti("outers")
     assert pcm(rep.keff, o.getd("Ke")) <= KTOL_PCM
     assert max_rel(c.power(), o.powdis()) <= PTOL
@@ -163,6 +169,9 @@ def test_small_adjoint_matches_oracle(seed):
     text = synth.small_core(seed=10 + seed, ng=2 + seed, adf=True, mode="ADJOINT")
     o = _oracle_run(text)
     c, rep = _gpu_run(text)
+    print("parity %s: dk %.2e pcm, power %.2e, outers %d vs %d" % (
+        os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0], pcm(rep.keff, o.getd("Ke")), max_rel(c.power(), o.powdis()), rep.outers,
+        o.geti("outers")))
     assert rep.outers == o.geti("outers")
     assert pcm(rep.keff, o.getd("Ke")) <= KTOL_PCM
     assert max_rel(c.power(), o.powdis()) <= PTOL
@@ -172,6 +181,9 @@ def test_quarter_core_2d_matches_oracle():
     text = synth.quarter_core_2d(0)
     o = _oracle_run(text)
     c, rep = _gpu_run(text)
+    print("parity %s: dk %.2e pcm, power %.2e, outers %d vs %d" % (
+        os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0], pcm(rep.keff, o.getd("Ke")), max_rel(c.power(), o.powdis()), rep.outers,
+        o.geti("outers")))
     assert rep.outers == o.geti("outers")
     assert pcm(rep.keff, o.getd("Ke")) <= KTOL_PCM
     assert max_rel(c.power(), o.powdis()) <= PTOL
@@ -181,6 +193,9 @@ def test_full_core_3d_matches_oracle():
     text = synth.full_core_3d(0)
     o = _oracle_run(text)
     c, rep = _gpu_run(text)
+    print("parity %s: dk %.2e pcm, power %.2e, outers %d vs %d" % (
+        os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0], pcm(rep.keff, o.getd("Ke")), max_rel(c.power(), o.powdis()), rep.outers,
+        o.geti("outers")))
     assert rep.outers == o.geti("outers")
     assert pcm(rep.keff, o.getd("Ke")) <= KTOL_PCM
     assert max_rel(c.power(), o.powdis()) <= PTOL
