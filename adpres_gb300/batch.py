@@ -20,6 +20,9 @@ from . import _lib
 from ._lib import AdpError, dptr, iptr
 from .core import _c, _fortran
 
+# Tuned configurations measured on GPU models, keyed "<device>:<signature>".
+TUNED_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "batch_tuned.json")
+
 
 def _batch_error(h):
     L = _lib.load()
@@ -109,9 +112,23 @@ class Batch:
             parts.append(f"{dk.nxx}x{dk.nyy}x{dk.nzz}:{len(dk.ix)}:{dk.ng}:{dk.kern_code}")
         return hashlib.sha1("|".join(parts).encode()).hexdigest()
 
-    def autotune(self, cache=None):
-        """Run the library autotuner; with a cache path, reuse or store the choice."""
+    def autotune(self, cache=None, device=None):
+        """Run the library autotuner; with a cache path, reuse or store the choice.
+
+        device: a key of the GPU model (for example "sm103x152": compute
+        capability and SM count); with it, the configurations measured on
+        that model and shipped with the package (batch_tuned.json) are
+        consulted first, read-only, so a fresh machine of a tuned model
+        starts tuned."""
         key = self.signature()
+        if device:
+            key = device + ":" + key
+            if os.path.exists(TUNED_PATH):
+                with open(TUNED_PATH) as f:
+                    shipped = json.load(f)
+                if key in shipped:
+                    self.set_config(**shipped[key]["config"])
+                    return shipped[key]["config"], shipped[key]["ms"], True
         if cache and os.path.exists(cache):
             with open(cache) as f:
                 db = json.load(f)

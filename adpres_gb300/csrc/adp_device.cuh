@@ -137,6 +137,9 @@ __device__ __forceinline__ int team_arrive_wait(OuterCtl* C, unsigned nblocks, u
     unsigned long long t0 = 0;
     unsigned spins = 0;
     while (!((ld_acquire_gpu(&C->bar_count) ^ old) & 0x80000000u)) {
+#if defined(ADP_BAR_SLEEP_NS) && ADP_BAR_SLEEP_NS > 0
+      __nanosleep(ADP_BAR_SLEEP_NS);
+#endif
       if ((++spins & 63u) == 0) {
         const unsigned long long t = globaltimer_ns();
         if (t0 == 0) t0 = t;

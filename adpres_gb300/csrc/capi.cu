@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/adpres_gb300.h"
 #include "adp_kernels.h"
 #include "handle.h"
@@ -37,6 +39,17 @@ void set_global_error(const std::string& msg) {
 
 
 namespace {
+
+// NVTX range over a scope: the phases of a call (CMFD outers, nodal update,
+// adjoint rounds) appear by name in a timeline profiler.  Each range ends
+// after the host has synchronised with its kernels, so it spans their
+// device time.  Without a profiler attached the calls cost next to nothing.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
 
 adp_status fail(adp_handle* h, adp_status s, const std::string& msg) {
   if (h) h->err = msg;
@@ -1099,7 +1112,9 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   h->tm.grid_blocks = blocks;
   h->tm.block_threads = threads;
   adp_status result = ADP_OK;
+  Range r_call(adj ? "adp_outer adjoint" : (h->trans_on ? "adp_outer transient" : "adp_outer"));
   for (int guard = 0; guard < 4 * h->o.nout + 8; ++guard) {
+    Range r_cmfd("CMFD outers");
     CK(cudaMemsetAsync(&h->d_ctl->bar_count, 0, sizeof(unsigned), h->st));
     CK(cudaEventRecord(h->e2, h->st));
     CK(launch_outer(P, blocks, threads, h->st));
@@ -1119,6 +1134,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
       break;
     }
     if (c.nodal_due) {
+      Range r_nodal("nodal update");
       CK(cudaEventRecord(h->e2, h->st));
       CK(launch_nodal(NP, h->st));
       AssembleParams A0 = AP;
@@ -1351,6 +1367,7 @@ static adp_status adjoint_frozen(adp_handle* h, double tol, OuterCtl& fwd, Outer
   launch_shape(h, blocks, threads);
   P.smem_rows = outer_smem_rows(h->NB, blocks, threads, P.mixed);
   adp_status result = ADP_OK;
+  Range r_adj("adjoint eigen-solve");
   for (int guard = 0; guard < 4 * h->o.nout + 8; ++guard) {
     CK(cudaMemsetAsync(&h->d_ctla->bar_count, 0, sizeof(unsigned), h->st));
     CK(launch_outer(P, blocks, threads, h->st));
@@ -1507,6 +1524,7 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
   lrel = 1.0;
   bool conv = false;
   for (int r = 0; r < max_rounds; ++r) {
+    Range r_round("nodal adjoint round");
     CK(launch_nodal_adjoint(Q, h->st));
     CK(launch_gpt_source(G, ng, nn, h->NBH, h->d_act, phi, h->d_nphibar, h->d_gpart, h->d_gsrc, h->st));
     CK(cudaMemsetAsync(&h->d_ctlg->p, 0, sizeof(int), h->st));

@@ -72,9 +72,9 @@ class DistributedBatch:
             self._batch.close()
             self._batch = None
 
-    def autotune(self, cache=None):
+    def autotune(self, cache=None, device=None):
         if self._batch is not None:
-            return self._batch.autotune(cache)
+            return self._batch.autotune(cache, device)
         return None
 
     def _local(self):

@@ -345,7 +345,9 @@ def batch_leg(flush, dist=None, steps=3, warmup=3, ncores=256, fp64_check=256):
     t_create = time.perf_counter() - t0
     cache = os.path.join(os.path.expanduser("~"), ".cache", "adpres_gb300", "batch_tune.json")
     t0 = time.perf_counter()
-    tuned = db.autotune(cache)
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    device_key = "sm%d%dx%d" % (props.major, props.minor, props.multi_processor_count)
+    tuned = db.autotune(cache, device_key)
     cfg, tune_ms, hit = tuned if tuned else (None, 0.0, False)
     t_tune = time.perf_counter() - t0
 
@@ -408,6 +410,7 @@ def batch_leg(flush, dist=None, steps=3, warmup=3, ncores=256, fp64_check=256):
                     "(seeded draw, members the reference converges on), SANM, mixed precision",
         "value": len(decks) / t, "unit": "solves/s", "ms_per_batch": t * 1e3, "steps": steps, "warmup": warmup,
         "converged": conv, "config": cfg, "tuned_from_cache": hit, "tune_s": t_tune, "create_s": t_create,
+        "device_key": device_key,
         "outers_mean": float(np.mean([r["outers"] for r in res])),
         "teams": sorted({r["team"] for r in res}),
         "dk_pcm_vs_fp64_single": {"max": float(max(dks)), "rms": float(np.sqrt(np.mean(np.square(dks)))),
