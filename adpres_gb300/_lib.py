@@ -27,11 +27,12 @@ ADP_ERR_NAN = 9
 ADP_ERR_BREAKDOWN = 10
 ADP_ERR_TIMEOUT = 11
 ADP_ERR_STATE = 12
+ADP_ERR_BOUNDS = 13
 
 STATUS_NAMES = {
     0: "ADP_OK", 1: "ADP_ERR_INPUT", 2: "ADP_ERR_BADXS", 3: "ADP_ERR_PIVOT", 4: "ADP_ERR_DIVERGED",
     5: "ADP_ERR_MAXOUTER", 6: "ADP_ERR_ZEROPOWER", 7: "ADP_ERR_UNSUPPORTED", 8: "ADP_ERR_CUDA",
-    9: "ADP_ERR_NAN", 10: "ADP_ERR_BREAKDOWN", 11: "ADP_ERR_TIMEOUT", 12: "ADP_ERR_STATE",
+    9: "ADP_ERR_NAN", 10: "ADP_ERR_BREAKDOWN", 11: "ADP_ERR_TIMEOUT", 12: "ADP_ERR_STATE", 13: "ADP_ERR_BOUNDS",
 }
 
 ADP_FORWARD, ADP_ADJOINT, ADP_FROZEN_DN = 0, 1, 4

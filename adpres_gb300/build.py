@@ -36,11 +36,13 @@ def _stale(target: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-# Variants for measurements only: "nofmad" compiles with -fmad=false (no
-# contraction of a separate multiply and add into an FMA by the compiler;
-# the kernels' explicit fma() calls stay).  A variant builds under
-# _build/<variant>/ and is loaded by setting ADPRES_LIB to its library.
-VARIANTS = {"default": [], "nofmad": ["-fmad=false"]}
+# Variants for tests and measurements: "nofmad" compiles with -fmad=false
+# (no contraction of a separate multiply and add into an FMA by the
+# compiler; the kernels' explicit fma() calls stay); "bounds" compiles the
+# range checks of device indices (ADP_BOUNDS: a bad index is reported as
+# ADP_ERR_BOUNDS and its item skipped, nothing traps).  A variant builds
+# under _build/<variant>/ and is loaded by setting ADPRES_LIB to its library.
+VARIANTS = {"default": [], "nofmad": ["-fmad=false"], "bounds": ["-DADP_BOUNDS"]}
 
 
 def build(force: bool = False, verbose: bool = False, variant: str = "default") -> str:

@@ -163,6 +163,46 @@ __device__ __forceinline__ bool team_barrier(OuterCtl* C, unsigned nblocks, unsi
   return s_ok != 0;
 }
 
+// ---- range checks of device indices (bounds-checked build) ---------------
+// Compiled in with -DADP_BOUNDS, a separate build of the library for tests:
+// an index outside the box, or a neighbour index that is not an active
+// node, records ADP_ERR_BOUNDS (first one wins, its index in err_node) and
+// the item that computed it is skipped -- nothing traps.  In the product
+// build the checks are constant true and compile to nothing.  The outer
+// kernel's rows are in [0, NB) by their loop bounds and its stencil reads
+// b +- plane stay inside the vectors' halo planes, so it needs none.
+#ifdef ADP_BOUNDS
+__device__ __forceinline__ bool adp_bounds_fail(OuterCtl* C, long long b) {
+  if (C && atomicCAS(&C->status, 0, ADP_ERR_BOUNDS) == 0)
+    C->err_node = (b >= -2147483647LL && b <= 2147483647LL) ? (int)b : -2;
+  return false;
+}
+#define ADP_IN_BOX(C, b, NB) (((long long)(b) >= 0 && (long long)(b) < (long long)(NB)) ? true : adp::adp_bounds_fail((C), (b)))
+#define ADP_NB_OK(C, G, bm) \
+  ((ADP_IN_BOX(C, bm, (G).NB) && ((G).nbm[(bm)] & adp::NB_ACTIVE)) ? true : adp::adp_bounds_fail((C), (bm)))
+#else
+#define ADP_IN_BOX(C, b, NB) true
+#define ADP_NB_OK(C, G, bm) true
+#endif
+
+// An item's node b and its neighbours across the faces its mask opens.
+__device__ __forceinline__ bool node_ok(OuterCtl* C, const BoxGeom& G, long long b) {
+#ifdef ADP_BOUNDS
+  if (!ADP_IN_BOX(C, b, G.NB)) return false;
+  const unsigned m = G.nbm[b];
+  if (!(m & NB_ACTIVE)) return adp_bounds_fail(C, b);
+  for (int f = 0; f < 6; ++f)
+    if (m & (1u << f)) {
+      const long long bm = b + face_off(G, f);
+      if (!ADP_NB_OK(C, G, bm)) return false;
+    }
+  return true;
+#else
+  (void)C; (void)G; (void)b;
+  return true;
+#endif
+}
+
 // ---- deterministic reductions ------------------------------------------
 // Sums use a fixed tree (xor-butterfly inside warps, warp results in order),
 // so every block that reduces the same partials gets bit-identical totals.

@@ -109,6 +109,7 @@ struct AssembleParams {
   double* A;
   float* A32;
   float2* A2;                 // (A32, A - A32) pairs (mixed path), may be null
+  OuterCtl* ctl;              // where the range-checked build reports a bad index (may be null)
 };
 
 // Contraction of forward and adjoint fluxes into dk/dSigma (adjoint.cu).

@@ -336,6 +336,7 @@ adp_status adp_batch_create(int n, const adp_geom* geoms, const adp_opts* opts, 
     I.ap.A = h->d_A;
     I.ap.A32 = h->d_A32;
     I.ap.A2 = h->d_A2;
+    I.ap.ctl = h->d_ctl;
     I.ap0 = I.ap;
     I.ap0.with_coupling = 0;
     I.sigtr = h->d_sigtr;

@@ -1017,6 +1017,9 @@ static adp_status ctl_error(adp_handle* h, const OuterCtl& c) {
     case ADP_ERR_NAN: std::snprintf(buf, sizeof buf, "non-finite eigenvalue or fission source at outer %d", c.p); break;
     case ADP_ERR_TIMEOUT: std::snprintf(buf, sizeof buf, "a grid barrier wait ran out of time"); break;
     case ADP_ERR_ZEROPOWER: std::snprintf(buf, sizeof buf, "total nodes power is zero or less"); break;
+    case ADP_ERR_BOUNDS:
+      std::snprintf(buf, sizeof buf, "device index out of range (range-checked build) at box row %d", c.err_node);
+      break;
     default: std::snprintf(buf, sizeof buf, "device error %d", c.status);
   }
   return fail(h, (adp_status)c.status, buf);
@@ -1066,6 +1069,7 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   AP.A = h->d_A;
   AP.A32 = h->d_A32;
   AP.A2 = h->d_A2;
+  AP.ctl = h->d_ctl;
   CK(launch_assemble(AP, h->st));
   OuterParams P = outer_params(h, adj);
   // first-call start (mod_cmfd.f90:448-454 / :635-641)
@@ -1646,6 +1650,7 @@ static AssembleParams assemble_params(adp_handle* h, int with_coupling) {
   AP.A = h->d_A;
   AP.A32 = h->d_A32;
   AP.A2 = h->d_A2;
+  AP.ctl = h->d_ctl;
   return AP;
 }
 
@@ -1734,6 +1739,7 @@ adp_status adp_nodal_vjp(adp_handle* h, const double* lam, double* phibar, doubl
   AP.A = h->d_A;
   AP.A32 = h->d_A32;
   AP.A2 = h->d_A2;
+  AP.ctl = h->d_ctl;
   CK(launch_assemble(AP, h->st));
   NodalParams NP = nodal_params(h, 1);
   CK(launch_nodal_prep(NP, h->st));

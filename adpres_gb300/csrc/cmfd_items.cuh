@@ -35,6 +35,7 @@ __device__ __forceinline__ void assemble_items(const AssembleParams& P, long lon
       }
       continue;
     }
+    if (!node_ok(P.ctl, G, b)) continue;
     const int i = b % G.nxx, j = (b / G.nxx) % G.nyy, k = b / G.plane;
     const double h[3] = {G.xdel[i], G.ydel[j], G.zdel[k]};
     if (P.with_coupling) {

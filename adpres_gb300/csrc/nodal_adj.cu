@@ -505,6 +505,7 @@ __global__ void __launch_bounds__(128) k_nadj_iface(NadjParams Q) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const int n = q % P.nnod, u = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     const LinePos L = line_pos(G, u, b);
     SideBar<NG> pb;
     pb.zero();
@@ -561,6 +562,7 @@ __global__ void __launch_bounds__(128) k_nadj_node(NadjParams Q) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const int n = q % P.nnod, u = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     SideBar<NG> t;
     t.zero();
     side_add<NG>(Q.side, NB, 0, u, b, t);
@@ -724,6 +726,7 @@ __global__ void k_nadj_lbar(NadjParams Q, int nq, int q_sself, int q_top, int q_
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const int n = q % P.nnod, g = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     const unsigned m = G.nbm[b];
     double Sb[3];
     for (int u = 0; u < 3; ++u) {
@@ -755,6 +758,7 @@ __global__ void k_nadj_leak(NadjParams Q, int nq, int q_phi) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const int n = q % P.nnod, g = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     const unsigned m = G.nbm[b];
     const double* F = phi + (size_t)g * P.NBH;
     const double fb0 = F[b];
@@ -843,6 +847,7 @@ __global__ void k_nadj_params(NadjParams Q, int nq, int q_D, int q_sigr, int q_n
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const int n = q % nn, g = q / nn;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     const unsigned m = G.nbm[b];
     const double Dn = P.D[(size_t)g * NB + b];
     double Db = 0.0, sr = 0.0, nf = 0.0;

@@ -106,6 +106,7 @@ __device__ __forceinline__ void tl_source_items(const NodalParams& P, int start,
   for (int q = start; q < total; q += stride) {
     const int n = q % P.nnod, g = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     double L[3];
     net_leakage(G, phi + (size_t)g * P.NBH, P.df + (size_t)g * 6 * NB, P.dn + (size_t)g * 6 * NB, b, L);
     if (P.cmode == 2) {
@@ -303,6 +304,7 @@ __device__ __forceinline__ void node_prep_items(const NodalParams& P, int start,
   for (int q = start; q < total; q += stride) {
     const int n = q % P.nnod, u = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     const double h = hdir(G, u, b);
     double fac[NG];
 #pragma unroll
@@ -399,6 +401,7 @@ __device__ __forceinline__ void interface_items(const NodalParams& P, int start,
   for (int q = start; q < total; q += stride) {
     const int n = q % P.nnod, u = q / P.nnod;
     const int b = P.act[n];
+    if (!node_ok(P.ctl, G, b)) continue;
     const LinePos L = line_pos(G, u, b);
     const int sf = 2 * u;         // plus face of u (X+, Y+, Z+); sf+1 is the minus face
     const long long ev = P.evbase[(size_t)u * NB + b];

@@ -46,7 +46,8 @@ typedef enum adp_status {
   ADP_ERR_NAN = 9,          /* non-finite eigenvalue or fission source         */
   ADP_ERR_BREAKDOWN = 10,   /* BiCGSTAB rho, (rs,v) or (t,t) exactly zero      */
   ADP_ERR_TIMEOUT = 11,     /* a device-side wait ran out of its time limit   */
-  ADP_ERR_STATE = 12        /* call made in the wrong order                    */
+  ADP_ERR_STATE = 12,       /* call made in the wrong order                    */
+  ADP_ERR_BOUNDS = 13       /* a device index out of range (only in the range-checked test build) */
 } adp_status;
 
 /* ADP_FROZEN_DN may be or-ed into the mode of adp_outer: the outers then
