@@ -190,7 +190,41 @@ def adjoint_leg(flush, steps=3):
                 "adjoint_outers": rep.outers, "rounds": rep.nodal_updates,
                 "fixed_point_residual": rep.ndmax if mode == "fixed_point" else None}
         c.close()
+    out["cpu_baseline"] = _adjoint_cpu_baseline(synth.full_core_3d(0), out["params_per_solve"])
     return out
+
+
+def _adjoint_cpu_baseline(text, nparams):
+    """The reference's only route to dk/dSigma: central differences of its
+    full solve, two warm-started solves per parameter (the oracle, one host
+    core, the deck's criteria).  Timed on two parameters (four solves)."""
+    import numpy as np
+
+    import oracle
+    o = oracle.Oracle(text=text)
+    o.run()
+    state = {a: o.array(a).copy() for a in ("f0", "fs0", "dn", "D", "sigr", "siga", "sigtr", "nuf", "sigs")}
+    k0 = o.getd("Ke")
+    nn, ng = o.geti("nnod"), o.geti("ng")
+    fuel = np.nonzero(o.fortran("nuf", (nn, ng))[:, 1] > 0)[0]
+    n = int(fuel[len(fuel) // 2])
+    t0 = time.perf_counter()
+    for kind in ("siga", "nuf"):
+        for r in (1e-4, -1e-4):
+            for a, v in state.items():
+                o.set_array(a, v)
+            o.setd("Ke", k0)
+            a = o.fortran(kind, (nn, ng)).copy()
+            a[n, 1] *= 1.0 + r
+            o.set_array(kind, a.reshape(-1, order="F"))
+            if kind != "nuf":
+                o.dsigr_updt()
+            o.outer(popt=1)
+    per_grad = (time.perf_counter() - t0) / 2
+    return {"value": 1.0 / per_grad, "unit": "gradients/s", "cores": 1, "kind": "port",
+            "sample": f"central differences of the oracle's full solve (two warm-started solves per parameter, "
+                      f"the deck's criteria), timed on two parameters: {per_grad:.2f} s per gradient, "
+                      f"{nparams * per_grad / 3600:.0f} h for the {nparams} parameters one adjoint solve gives"}
 
 
 # ------------------------------------------- critical boron search leg ----
