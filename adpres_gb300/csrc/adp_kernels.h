@@ -28,6 +28,7 @@ struct OuterParams {
   unsigned src_nz;
   unsigned long long sc_nz;
   const double* exsrc;        // [ng][NB] external source of the transient step (trans only)
+  const float2* exsrc2;       // [ng][NB] external source as (hi, lo) pairs (mixed trans: the generalized adjoint)
   double serc, ferc;
   long long NBH;              // group stride of halo'd arrays
   const double* A;            // [ng][7][NB] FP64 CMFD matrix

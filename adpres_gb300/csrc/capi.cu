@@ -1400,7 +1400,7 @@ static adp_status nadj_alloc(adp_handle* h) {
   const size_t pieces[] = {nadj_side_doubles(h->ng, h->NB) * 8, nadj_nodeu_doubles(h->ng, h->NB) * 8,
                            3 * G * NB * 8, face, face, G * NB * 8, face, face, face, kMaxBlocks * 8, kMaxBlocks * 8,
                            4 * 8, sens, sens, G * NBH * 8, G * NBH * 8, NB * 8, NB * 8, G * NB * 8, G * NB * 8,
-                           2 * kMaxBlocks * 8, 2 * kMaxBlocks * 8, sizeof(OuterCtl)};
+                           2 * kMaxBlocks * 8, 2 * kMaxBlocks * 8, sizeof(OuterCtl), G * NB * 8, G * NB * 8};
   size_t bytes = 0;
   for (size_t b : pieces) bytes += ((b + 255) & ~(size_t)255) + 256;
   DevArena A;
@@ -1429,6 +1429,8 @@ static adp_status nadj_alloc(adp_handle* h) {
   h->d_lpart = (double*)A.take(pieces[i++]);
   h->d_gpart = (double*)A.take(pieces[i++]);
   h->d_ctlg = (OuterCtl*)A.take(pieces[i++]);
+  h->d_gsrc2 = (float2*)A.take(pieces[i++]);
+  h->d_nufk2 = (float2*)A.take(pieces[i++]);
   if (A.used > A.size) return fail(h, ADP_ERR_CUDA, "internal: nodal adjoint arena overflow");
   CK(cudaMemsetAsync(A.base, 0, A.size, h->st));   // halos, inactive positions and non-canonical slots stay 0
   CK(cudaStreamSynchronize(h->st));
@@ -1478,6 +1480,7 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
   CK(launch_face_contract(G, ng, nn, h->NBH, h->d_act, phi, psi, -k * k / den, h->d_Kd, h->st));
   CK(cudaMemcpyAsync(h->d_lam, h->d_Kd, (size_t)ng * 6 * h->NB * 8, cudaMemcpyDeviceToDevice, h->st));
   CK(launch_scale_planes(h->d_nuf, 1.0 / k, h->d_nufk, (long long)ng * h->NB, h->st));
+  if (h->o.precision == ADP_MIXED) CK(launch_split(h->d_nufk, h->d_nufk2, (long long)ng * h->NB, h->st));
   NadjParams Q;
   std::memset(&Q, 0, sizeof Q);
   Q.N = NP;
@@ -1493,9 +1496,17 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
   Q.scal = h->d_nscal;
   Q.out = h->d_NS;
   OuterParams P = outer_params(h, 1);
-  P.mixed = 0;
+  // a mixed-precision handle runs the generalized adjoint in the mixed
+  // kernel (FP32 Krylov steps, double-float defect correction: it converges
+  // to the FP64 solution), an FP64 handle in the FP64 kernel
   P.trans = 1;
   P.A = h->d_AT;
+  if (P.mixed) {
+    P.A32 = h->d_AT32;
+    P.A2 = h->d_AT2;
+    P.wsrc2 = h->d_nufk2;
+    P.exsrc2 = h->d_gsrc2;
+  }
   for (int t = 0; t < 2; ++t) {
     P.phi[t] = h->d_gam[t];
     P.fs[t] = h->d_fsg[t];
@@ -1531,6 +1542,7 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
     Range r_round("nodal adjoint round");
     CK(launch_nodal_adjoint(Q, h->st));
     CK(launch_gpt_source(G, ng, nn, h->NBH, h->d_act, phi, h->d_nphibar, h->d_gpart, h->d_gsrc, h->st));
+    if (P.mixed) CK(launch_split(h->d_gsrc, h->d_gsrc2, (long long)ng * h->NB, h->st));
     CK(cudaMemsetAsync(&h->d_ctlg->p, 0, sizeof(int), h->st));
     CK(cudaMemsetAsync(&h->d_ctlg->nodal_due, 0, sizeof(int), h->st));
     CK(cudaMemsetAsync(&h->d_ctlg->bar_count, 0, sizeof(unsigned), h->st));

@@ -62,9 +62,9 @@ cudaError_t launch_init_flux(const OuterParams& P, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <bool MIXED, bool SMEMA>
+template <bool MIXED, bool SMEMA, bool XSRC = false>
 __global__ void __launch_bounds__(kOuterThreads, 1) k_outer(OuterParams P) {
-  outer_body<MIXED, SMEMA>(P, blockIdx.x, gridDim.x + P.phantom);
+  outer_body<MIXED, SMEMA, XSRC>(P, blockIdx.x, gridDim.x + P.phantom);
 }
 
 int outer_max_blocks_per_sm(int threads, int mixed) {
@@ -100,6 +100,12 @@ static cudaError_t launch_outer_t(const OuterParams& P, int blocks, int threads,
 }
 
 cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st) {
+  if (P.mixed && P.trans) {
+    // the generalized adjoint in mixed precision (no shared-memory matrix copy)
+    void* args[] = {(void*)&P};
+    return cudaLaunchCooperativeKernel((const void*)k_outer<true, false, true>, dim3(blocks), dim3(threads), args, 0,
+                                       st);
+  }
   if (P.smem_rows > 0)
     return P.mixed ? launch_outer_t<true, true>(P, blocks, threads, st) : launch_outer_t<false, true>(P, blocks, threads, st);
   return P.mixed ? launch_outer_t<true, false>(P, blocks, threads, st) : launch_outer_t<false, false>(P, blocks, threads, st);

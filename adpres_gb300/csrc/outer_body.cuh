@@ -119,7 +119,11 @@ __device__ __forceinline__ double2 mk2(double a, double b) { return make_double2
 // row k * nthreads + tid of the block at index k * blockDim.x + tid): P0
 // reads them from memory anyway and stores them, the 2 nin Krylov phases
 // that follow read them from there instead of L2 or HBM.
-template <bool MIXED, bool SMEMA = false>
+// XSRC (mixed path only): the group source also carries the external source
+// P.exsrc2 as (hi, lo) pairs -- the fixed-eigenvalue mode of the
+// generalized adjoint of adp_adjoint_sens.  The forward and adjoint
+// solves are the XSRC = false instantiation.
+template <bool MIXED, bool SMEMA = false, bool XSRC = false>
 __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, unsigned nteam) {
   using T = typename KV<MIXED>::T;
   using T2 = typename KV<MIXED>::T2;
@@ -226,7 +230,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       // ---- P0: source and initial residual (TSrc + r = b - A x) --------
       double tot1[1];
       if constexpr (MIXED) {
-        // (the transient runs the FP64 kernel only)
+        // (the transient runs the FP64 kernel only; XSRC adds the
+        // generalized adjoint's external source)
         // Defect of the current flux in double-float: one compensated dot
         // product over the source and the seven matrix terms (A = A32 + lo).
         const float2* xO2 = P.x2[old] + (size_t)g * NBH;
@@ -238,6 +243,7 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
               Dot2 d;
               if ((P.src_nz >> g) & 1u)
                 d.add(ff_mul(ld_ff(&P.wsrc2[(size_t)g * NB + b]), ld_ff(&P.fs2[old][b])), invKe_ff);
+              if constexpr (XSRC) d.add(ld_ff(&P.exsrc2[(size_t)g * NB + b]), ff{1.f, 0.f});
               for (int h = 0; h < ng; ++h) {
                 if (h == g) continue;
                 const int q = P.adj ? g * ng + h : h * ng + g;
