@@ -1515,7 +1515,13 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
   P.exsrc = h->d_gsrc;
   P.ctl = h->d_ctlg;
   P.do_nodal = 1;
-  const int K = std::min(std::max(h->o.nupd, 2 * h->o.nac), std::max(h->o.nout, 1));
+#ifndef ADP_GPT_OUTERS
+#define ADP_GPT_OUTERS 0   // outers of Gam per round; 0: two extrapolation intervals, 2 nac
+#endif
+  // Measured on the 34x34x22 core (tol 1e-8): the rounds lam needs do not
+  // depend on the outers per round between 12 and 72 (22 rounds either way),
+  // so short rounds cost least; at 5 the rounds grow (41), at 2 they explode.
+  const int K = std::min(ADP_GPT_OUTERS > 0 ? ADP_GPT_OUTERS : std::max(2 * h->o.nac, 4), std::max(h->o.nout, 1));
   P.nupd = K;
   P.serc = P.ferc = 0.0;   // rounds end on the count; convergence is lam's
   int blocks, threads;

@@ -302,7 +302,7 @@ adp_status adp_power_noalloc(int nnod, int ng, const double* f0, const double* s
  * face coefficients, s = lam^T dN/dk, and Gam the generalized adjoint of
  * the flux: (M - F/k)^T Gam = lam^T dN/dphi with Gam^T F phi = 0.  lam and
  * Gam are iterated together as the forward iteration is (rounds of
- * max(nupd, 2 nac) outers of Gam, each followed by the reverse-mode
+ * 2 nac outers of Gam, each followed by the reverse-mode
  * derivative of the nodal update at the converged state and an update of
  * lam) until lam's relative change is below tol (at least 1e-13).  For the
  * FDM kernel (d = 0) the frozen-d derivative is the whole derivative.  The
