@@ -127,13 +127,13 @@ class Batch:
                 with open(TUNED_PATH) as f:
                     shipped = json.load(f)
                 if key in shipped:
-                    self.set_config(**shipped[key]["config"])
+                    self._apply_cached(shipped[key]["config"])
                     return shipped[key]["config"], shipped[key]["ms"], True
         if cache and os.path.exists(cache):
             with open(cache) as f:
                 db = json.load(f)
             if key in db:
-                self.set_config(**db[key]["config"])
+                self._apply_cached(db[key]["config"])
                 return db[key]["config"], db[key]["ms"], True
         c = _lib.AdpBatchConfig()
         ms = ctypes.c_double()
@@ -149,6 +149,15 @@ class Batch:
             with open(cache, "w") as f:
                 json.dump(db, f, indent=1)
         return cfg, ms.value, False
+
+    def _apply_cached(self, cfg):
+        """A cached configuration, then one solve to measure every core's
+        block time and a re-plan with those weights, as the autotuner plans
+        its candidates (the plan before any solve weighs cores by box rows
+        x groups)."""
+        self.set_config(**cfg)
+        self.solve(check=False)
+        self.set_config(**cfg)
 
     # -- solve and results ----------------------------------------------------
     def solve(self, check=True):
