@@ -245,8 +245,10 @@ size_t nadj_nodeu_doubles(int ng, long long NB);
 cudaError_t launch_face_contract(const BoxGeom& G, int ng, int nnod, long long NBH, const int* act,
                                  const double* phi, const double* w, double scale, double* out, cudaStream_t st);
 cudaError_t launch_lam_update(const BoxGeom& G, int ng, int nnod, const int* act, const double* Kd,
-                              const double* dnbar, const double* cG, const double* scal, double* lam, double* part,
-                              cudaStream_t st);
+                              const double* dnbar, const double* cG, const double* scal, double* lam, double* dlam,
+                              double* part, cudaStream_t st);
+cudaError_t launch_lam_extrap(const BoxGeom& G, int ng, int nnod, const int* act, const double* dlam, double c,
+                              double* lam, cudaStream_t st);
 int lam_update_blocks(int ng, int nnod);
 cudaError_t launch_gpt_source(const BoxGeom& G, int ng, int nnod, long long NBH, const int* act, const double* phi,
                               const double* v, double* part, double* src, cudaStream_t st);

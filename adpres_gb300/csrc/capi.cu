@@ -1400,7 +1400,7 @@ static adp_status nadj_alloc(adp_handle* h) {
   const size_t pieces[] = {nadj_side_doubles(h->ng, h->NB) * 8, nadj_nodeu_doubles(h->ng, h->NB) * 8,
                            3 * G * NB * 8, face, face, G * NB * 8, face, face, face, kMaxBlocks * 8, kMaxBlocks * 8,
                            4 * 8, sens, sens, G * NBH * 8, G * NBH * 8, NB * 8, NB * 8, G * NB * 8, G * NB * 8,
-                           2 * kMaxBlocks * 8, 2 * kMaxBlocks * 8, sizeof(OuterCtl), G * NB * 8, G * NB * 8};
+                           2 * kMaxBlocks * 8, 2 * kMaxBlocks * 8, sizeof(OuterCtl), G * NB * 8, G * NB * 8, face};
   size_t bytes = 0;
   for (size_t b : pieces) bytes += ((b + 255) & ~(size_t)255) + 256;
   DevArena A;
@@ -1431,6 +1431,7 @@ static adp_status nadj_alloc(adp_handle* h) {
   h->d_ctlg = (OuterCtl*)A.take(pieces[i++]);
   h->d_gsrc2 = (float2*)A.take(pieces[i++]);
   h->d_nufk2 = (float2*)A.take(pieces[i++]);
+  h->d_dlam = (double*)A.take(pieces[i++]);
   if (A.used > A.size) return fail(h, ADP_ERR_CUDA, "internal: nodal adjoint arena overflow");
   CK(cudaMemsetAsync(A.base, 0, A.size, h->st));   // halos, inactive positions and non-canonical slots stay 0
   CK(cudaStreamSynchronize(h->st));
@@ -1544,6 +1545,8 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
   gouters = 0;
   lrel = 1.0;
   bool conv = false;
+  double dprev = 0.0, rprev = 0.0;
+  int since = 0;
   for (int r = 0; r < max_rounds; ++r) {
     Range r_round("nodal adjoint round");
     CK(launch_nodal_adjoint(Q, h->st));
@@ -1562,8 +1565,8 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
     CK(launch_gpt_project(G, ng, nn, h->NBH, h->d_act, h->d_chin, h->d_nuf, phi, psi, h->d_gpart, gam,
                           h->d_fsg[c.cur], h->st));
     CK(launch_face_contract(G, ng, nn, h->NBH, h->d_act, phi, gam, 1.0, h->d_cG, h->st));
-    CK(launch_lam_update(G, ng, nn, h->d_act, h->d_Kd, h->d_ndnbar, h->d_cG, h->d_nscal, h->d_lam, h->d_lpart,
-                         h->st));
+    CK(launch_lam_update(G, ng, nn, h->d_act, h->d_Kd, h->d_ndnbar, h->d_cG, h->d_nscal, h->d_lam, h->d_dlam,
+                         h->d_lpart, h->st));
     CK(cudaMemcpyAsync(lp.data(), h->d_lpart, lp.size() * 8, cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(scal, h->d_nscal, 2 * 8, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -1580,6 +1583,25 @@ static adp_status adjoint_nodal(adp_handle* h, double tol, const OuterCtl& fwd, 
     if (r >= 2 && lrel < ltol) {
       conv = true;
       break;
+    }
+#ifndef ADP_LAM_EXTRAP
+#define ADP_LAM_EXTRAP 1
+#endif
+    // lam converges linearly (about 0.4 per round): once two successive
+    // contractions agree, extrapolate along the last change as the forward
+    // iteration does its fission source (mod_cmfd.f90:308-335)
+    const double dn = std::sqrt(d2);
+    const double ratio = dprev > 0.0 ? dn / dprev : 0.0;
+    if (ADP_LAM_EXTRAP && since >= 2 && ratio > 0.0 && ratio < 0.9 && rprev > 0.0 &&
+        std::fabs(ratio - rprev) <= 0.1 * ratio) {
+      CK(launch_lam_extrap(G, ng, nn, h->d_act, h->d_dlam, ratio / (1.0 - ratio), h->d_lam, h->st));
+      since = 0;
+      dprev = 0.0;
+      rprev = 0.0;
+    } else {
+      ++since;
+      rprev = ratio;
+      dprev = dn;
     }
   }
   if (!conv) return fail(h, ADP_ERR_MAXOUTER, "adp_adjoint_sens: the adjoint of the nodal update did not converge");

@@ -103,6 +103,7 @@ struct adp_handle {
   double *d_gsrc = nullptr, *d_nufk = nullptr, *d_lpart = nullptr, *d_gpart = nullptr;
   adp::OuterCtl* d_ctlg = nullptr;
   float2 *d_gsrc2 = nullptr, *d_nufk2 = nullptr;   // (hi, lo) copies for the mixed kernel
+  double* d_dlam = nullptr;                        // the last change of lam (its extrapolation)
   // feedback tables of adp_fb_set, kept until the next call
   char* fb_base = nullptr;
   size_t fb_size = 0;

@@ -921,7 +921,7 @@ __global__ void k_face_contract(BoxGeom G, int ng, int nnod, long long NBH, cons
 // lam_new = Kd (1 + s) + dnbar - cG at the canonical slots; partials of
 // |lam_new - lam|^2 and |lam_new|^2.
 __global__ void k_lam_update(BoxGeom G, int ng, int nnod, const int* act, const double* Kd, const double* dnbar,
-                             const double* cG, const double* scal, double* lam, double* part) {
+                             const double* cG, const double* scal, double* lam, double* dlam, double* part) {
   const int NB = G.NB;
   const double s1 = 1.0 + scal[0];
   double acc[2] = {0.0, 0.0};
@@ -939,9 +939,28 @@ __global__ void k_lam_update(BoxGeom G, int ng, int nnod, const int* act, const 
       acc[0] = fma(d, d, acc[0]);
       acc[1] = fma(v, v, acc[1]);
       lam[i] = v;
+      dlam[i] = d;
     }
   }
   block_partials<2, 0u>(acc, part);
+}
+
+// lam += c dlam at the canonical slots: the extrapolation of a linearly
+// converging iteration by its observed contraction d, c = d / (1 - d), as
+// fiss_extrp does for the fission source (mod_cmfd.f90:308-335).
+__global__ void k_lam_extrap(BoxGeom G, int ng, int nnod, const int* act, const double* dlam, double c, double* lam) {
+  const int NB = G.NB;
+  const int total = nnod * ng;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    const int n = q % nnod, g = q / nnod;
+    const int b = act[n];
+    const unsigned m = G.nbm[b];
+    for (int f = 0; f < 6; ++f) {
+      if (!((f & 1) || !(m & (1u << f)))) continue;
+      const size_t i = ((size_t)g * 6 + f) * NB + b;
+      lam[i] = fma(c, dlam[i], lam[i]);
+    }
+  }
 }
 
 // Partials of (phi . v) and (phi . phi) over the active rows, v = phibar.
@@ -1071,10 +1090,16 @@ cudaError_t launch_face_contract(const BoxGeom& G, int ng, int nnod, long long N
 }
 
 cudaError_t launch_lam_update(const BoxGeom& G, int ng, int nnod, const int* act, const double* Kd,
-                              const double* dnbar, const double* cG, const double* scal, double* lam, double* part,
-                              cudaStream_t st) {
+                              const double* dnbar, const double* cG, const double* scal, double* lam, double* dlam,
+                              double* part, cudaStream_t st) {
   k_lam_update<<<blocks_for((long long)nnod * ng, 256, kMaxBlocks), 256, 0, st>>>(G, ng, nnod, act, Kd, dnbar, cG,
-                                                                                  scal, lam, part);
+                                                                                  scal, lam, dlam, part);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lam_extrap(const BoxGeom& G, int ng, int nnod, const int* act, const double* dlam, double c,
+                              double* lam, cudaStream_t st) {
+  k_lam_extrap<<<blocks_for((long long)nnod * ng, 256, 8192), 256, 0, st>>>(G, ng, nnod, act, dlam, c, lam);
   return cudaGetLastError();
 }
 
