@@ -23,16 +23,42 @@
 
 namespace adp {
 
-// Everything after the cross-section update; false when a barrier wait ran
-// out of time (the core's status then says ADP_ERR_TIMEOUT).
-template <bool MIXED, int NG>
-__device__ __forceinline__ bool solve_core(const BatchInst& I, unsigned rank, unsigned size) {
+// The nodal update of one core (mod_cmfd.f90:339-383) and matrix_setup(0),
+// by the core's team.  Not inlined: it runs once per nodal interval, and as
+// a function of its own its register needs (the 2G x 2G face systems) do
+// not press on the register allocation of the outer-iteration loop, which
+// then fits the two-blocks-per-SM budget.  Returns: 0 go on, 1 stop (a
+// status, convergence or nout), -1 a barrier wait ran out of time.
+template <int NG>
+__device__ __noinline__ int nodal_stage(const BatchInst& I, unsigned rank, unsigned size) {
+  const NodalParams& N = I.np;
+  OuterCtl* C = I.op.ctl;
+  const int start = rank * blockDim.x + threadIdx.x, stride = size * blockDim.x;
+  tl_source_items(N, start, stride);
+  if (!team_barrier(C, size, rank)) return -1;
+  node_prep_items<NG>(N, start, stride);
+  if (!team_barrier(C, size, rank)) return -1;
+  NdBest best{0.0, 0x7fffffffffffffffLL, -1};
+  interface_items<NG>(N, start, stride, best);
+  nd_block_reduce(N, best, rank);
+  if (!team_barrier(C, size, rank)) return -1;
+  if (rank == 0 && threadIdx.x < 32) nodal_finish_warp(N, size);
+  if (!team_barrier(C, size, rank)) return -1;
+  if (vld(&C->status) || vld(&C->converged) || vld(&C->max_reached)) return 1;
+  assemble_items(I.ap0, start, stride);
+  if (!team_barrier(C, size, rank)) return -1;
+  return 0;
+}
+
+// XS_updt, dn = 0, the SANM constants, matrix_setup(1) and the first-call
+// start of one core (not inlined, as the nodal stage).  Returns 0 go on,
+// 1 stop (a cross-section check failed), -1 a barrier wait ran out of time.
+template <int NG>
+__device__ __noinline__ int setup_stage(const BatchInst& I, unsigned rank, unsigned size) {
   const OuterParams& P = I.op;
   const NodalParams& N = I.np;
   OuterCtl* C = P.ctl;
   const int start = rank * blockDim.x + threadIdx.x, stride = size * blockDim.x;
-  const bool lead = rank == 0 && threadIdx.x == 0;
-
   // XS_updt: D = 1/(3 sigtr), sigr = siga + sum_{h/=g} sigs(g->h), checks
   xs_updt_items(P.G, NG, N.act, I.nnod, I.sigtr, I.siga, P.sigs, const_cast<double*>(N.D),
                 const_cast<double*>(N.sigr), C, start, stride);
@@ -42,35 +68,49 @@ __device__ __forceinline__ bool solve_core(const BatchInst& I, unsigned rank, un
     const long long ndn = (long long)NG * 6 * P.G.NB;
     for (long long q = start; q < ndn; q += stride) dn[q] = 0.0;
   }
-  if (!team_barrier(C, size, rank)) return false;
-  if (vld(&C->status)) return true;
+  if (!team_barrier(C, size, rank)) return -1;
+  if (vld(&C->status)) return 1;
   if (I.kern == ADP_KERN_SANM) sanm_consts_items(N, start, stride);
   assemble_items(I.ap, start, stride);
   init_flux_items(P, start, stride);
-  if (!team_barrier(C, size, rank)) return false;
+  if (!team_barrier(C, size, rank)) return -1;
+  return 0;
+}
+
+template <int NG>
+__device__ __noinline__ bool power_stage(const BatchInst& I, unsigned rank, unsigned size);
+
+// Everything after the cross-section update; false when a barrier wait ran
+// out of time (the core's status then says ADP_ERR_TIMEOUT).
+template <bool MIXED, int NG>
+__device__ __forceinline__ bool solve_core(const BatchInst& I, unsigned rank, unsigned size) {
+  const OuterParams& P = I.op;
+  OuterCtl* C = P.ctl;
+
+  const int su = setup_stage<NG>(I, rank, size);
+  if (su < 0) return false;
+  if (su > 0) return true;
 
   for (int guard = 0; guard < 4 * P.nout + 8; ++guard) {
     outer_body<MIXED>(P, rank, size);
     if (!team_barrier(C, size, rank)) return false;
     if (vld(&C->status) || vld(&C->converged) || vld(&C->max_reached) || !vld(&C->nodal_due)) break;
-    // nodal update (mod_cmfd.f90:339-383) and matrix_setup(0)
-    tl_source_items(N, start, stride);
-    if (!team_barrier(C, size, rank)) return false;
-    node_prep_items<NG>(N, start, stride);
-    if (!team_barrier(C, size, rank)) return false;
-    NdBest best{0.0, 0x7fffffffffffffffLL, -1};
-    interface_items<NG>(N, start, stride, best);
-    nd_block_reduce(N, best, rank);
-    if (!team_barrier(C, size, rank)) return false;
-    if (rank == 0 && threadIdx.x < 32) nodal_finish_warp(N, size);
-    if (!team_barrier(C, size, rank)) return false;
-    if (vld(&C->status) || vld(&C->converged) || vld(&C->max_reached)) break;
-    assemble_items(I.ap0, start, stride);
-    if (!team_barrier(C, size, rank)) return false;
+    const int ns = nodal_stage<NG>(I, rank, size);
+    if (ns < 0) return false;
+    if (ns > 0) break;
   }
   if (vld(&C->status) || !vld(&C->converged)) return true;
+  return power_stage<NG>(I, rank, size);
+}
 
-  // PowDis: p = sum_g max(0, phi sigf vdel), normalised to sum 1
+// PowDis: p = sum_g max(0, phi sigf vdel), normalised to sum 1 (not
+// inlined, as the nodal stage).
+template <int NG>
+__device__ __noinline__ bool power_stage(const BatchInst& I, unsigned rank, unsigned size) {
+  const OuterParams& P = I.op;
+  OuterCtl* C = P.ctl;
+  const int start = rank * blockDim.x + threadIdx.x, stride = size * blockDim.x;
+  const bool lead = rank == 0 && threadIdx.x == 0;
   const BoxGeom& G = P.G;
   const double* phi = P.phi[vld(&C->cur)];
   double acc[1] = {0.0};
