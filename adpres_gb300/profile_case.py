@@ -3,11 +3,15 @@ solver in isolation (for example under ncu):
 
     python -m adpres_gb300.profile_case --config core_4g --planes 40 --precision mixed --solves 1
     python -m adpres_gb300.profile_case --config batch --members 16 --precision mixed
+    python -m adpres_gb300.profile_case --config batch --members 16 --shipped
     python -m adpres_gb300.profile_case --config full_core_3d --adjoint
 
 Prints k, the outer count and the device time of each solve.  The batch
-case solves the first `members` cores of the batched workload; --adjoint
-adds the discrete adjoint and dk/dSigma after the forward solve.
+case solves the first `members` cores of the batched workload, in the
+library's default schedule or, with --shipped, in the launch shape shipped
+for this GPU model in batch_tuned.json (applied as a cached configuration:
+one solve to measure the cores' times, then the re-planned schedule);
+--adjoint adds the discrete adjoint and dk/dSigma after the forward solve.
 """
 from __future__ import annotations
 
@@ -26,6 +30,7 @@ def main():
     ap.add_argument("--planes", type=int, default=80, help="axial planes of core_4g (20, 40 or 80)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--solves", type=int, default=1)
+    ap.add_argument("--shipped", action="store_true", help="batch case: the shipped tuned launch shape")
     a = ap.parse_args()
     if a.config == "batch":
         import json
@@ -36,6 +41,13 @@ def main():
             acc = json.load(f)
         decks = [deck.parse(synth.batch_member(acc["seed"], i)) for i in acc["accepted"][:a.members]]
         b = Batch(decks, precision=a.precision)
+        if a.shipped:
+            from .batch import TUNED_PATH
+            with open(TUNED_PATH) as f:
+                shipped = json.load(f)
+            cfg = next(iter(shipped.values()))["config"]
+            b._apply_cached(cfg)
+            print("shipped shape:", b.config(), flush=True)
         for _ in range(a.solves):
             res, ms = b.solve()
             print(f"batch of {len(decks)} ({sum(len(d.ix) for d in decks)} nodes) {a.precision}: "
