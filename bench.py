@@ -447,6 +447,11 @@ def batch_leg(flush, dist=None, steps=3, warmup=3, ncores=256, fp64_check=256):
         "device_key": device_key,
         "outers_mean": float(np.mean([r["outers"] for r in res])),
         "teams": sorted({r["team"] for r in res}),
+        # share of the launch's block-time spent inside some core's solve
+        # (each core's start-to-end time x its team size over blocks x the
+        # batch time): what the schedule leaves idle at the tail
+        "block_time_used": (sum(r["device_ms"] * r["team"] for r in res)
+                            / (props.multi_processor_count * int((cfg or {}).get("blocks_per_sm", 1)) * ms[-1])),
         "dk_pcm_vs_fp64_single": {"max": float(max(dks)), "rms": float(np.sqrt(np.mean(np.square(dks)))),
                                   "checked": len(dks), "fp64_single_s": t_fp64,
                                   "above_1pcm": int(sum(d > 1.0 for d in dks)),
