@@ -150,14 +150,15 @@ class Batch:
                 json.dump(db, f, indent=1)
         return cfg, ms.value, False
 
-    def _apply_cached(self, cfg):
-        """A cached configuration, then one solve to measure every core's
-        block time and a re-plan with those weights, as the autotuner plans
-        its candidates (the plan before any solve weighs cores by box rows
-        x groups)."""
+    def _apply_cached(self, cfg, rounds=3):
+        """A cached configuration, then `rounds` solves, each followed by a
+        re-plan with the per-core times gathered so far (the plan before
+        any solve weighs cores by box rows x groups; each re-plan adds the
+        times of the team sizes the last plan chose)."""
         self.set_config(**cfg)
-        self.solve(check=False)
-        self.set_config(**cfg)
+        for _ in range(rounds):
+            self.solve(check=False)
+            self.set_config(**cfg)
 
     # -- solve and results ----------------------------------------------------
     def solve(self, check=True):

@@ -5,22 +5,33 @@
 // mod_control.f90:11-47); a batch owns one single-core handle per core (the
 // same device state and the same per-core API for results) and runs all of
 // them in one launch of k_batch (batch_kernel.cuh).  The schedule assigns
-// each core a team of blocks and each block an ordered task list:
-//   - weights: box rows x groups until a solve has been timed, then the
-//     measured block time of each core (device clock, t_ns);
-//   - team size: ceil(weight * grain / (total / blocks)), at most max_team;
-//   - longest-first list scheduling: a core goes to the `size` least loaded
-//     blocks and starts when the last of them is free.
+// each core a team of blocks and each block an ordered task list, by
+// longest-first list scheduling: a core goes to the `size` least loaded
+// blocks and starts when the last of them is free.
+//   - Before any solve is timed: weights box rows x groups, team size
+//     ceil(weight * grain / (total / blocks)), at most max_team.
+//   - Once timed: every core's time at each (kernel shape, team size) it
+//     ran at is kept (device clock, t_ns: from the arrival of the last
+//     block of its team to its end).  Its duration on s blocks is that time,
+//     or the time at the nearest size scaled by the model
+//     t(s) = A (1/s + kappa), kappa fitted to all cores timed at two sizes.
+//     For a target end T each core (longest first) takes the smallest team,
+//     at most max_team, that ends by T on the least loaded blocks (else the
+//     one that ends earliest); T is scanned upward from a lower bound (the
+//     least block-time of all cores over the blocks, the longest core at
+//     max_team) and the plan with the earliest predicted end is kept.
 // Since cores are placed in one global order and appended to the chosen
 // blocks' lists in that order, every block's list is a subsequence of the
 // same order and no cycle of teams waiting on each other can form.
-// The autotuner (adp_batch_autotune) times the whole batch over block size,
-// max_team and grain with measured weights and keeps the fastest.
+// The autotuner (adp_batch_autotune) times the whole batch over kernel
+// shape and max_team and keeps the fastest.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <map>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -90,7 +101,10 @@ struct adp_batch {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::vector<adp_handle*> core;
   std::vector<double> rows;          // box rows x groups per core
-  std::vector<double> measured;      // block-ns per core from the last solve (0: none)
+  // per core: ns of its solves by kernel shape and team size (shape_key)
+  std::vector<std::map<int, double>> took;
+  std::vector<double> last_t;        // per core: ns of the last solve (0: none) ...
+  std::vector<int> last_team;        // ... on a team of this size
   // device
   BatchInst* d_inst = nullptr;
   unsigned long long* d_tns = nullptr;
@@ -109,6 +123,7 @@ struct adp_batch {
   std::vector<int> begin;
   std::vector<int> team;             // team size per core
   bool plan_ok = false;
+  bool keep_tasks = false;           // re-capture without re-planning
   cudaGraphExec_t gexec = nullptr;
   bool graph_ok = false;
   double last_ms = 0.0;
@@ -135,46 +150,188 @@ void drop_graph(adp_batch* b) {
   b->graph_ok = false;
 }
 
-// Longest-first list scheduling with teams (see the file comment).
-void make_plan(adp_batch* b) {
-  const int n = b->n, B = b->blocks;
-  std::vector<double> w(n);
-  bool meas = true;
-  for (int i = 0; i < n; ++i) meas = meas && b->measured[i] > 0.0;
-  for (int i = 0; i < n; ++i) w[i] = meas ? b->measured[i] : b->rows[i];
-  const double total = std::accumulate(w.begin(), w.end(), 0.0);
-  const double avg = total / B;
-  std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return w[a] > w[c]; });
+// Team overhead kappa of the duration model t(s) = A (1/s + kappa): least
+// squares over every pair of team sizes some core was timed at (kappa in
+// [0, 0.3] by steps of 0.002); 0.03 when no core has two sizes yet.
+// Key of a time in adp_batch::took: kernel shape and team size.
+int shape_key(const adp_batch_config& c, int s) { return ((c.threads / 256) * 8 + c.blocks_per_sm) * 65536 + s; }
+
+// Times of core i in the current kernel shape: team size -> ns.
+std::map<int, double> times_here(const adp_batch* b, int i) {
+  std::map<int, double> m;
+  const int lo = shape_key(b->cfg, 0), hi = shape_key(b->cfg, 65535);
+  for (auto it = b->took[i].lower_bound(lo); it != b->took[i].end() && it->first <= hi; ++it)
+    m[it->first - lo] = it->second;
+  return m;
+}
+
+double fit_kappa(const adp_batch* b) {
+  std::vector<double> r, q0, q1;   // t(s1)/t(s0) with 1/s0, 1/s1
+  for (int i = 0; i < b->n; ++i) {
+    const std::map<int, double> m = times_here(b, i);
+    for (auto a = m.begin(); a != m.end(); ++a)
+      for (auto c = std::next(a); c != m.end(); ++c) {
+        r.push_back(c->second / a->second);
+        q0.push_back(1.0 / a->first);
+        q1.push_back(1.0 / c->first);
+      }
+  }
+  if (r.empty()) return 0.03;
+  double best = 0.03, err_best = 1e300;
+  for (int j = 0; j <= 150; ++j) {
+    const double k = 0.002 * j;
+    double e = 0.0;
+    for (size_t p = 0; p < r.size(); ++p) {
+      const double d = r[p] - (q1[p] + k) / (q0[p] + k);
+      e += d * d;
+    }
+    if (e < err_best) {
+      err_best = e;
+      best = k;
+    }
+  }
+  return best;
+}
+
+// Predicted duration of core i on a team of s blocks: its time at s when
+// timed in this kernel shape, else the time at the nearest size timed (or
+// of the last solve, in any shape) scaled by (1/s + kappa) / (1/s0 + kappa).
+double duration(const adp_batch* b, int i, int s, double kappa) {
+  const std::map<int, double> m = times_here(b, i);
+  auto it = m.find(s);
+  if (it != m.end()) return it->second;
+  int s0 = b->last_team[i];
+  double t0 = b->last_t[i];
+  double gap = 1e300;
+  for (const auto& e : m) {
+    const double g = std::fabs(std::log((double)e.first / s));
+    if (g < gap) {
+      gap = g;
+      s0 = e.first;
+      t0 = e.second;
+    }
+  }
+  return t0 * (1.0 / s + kappa) / (1.0 / s0 + kappa);
+}
+
+struct Plan {
+  std::vector<std::vector<BatchTask>> lists;
+  std::vector<int> team;
+  double makespan = 0.0;
+};
+
+// One list schedule: cores longest first, each on the `size` least loaded
+// blocks (ties to the lower index), starting when the last of them is free.
+// size(i, sorted loads) picks the team size.
+template <class SizeRule>
+Plan list_schedule(int n, int B, const std::vector<int>& order, SizeRule size,
+                   const std::function<double(int, int)>& dur) {
+  Plan P;
+  P.lists.assign(B, {});
+  P.team.assign(n, 1);
   std::vector<double> load(B, 0.0);
-  std::vector<std::vector<BatchTask>> lists(B);
   std::vector<int> idx(B);
-  b->team.assign(n, 1);
-  const int maxteam = std::max(1, std::min(b->cfg.max_team, B));
-  const double grain = b->cfg.grain > 0 ? b->cfg.grain : 1.0;
   for (int i : order) {
-    int s = (int)std::ceil(w[i] * grain / avg - 1e-9);
-    s = std::max(1, std::min(s, maxteam));
     std::iota(idx.begin(), idx.end(), 0);
-    std::partial_sort(idx.begin(), idx.begin() + s, idx.end(), [&](int a, int c) {
+    const int smax = size.cap;
+    std::partial_sort(idx.begin(), idx.begin() + smax, idx.end(), [&](int a, int c) {
       return load[a] < load[c] || (load[a] == load[c] && a < c);
     });
+    const int s = size(i, load, idx);
     std::sort(idx.begin(), idx.begin() + s);
     double t0 = 0.0;
     for (int k = 0; k < s; ++k) t0 = std::max(t0, load[idx[k]]);
-    const double t1 = t0 + w[i] / s;
+    const double t1 = t0 + dur(i, s);
     for (int k = 0; k < s; ++k) {
-      lists[idx[k]].push_back(BatchTask{i, k, s, 0});
+      P.lists[idx[k]].push_back(BatchTask{i, k, s, 0});
       load[idx[k]] = t1;
     }
-    b->team[i] = s;
+    P.team[i] = s;
   }
+  P.makespan = *std::max_element(load.begin(), load.end());
+  return P;
+}
+
+// Longest-first list scheduling with teams (see the file comment).
+void make_plan(adp_batch* b) {
+  const int n = b->n, B = b->blocks;
+  bool meas = true;
+  for (int i = 0; i < n; ++i) meas = meas && b->last_t[i] > 0.0;
+  const int maxteam = std::max(1, std::min(b->cfg.max_team, B));
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  Plan P;
+  if (!meas) {
+    // before any solve is timed: weights box rows x groups, team size from
+    // the grain
+    const std::vector<double>& w = b->rows;
+    const double avg = std::accumulate(w.begin(), w.end(), 0.0) / B;
+    const double grain = b->cfg.grain > 0 ? b->cfg.grain : 1.0;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return w[a] > w[c]; });
+    struct Grain {
+      int cap;
+      const std::vector<double>& w;
+      double avg, grain;
+      int operator()(int i, const std::vector<double>&, const std::vector<int>&) const {
+        return std::max(1, std::min((int)std::ceil(w[i] * grain / avg - 1e-9), cap));
+      }
+    } rule{maxteam, w, avg, grain};
+    P = list_schedule(n, B, order, rule, [&](int i, int s) { return w[i] / s; });
+  } else {
+    // timed: for a target end T each core takes the smallest team that
+    // ends by T on the least loaded blocks (else the team that ends
+    // earliest); T runs over [lower bound, 1.3 x lower bound] and the plan
+    // with the earliest predicted end is kept
+    const double kappa = fit_kappa(b);
+    std::vector<double> d1(n);
+    double work = 0.0, longest = 0.0;
+    for (int i = 0; i < n; ++i) {
+      d1[i] = duration(b, i, 1, kappa);
+      double wmin = 1e300;
+      for (int s = 1; s <= maxteam; ++s) wmin = std::min(wmin, s * duration(b, i, s, kappa));
+      work += wmin;
+      longest = std::max(longest, duration(b, i, maxteam, kappa));
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return d1[a] > d1[c]; });
+    // durations per core and team size, computed once
+    std::vector<double> dt((size_t)n * (maxteam + 1));
+    for (int i = 0; i < n; ++i)
+      for (int s = 1; s <= maxteam; ++s) dt[(size_t)i * (maxteam + 1) + s] = duration(b, i, s, kappa);
+    std::function<double(int, int)> dur = [&](int i, int s) { return dt[(size_t)i * (maxteam + 1) + s]; };
+    const double lb = std::max(work / B, longest);
+    struct Fill {
+      int cap;
+      double T;
+      const std::function<double(int, int)>& dur;
+      int operator()(int i, const std::vector<double>& load, const std::vector<int>& idx) const {
+        int best = 1;
+        double fbest = 1e300;
+        for (int s = 1; s <= cap; ++s) {
+          const double f = load[idx[s - 1]] + dur(i, s);
+          if (f <= T) return s;
+          if (f < fbest) {
+            fbest = f;
+            best = s;
+          }
+        }
+        return best;
+      }
+    };
+    bool have = false;
+    for (int j = 0; j <= 60; ++j) {
+      Plan Q = list_schedule(n, B, order, Fill{maxteam, lb * (1.0 + 0.005 * j), dur}, dur);
+      if (!have || Q.makespan < P.makespan) {
+        P = std::move(Q);
+        have = true;
+      }
+    }
+  }
+  b->team = P.team;
   b->tasks.clear();
   b->begin.assign(B + 1, 0);
   for (int c = 0; c < B; ++c) {
     b->begin[c] = (int)b->tasks.size();
-    b->tasks.insert(b->tasks.end(), lists[c].begin(), lists[c].end());
+    b->tasks.insert(b->tasks.end(), P.lists[c].begin(), P.lists[c].end());
   }
   b->begin[B] = (int)b->tasks.size();
 }
@@ -217,7 +374,8 @@ adp_status prepare(adp_batch* b) {
   const int occ = batch_max_blocks_per_sm(b->mixed, b->ng, b->cfg.threads, b->cfg.blocks_per_sm);
   if (occ < 1) return bfail(b, ADP_ERR_CUDA, "batched kernel cannot be resident with this block size");
   b->blocks = std::min(b->sms * std::min(occ, std::max(1, b->cfg.blocks_per_sm)), kMaxBlocks);
-  make_plan(b);
+  if (!b->keep_tasks) make_plan(b);
+  b->keep_tasks = false;
   adp_status s = upload_plan(b);
   if (s != ADP_OK) return s;
   if (b->cfg.use_graph) {
@@ -315,7 +473,9 @@ adp_status adp_batch_create(int n, const adp_geom* geoms, const adp_opts* opts, 
   }
   std::vector<BatchInst> inst(n);
   b->rows.resize(n);
-  b->measured.assign(n, 0.0);
+  b->took.assign(n, {});
+  b->last_t.assign(n, 0.0);
+  b->last_team.assign(n, 1);
   for (int i = 0; i < n; ++i) {
     adp_handle* h = b->core[i];
     BatchInst& I = inst[i];
@@ -381,6 +541,11 @@ adp_status adp_batch_set_config(adp_batch* b, const adp_batch_config* c) {
   if (!batch_supported(b->ng, c->threads)) return bfail(b, ADP_ERR_INPUT, "adp_batch_set_config: threads must be 256 or 512");
   if (c->max_team < 1 || c->blocks_per_sm < 1 || !(c->grain > 0))
     return bfail(b, ADP_ERR_INPUT, "adp_batch_set_config: max_team, blocks_per_sm >= 1 and grain > 0");
+  // a change of use_graph alone keeps the schedule (the same tasks, so the
+  // same results to the bit); any other call re-plans from the latest times
+  b->keep_tasks = c->threads == b->cfg.threads && c->max_team == b->cfg.max_team && c->grain == b->cfg.grain &&
+                  c->blocks_per_sm == b->cfg.blocks_per_sm && c->use_graph != b->cfg.use_graph &&
+                  !b->tasks.empty();
   b->cfg = *c;
   b->plan_ok = false;
   return ADP_OK;
@@ -413,7 +578,11 @@ adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_m
     const OuterCtl& c = b->h_res[i];
     const unsigned long long t0 = b->h_tns[2 * i], t1 = b->h_tns[2 * i + 1];
     const double t = (t1 > t0) ? (double)(t1 - t0) : 0.0;
-    b->measured[i] = t * b->team[i];
+    if (t > 0.0) {
+      b->last_t[i] = t;
+      b->last_team[i] = b->team[i];
+      b->took[i][shape_key(b->cfg, b->team[i])] = t;
+    }
     adp_status st = (adp_status)c.status;
     if (st == ADP_OK && !c.converged) st = ADP_ERR_MAXOUTER;
     if (st != ADP_OK && worst == ADP_OK) worst = st;
@@ -442,38 +611,36 @@ adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_m
 adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best_out, double* best_ms) {
   if (!b) return ADP_ERR_INPUT;
   const adp_batch_config base = b->cfg;
-  // measured weights from one solve with the current settings
+  // per-core times from one solve with the current settings
   adp_status s = adp_batch_solve(b, nullptr, nullptr);
   if (s != ADP_OK) return s;
   adp_batch_config best = base;
   double best_t = 1e300;
-  // kernel shapes: (threads, blocks per SM) = (256, 1), (256, 2), (512, 1)
+  // kernel shapes: (threads, blocks per SM) = (256, 1), (256, 2), (512, 1);
+  // each candidate is solved twice, the second time planned with the
+  // times of its own team sizes from the first
   const int shapes[3][2] = {{256, 1}, {256, 2}, {512, 1}};
-  const int teams[3] = {2, 8, 32};
-  const double grains[2] = {1.0, 4.0};
-  const std::vector<double> meas = b->measured;
+  const int teams[4] = {4, 8, 16, 32};
   for (const auto& sh : shapes) {
     if (batch_max_blocks_per_sm(b->mixed, b->ng, sh[0], sh[1]) < sh[1]) continue;
-    for (int mt : teams)
-      for (double gr : grains) {
-        adp_batch_config c = base;
-        c.threads = sh[0];
-        c.max_team = mt;
-        c.grain = gr;
-        c.blocks_per_sm = sh[1];
+    for (int mt : teams) {
+      adp_batch_config c = base;
+      c.threads = sh[0];
+      c.max_team = mt;
+      c.blocks_per_sm = sh[1];
+      double ms = 0.0;
+      for (int rep = 0; rep < 2; ++rep) {
         s = adp_batch_set_config(b, &c);
         if (s != ADP_OK) return s;
-        b->measured = meas;   // every candidate plans from the same measurement
-        double ms = 0.0;
         s = adp_batch_solve(b, nullptr, &ms);
         if (s != ADP_OK) return s;
-        if (ms < best_t) {
-          best_t = ms;
-          best = c;
-        }
       }
+      if (ms < best_t) {
+        best_t = ms;
+        best = c;
+      }
+    }
   }
-  b->measured = meas;
   s = adp_batch_set_config(b, &best);
   if (s != ADP_OK) return s;
   if (best_out) *best_out = best;

@@ -150,10 +150,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
       for (int i = threadIdx.x; i < (int)(sizeof(BatchInst) / 4); i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
-    const bool lead = tk.rank == 0 && threadIdx.x == 0;
-    if (lead) sI.t_ns[0] = globaltimer_ns();
+    // The core's time runs from the arrival of the last block of its team
+    // (every member raises the start to its own arrival; the time a member
+    // waited for the others is not the core's work) to rank 0's end.
+    if (threadIdx.x == 0) atomicMax(sI.t_ns, globaltimer_ns());
     solve_core<MIXED, NG>(sI, (unsigned)tk.rank, (unsigned)tk.size);
-    if (lead) sI.t_ns[1] = globaltimer_ns();
+    if (tk.rank == 0 && threadIdx.x == 0) sI.t_ns[1] = globaltimer_ns();
   }
 }
 

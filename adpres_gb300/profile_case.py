@@ -10,7 +10,8 @@ Prints k, the outer count and the device time of each solve.  The batch
 case solves the first `members` cores of the batched workload, in the
 library's default schedule or, with --shipped, in the launch shape shipped
 for this GPU model in batch_tuned.json (applied as a cached configuration:
-one solve to measure the cores' times, then the re-planned schedule);
+three solves, each followed by a re-plan with the cores' times, so the
+solve printed is the fourth launch of k_batch);
 --adjoint adds the discrete adjoint and dk/dSigma after the forward solve.
 """
 from __future__ import annotations

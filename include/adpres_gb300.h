@@ -456,9 +456,11 @@ adp_status adp_trans_step(adp_handle* h, double dt, int omeg_mode, adp_trans_res
 typedef struct adp_batch adp_batch;
 
 /* Launch shape and schedule: threads per block (256 or 512), the largest
- * team of blocks on one core, grain (cores are split into teams so that a
- * team member's share is about 1/grain of a block's average load),
- * blocks per SM (2 with 256 threads selects the kernel built for two
+ * team of blocks on one core, grain (for the first schedule, before any
+ * solve is timed: cores are split into teams so that a team member's share
+ * is about 1/grain of a block's average load; once cores are timed, each
+ * takes the smallest team that meets the schedule's target end), blocks
+ * per SM (2 with 256 threads selects the kernel built for two
  * resident blocks per SM, 128 registers a thread), and whether the solve is
  * replayed from a captured graph. */
 typedef struct adp_batch_config {
@@ -473,7 +475,8 @@ typedef struct adp_batch_result {
   int status;               /* adp_status of the core                          */
   int converged, outers, nodal_updates;
   double keff, ser, fer, ndmax;
-  double device_ms;         /* device time of the core's team (global timer)   */
+  double device_ms;         /* device time of the core (global timer), from    */
+                            /* the arrival of its team's last block           */
   int team;                 /* blocks that solved it                           */
 } adp_batch_result;
 
@@ -484,6 +487,9 @@ size_t adp_batch_last_error(const adp_batch* b, char* buf, size_t len);
 adp_status adp_batch_set_xs(adp_batch* b, int i, int nmat, const double* sigtr, const double* siga, const double* nuf,
                             const double* sigf, const double* chi, const int* mat, const double* sigs,
                             const double* dc);
+/* Sets the configuration and re-plans the schedule from the latest per-core
+ * times (so a call with the unchanged configuration after a solve re-plans
+ * with that solve's times); a change of use_graph alone keeps the schedule. */
 adp_status adp_batch_set_config(adp_batch* b, const adp_batch_config* c);
 adp_status adp_batch_get_config(const adp_batch* b, adp_batch_config* c);
 /* Solve every core from a fresh start; res has n entries (may be NULL);
@@ -491,9 +497,10 @@ adp_status adp_batch_get_config(const adp_batch* b, adp_batch_config* c);
  * core's status, or ADP_OK. */
 adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_ms);
 /* Time the batch over the kernel shapes (threads, blocks per SM) = (256, 1),
- * (256, 2), (512, 1) x max_team {2, 8, 32} x grain {1, 4} (schedules built
- * from the measured per-core times of one solve) and keep the fastest:
- * 19 solves of the whole batch. */
+ * (256, 2), (512, 1) x max_team {4, 8, 16, 32} and keep the fastest: one
+ * solve to time the cores, then each candidate solved twice (the second
+ * schedule planned with the times of the first), 25 solves of the whole
+ * batch.  best_ms is the winner's second solve. */
 adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best, double* best_ms);
 adp_status adp_batch_core(adp_batch* b, int i, adp_handle** h);
 /* Per-outer trace of core i from the last adp_batch_solve (as the trace of
