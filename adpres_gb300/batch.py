@@ -127,13 +127,13 @@ class Batch:
                 with open(TUNED_PATH) as f:
                     shipped = json.load(f)
                 if key in shipped:
-                    self._apply_cached(shipped[key]["config"])
+                    self.apply_config(shipped[key]["config"])
                     return shipped[key]["config"], shipped[key]["ms"], True
         if cache and os.path.exists(cache):
             with open(cache) as f:
                 db = json.load(f)
             if key in db:
-                self._apply_cached(db[key]["config"])
+                self.apply_config(db[key]["config"])
                 return db[key]["config"], db[key]["ms"], True
         c = _lib.AdpBatchConfig()
         ms = ctypes.c_double()
@@ -150,11 +150,12 @@ class Batch:
                 json.dump(db, f, indent=1)
         return cfg, ms.value, False
 
-    def _apply_cached(self, cfg, rounds=3):
-        """A cached configuration, then `rounds` solves, each followed by a
-        re-plan with the per-core times gathered so far (the plan before
-        any solve weighs cores by box rows x groups; each re-plan adds the
-        times of the team sizes the last plan chose)."""
+    def apply_config(self, cfg, rounds=3):
+        """Set a configuration (a cached or shipped one) and settle its
+        schedule: `rounds` solves, each followed by a re-plan with the
+        per-core times gathered so far (the plan before any solve weighs
+        cores by box rows x groups; each re-plan adds the times of the team
+        sizes the last plan chose)."""
         self.set_config(**cfg)
         for _ in range(rounds):
             self.solve(check=False)

@@ -47,7 +47,7 @@ def main():
             with open(TUNED_PATH) as f:
                 shipped = json.load(f)
             cfg = next(iter(shipped.values()))["config"]
-            b._apply_cached(cfg)
+            b.apply_config(cfg)
             print("shipped shape:", b.config(), flush=True)
         for _ in range(a.solves):
             res, ms = b.solve()

@@ -119,6 +119,24 @@ def test_team_sizes_give_the_same_answer(members):
         assert pcm(a["keff"], c["keff"]) <= 0.01
 
 
+def test_timed_replans_keep_the_answer_and_the_team_cap(members):
+    """After timed solves the schedule is re-planned from the cores' times
+    per team size (target-end team sizing); the teams stay within max_team,
+    each core's time is recorded, and the answers stay those of the first
+    (box-rows) plan."""
+    from adpres_gb300.batch import Batch
+    b = Batch([deck.parse(t) for t in members[:6]], precision="fp64")
+    cfg = dict(threads=256, max_team=4, grain=1.0, blocks_per_sm=1, use_graph=1)
+    b.set_config(**cfg)
+    r0, _ = b.solve()
+    b.apply_config(cfg, rounds=2)
+    r1, _ = b.solve()
+    for a, c in zip(r0, r1):
+        assert c["converged"] == 1 and 1 <= c["team"] <= 4 and c["device_ms"] > 0
+        assert pcm(a["keff"], c["keff"]) <= 0.01
+        assert a["outers"] == c["outers"]
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_kernel_shapes_give_the_same_answer(members, precision):
     """The three kernel shapes (256 threads for one or two blocks per SM,
