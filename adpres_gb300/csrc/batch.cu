@@ -17,9 +17,9 @@
 //     t(s) = A (1/s + kappa), kappa fitted to all cores timed at two sizes.
 //     For a target end T each core (longest first) takes the smallest team,
 //     at most max_team, that ends by T on the least loaded blocks (else the
-//     one that ends earliest); T is scanned upward from a lower bound (the
-//     least block-time of all cores over the blocks, the longest core at
-//     max_team) and the plan with the earliest predicted end is kept.
+//     one that ends earliest); T is scanned over [1, 1.3] x a lower bound
+//     (the least block-time of all cores over the blocks, the longest core
+//     at max_team) and the plan with the earliest predicted end is kept.
 // Since cores are placed in one global order and appended to the chosen
 // blocks' lists in that order, every block's list is a subsequence of the
 // same order and no cycle of teams waiting on each other can form.
@@ -317,9 +317,12 @@ void make_plan(adp_batch* b) {
         return best;
       }
     };
+    // 61 targets 0.5% apart; fewer (at least 9, over the same range) when
+    // cores x blocks is large, to bound the host time of a plan
+    const int nt = std::max(9, std::min(61, (int)(2.0e7 / ((double)n * B))));
     bool have = false;
-    for (int j = 0; j <= 60; ++j) {
-      Plan Q = list_schedule(n, B, order, Fill{maxteam, lb * (1.0 + 0.005 * j), dur}, dur);
+    for (int j = 0; j < nt; ++j) {
+      Plan Q = list_schedule(n, B, order, Fill{maxteam, lb * (1.0 + 0.3 * j / (nt - 1)), dur}, dur);
       if (!have || Q.makespan < P.makespan) {
         P = std::move(Q);
         have = true;
