@@ -137,6 +137,40 @@ def test_timed_replans_keep_the_answer_and_the_team_cap(members):
         assert a["outers"] == c["outers"]
 
 
+def test_many_small_cores_more_cores_than_blocks():
+    """400 small ragged cores (more cores than the 304 blocks of the
+    two-block shape, so blocks run several cores in turn), with the
+    schedule re-planned from timed solves: the cores the oracle converges
+    on converge (a sample within 0.1 pcm and 1e-6 in power of its single
+    FP64 solve), and the one whose two-node iteration diverges in the
+    oracle (mod_nodal.f90:131-142) reports ADP_ERR_DIVERGED for itself."""
+    from adpres_gb300 import _lib
+    from adpres_gb300.batch import Batch
+    texts = [synth.small_core(seed=100 + i, nx=3 + i % 3, ny=3 + (i // 3) % 3, nz=2 + i % 2) for i in range(400)]
+    diverged = set()
+    for i, t in enumerate(texts):
+        try:
+            oracle.Oracle(text=t).run()
+        except oracle.OracleError as e:
+            assert e.code == oracle.ORA_ERR_DIVERGED
+            diverged.add(i)
+    assert len(diverged) < 10
+    b = Batch([deck.parse(t) for t in texts], precision="fp64")
+    b.apply_config(dict(threads=256, max_team=4, grain=1.0, blocks_per_sm=2, use_graph=1), rounds=2)
+    res, _ = b.solve(check=False)
+    for i, r in enumerate(res):
+        if i in diverged:
+            assert r["status"] == _lib.ADP_ERR_DIVERGED
+        else:
+            assert r["status"] == 0 and r["converged"] == 1
+    for i in range(0, 400, 41):
+        if i in diverged:
+            continue
+        r, p = _single(texts[i])
+        assert pcm(res[i]["keff"], r.keff) <= 0.1
+        assert max_rel(b.power(i), p) <= 1e-6
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_kernel_shapes_give_the_same_answer(members, precision):
     """The three kernel shapes (256 threads for one or two blocks per SM,
