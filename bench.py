@@ -633,9 +633,11 @@ def run_ours(args):
     perr = np.abs(p_mixed[m] - p64[m]) / p64[m]
     core64.close()
 
-    adjoint = adjoint_leg(flush)
-    boron = cbsearch_leg(flush)
-    transient = transient_leg()
+    # single-GPU legs reported by rank 0 only; with N ranks the others go
+    # straight to the batched leg's first barrier
+    adjoint = adjoint_leg(flush) if rank == 0 else None
+    boron = cbsearch_leg(flush) if rank == 0 else None
+    transient = transient_leg() if rank == 0 else None
     batched = batch_leg(flush, dist) if not args.no_batch else None
     batched_stated = (batch_stated_leg(flush, batched.get("config")) if batched and world == 1 else None)
 
