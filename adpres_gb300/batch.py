@@ -37,6 +37,29 @@ def node_tables(dk):
     return dict(sigtr=dk.xsigtr[m], siga=dk.xsiga[m], nuf=dk.xnuf[m], sigf=dk.xsigf[m], sigs=dk.xsigs[m])
 
 
+def _read_cache(path):
+    """The tuning cache, or {} when it is absent or unreadable (a cache is
+    an optimisation: a damaged one costs a tuning run, not the solve)."""
+    try:
+        with open(path) as f:
+            db = json.load(f)
+        return db if isinstance(db, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _write_cache(path, db):
+    """Write the cache through a file of this process and an atomic rename,
+    so that processes sharing the path (one per GPU) never read a partial
+    file; the last writer's entries win."""
+    d = os.path.dirname(os.path.abspath(path))
+    os.makedirs(d, exist_ok=True)
+    tmp = os.path.join(d, ".%s.%d.tmp" % (os.path.basename(path), os.getpid()))
+    with open(tmp, "w") as f:
+        json.dump(db, f, indent=1)
+    os.replace(tmp, path)
+
+
 class Batch:
     def __init__(self, decks, precision="mixed", **over):
         self.L = _lib.load()
@@ -129,9 +152,8 @@ class Batch:
                 if key in shipped:
                     self.apply_config(shipped[key]["config"])
                     return shipped[key]["config"], shipped[key]["ms"], True
-        if cache and os.path.exists(cache):
-            with open(cache) as f:
-                db = json.load(f)
+        if cache:
+            db = _read_cache(cache)
             if key in db:
                 self.apply_config(db[key]["config"])
                 return db[key]["config"], db[key]["ms"], True
@@ -140,14 +162,9 @@ class Batch:
         self._check(self.L.adp_batch_autotune(self.h, ctypes.byref(c), ctypes.byref(ms)))
         cfg = {k: getattr(c, k) for k, _ in c._fields_}
         if cache:
-            db = {}
-            if os.path.exists(cache):
-                with open(cache) as f:
-                    db = json.load(f)
+            db = _read_cache(cache)
             db[key] = {"config": cfg, "ms": ms.value}
-            os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
-            with open(cache, "w") as f:
-                json.dump(db, f, indent=1)
+            _write_cache(cache, db)
         return cfg, ms.value, False
 
     def apply_config(self, cfg, rounds=3):
