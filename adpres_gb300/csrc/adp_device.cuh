@@ -382,6 +382,59 @@ __device__ __forceinline__ void warp_all_ff(ff (&x)[NQ]) {
   }
 }
 
+// The butterfly of warp_all_ff over the lanes below 2 * o0 (o0 a power of
+// two, the lanes above it ignored), leaving the totals in lane 0 only, with
+// the quantities scattered over the lanes: at each of the first log2(NQ)
+// levels a lane keeps half of its quantities and hands the partner the
+// other half, so the next levels carry one quantity per lane, and lane 0
+// collects the NQ totals at the end.  Every total is formed from the same
+// pairs in the same order as in warp_all_ff (the sum of a lane and its
+// partner at each level; the sums are commutative), so the totals are the
+// same to the bit; a level of warp_all_ff that only adds lanes holding
+// exact zeros is left out.  With fewer levels than quantities it runs
+// warp_all_ff.
+template <int NQ, unsigned MAXMASK>
+__device__ __forceinline__ void warp_reduce_lane0_ff(ff (&x)[NQ], int o0) {
+  static_assert(NQ == 1 || NQ == 2 || NQ == 4, "1, 2 or 4 quantities");
+  constexpr int L = NQ == 4 ? 2 : (NQ == 2 ? 1 : 0);
+  if ((o0 >> (L > 0 ? L - 1 : 0)) < 1 && L > 0) {
+    warp_all_ff<NQ, MAXMASK>(x);
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  int o = o0, q0 = 0;
+  ff v[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = x[q];
+#pragma unroll
+  for (int m = NQ; m > 1; m >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int j = 0; j < m / 2; ++j) {
+      const ff give = up ? v[j] : v[j + m / 2];
+      const ff keep = up ? v[j + m / 2] : v[j];
+      const ff y{__shfl_xor_sync(0xffffffffu, give.hi, o), __shfl_xor_sync(0xffffffffu, give.lo, o)};
+      const int q = q0 + (up ? m / 2 : 0) + j;
+      v[j] = ((MAXMASK >> q) & 1u) ? (y.hi > keep.hi ? y : keep) : ff_add(keep, y);
+    }
+    if (up) q0 += m / 2;
+    o >>= 1;
+  }
+  for (; o > 0; o >>= 1) {
+    const ff y{__shfl_xor_sync(0xffffffffu, v[0].hi, o), __shfl_xor_sync(0xffffffffu, v[0].lo, o)};
+    v[0] = ((MAXMASK >> q0) & 1u) ? (y.hi > v[0].hi ? y : v[0]) : ff_add(v[0], y);
+  }
+  // quantity q sits in the lanes whose scatter bits spell q: the lowest is
+  // the sum of the scatter offsets of q's bits
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    int src = 0;
+#pragma unroll
+    for (int i = 0; i < L; ++i) src += ((q >> (L - 1 - i)) & 1) * (o0 >> i);
+    x[q] = ff{__shfl_sync(0xffffffffu, v[0].hi, src), __shfl_sync(0xffffffffu, v[0].lo, src)};
+  }
+}
+
 template <int NQ, unsigned MAXMASK>
 __device__ __forceinline__ bool grid_reduce_ff(OuterCtl* C, unsigned nblocks, unsigned rank, double* slot_d,
                                                const ff (&v)[NQ], double (&tot)[NQ]) {
@@ -393,7 +446,7 @@ __device__ __forceinline__ bool grid_reduce_ff(OuterCtl* C, unsigned nblocks, un
   ff x[NQ];
 #pragma unroll
   for (int q = 0; q < NQ; ++q) x[q] = v[q];
-  warp_all_ff<NQ, MAXMASK>(x);
+  warp_reduce_lane0_ff<NQ, MAXMASK>(x, 16);
   if (lane == 0) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) sw[q][w] = x[q];
@@ -402,7 +455,10 @@ __device__ __forceinline__ bool grid_reduce_ff(OuterCtl* C, unsigned nblocks, un
   if (w == 0) {
 #pragma unroll
     for (int q = 0; q < NQ; ++q) x[q] = lane < nw ? sw[q][lane] : ff{0.f, 0.f};
-    warp_all_ff<NQ, MAXMASK>(x);
+    // the levels that reach the nw lanes holding a warp's sum
+    int o0 = 16;
+    while (o0 > 1 && o0 >= nw) o0 >>= 1;
+    if (nw > 1) warp_reduce_lane0_ff<NQ, MAXMASK>(x, o0);
     int ok = 1;
     if (nblocks > 1) {
       if (lane == 0) {
@@ -417,23 +473,27 @@ __device__ __forceinline__ bool grid_reduce_ff(OuterCtl* C, unsigned nblocks, un
 #pragma unroll
         for (int q = 0; q < NQ; ++q) x[q] = ff{0.f, 0.f};
         for (int base = 0; base < nblk; base += 256) {
+          // partials past the last block would add exact zeros: left out
+          const int kmax = min(8, (nblk - base + 31) >> 5);
           float2 y[NQ][8];
 #pragma unroll
           for (int q = 0; q < NQ; ++q)
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
               const int i = base + lane + 32 * k;
-              y[q][k] = (i < nblk) ? __ldcg(slot + q * kMaxBlocks + i) : make_float2(0.f, 0.f);
+              y[q][k] = (k < kmax && i < nblk) ? __ldcg(slot + q * kMaxBlocks + i) : make_float2(0.f, 0.f);
             }
 #pragma unroll
           for (int k = 0; k < 8; ++k)
+            if (k < kmax) {
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-              const ff yy{y[q][k].x, y[q][k].y};
-              x[q] = ((MAXMASK >> q) & 1u) ? (yy.hi > x[q].hi ? yy : x[q]) : ff_add(x[q], yy);
+              for (int q = 0; q < NQ; ++q) {
+                const ff yy{y[q][k].x, y[q][k].y};
+                x[q] = ((MAXMASK >> q) & 1u) ? (yy.hi > x[q].hi ? yy : x[q]) : ff_add(x[q], yy);
+              }
             }
         }
-        warp_all_ff<NQ, MAXMASK>(x);
+        warp_reduce_lane0_ff<NQ, MAXMASK>(x, 16);
       }
     }
     if (lane == 0) {
