@@ -1103,12 +1103,20 @@ adp_status adp_outer(adp_handle* h, int mode, int popt, adp_report* rep) {
   P.phantom = h->phantom;
   NodalParams NP = nodal_params(h, adj ? 0 : (h->trans_on ? 2 : 1));
   if (h->trans_on) {
-    // outer_tr (mod_cmfd.f90:800-868): the FP64 kernel with the step's
-    // source weights and external source, no eigenvalue update
+    // outer_tr (mod_cmfd.f90:800-868): the step's source weights and
+    // external source, no eigenvalue update; on the mixed path both as
+    // (hi, lo) pairs for the double-float defect (the kernel of the
+    // generalized adjoint's fixed-eigenvalue mode, here forward)
     P.trans = 1;
-    P.mixed = 0;
     P.wsrc = h->d_wtr;
     P.exsrc = h->d_exsrc;
+    if (P.mixed) {
+      const long long gn = (long long)h->ng * h->NB;
+      CK(launch_split(h->d_wtr, h->d_wtr2, gn, h->st));
+      CK(launch_split(h->d_exsrc, h->d_exsrc2, gn, h->st));
+      P.wsrc2 = h->d_wtr2;
+      P.exsrc2 = h->d_exsrc2;
+    }
   }
   int blocks, threads;
   launch_shape(h, blocks, threads);

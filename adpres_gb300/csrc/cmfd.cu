@@ -101,7 +101,8 @@ static cudaError_t launch_outer_t(const OuterParams& P, int blocks, int threads,
 
 cudaError_t launch_outer(const OuterParams& P, int blocks, int threads, cudaStream_t st) {
   if (P.mixed && P.trans) {
-    // the generalized adjoint in mixed precision (no shared-memory matrix copy)
+    // a transient step or the generalized adjoint in mixed precision: the
+    // external source as (hi, lo) pairs, no shared-memory matrix copy
     void* args[] = {(void*)&P};
     return cudaLaunchCooperativeKernel((const void*)k_outer<true, false, true>, dim3(blocks), dim3(threads), args, 0,
                                        st);

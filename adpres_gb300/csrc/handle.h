@@ -126,6 +126,7 @@ struct adp_handle {
   double *d_c0 = nullptr, *d_omeg = nullptr, *d_ft = nullptr, *d_fst = nullptr, *d_sigrp = nullptr;
   double *d_Lt = nullptr, *d_exsrc = nullptr, *d_wtr = nullptr, *d_wnode = nullptr, *d_af = nullptr;
   double *d_velo = nullptr, *d_tpart = nullptr, *d_s0q = nullptr;
+  float2 *d_wtr2 = nullptr, *d_exsrc2 = nullptr;   // (hi, lo) copies for the mixed path
   // planes of chi, nu*fission and sigs that are nonzero at some node
   // (after_xs); all ones until known
   unsigned chi_nz = ~0u, nuf_nz = ~0u;

@@ -120,9 +120,10 @@ __device__ __forceinline__ double2 mk2(double a, double b) { return make_double2
 // reads them from memory anyway and stores them, the 2 nin Krylov phases
 // that follow read them from there instead of L2 or HBM.
 // XSRC (mixed path only): the group source also carries the external source
-// P.exsrc2 as (hi, lo) pairs -- the fixed-eigenvalue mode of the
-// generalized adjoint of adp_adjoint_sens.  The forward and adjoint
-// solves are the XSRC = false instantiation.
+// P.exsrc2 as (hi, lo) pairs -- the transient step (outer_tr) and the
+// fixed-eigenvalue mode of the generalized adjoint of adp_adjoint_sens.
+// The forward and adjoint eigenvalue solves are the XSRC = false
+// instantiation.
 template <bool MIXED, bool SMEMA = false, bool XSRC = false>
 __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, unsigned nteam) {
   using T = typename KV<MIXED>::T;
@@ -230,8 +231,8 @@ __device__ __forceinline__ void outer_body(const OuterParams& P, unsigned rank, 
       // ---- P0: source and initial residual (TSrc + r = b - A x) --------
       double tot1[1];
       if constexpr (MIXED) {
-        // (the transient runs the FP64 kernel only; XSRC adds the
-        // generalized adjoint's external source)
+        // (XSRC adds the external source: the transient step's, or the
+        // generalized adjoint's)
         // Defect of the current flux in double-float: one compensated dot
         // product over the source and the seven matrix terms (A = A32 + lo).
         const float2* xO2 = P.x2[old] + (size_t)g * NBH;

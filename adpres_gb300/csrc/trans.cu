@@ -283,6 +283,7 @@ adp_status adp_trans_init(adp_handle* h, const adp_trans_opts* o, const double* 
     auto add = [&](size_t b) { bytes += ((b + 255) & ~(size_t)255) + 256; };
     add(8 * NB * 8);              // c0
     for (int q = 0; q < 7; ++q) add(G * NB * 8);   // omeg ft sigrp Lt exsrc wtr af
+    for (int q = 0; q < 2; ++q) add(G * NB * 8);   // wtr2 exsrc2 (double-float copies, mixed path)
     add(NB * 8);                  // fst
     add(NB * 8);                  // wnode
     add(NB * 8);                  // s0q
@@ -296,6 +297,8 @@ adp_status adp_trans_init(adp_handle* h, const adp_trans_opts* o, const double* 
     h->d_c0 = (double*)A.take(8 * NB * 8);
     double** pp[7] = {&h->d_omeg, &h->d_ft, &h->d_sigrp, &h->d_Lt, &h->d_exsrc, &h->d_wtr, &h->d_af};
     for (auto p : pp) *p = (double*)A.take(G * NB * 8);
+    h->d_wtr2 = (float2*)A.take(G * NB * 8);
+    h->d_exsrc2 = (float2*)A.take(G * NB * 8);
     h->d_fst = (double*)A.take(NB * 8);
     h->d_wnode = (double*)A.take(NB * 8);
     h->d_s0q = (double*)A.take(NB * 8);

@@ -296,9 +296,12 @@ def transient_leg(steps=2):
     """rod_eject on the 34x34x22-node core (seed 0): steady state with k
     brought to one, adjoint weight, then 18 time steps (bank 1 ejected in
     0.05 s, theta 0.5); each step XS_updt at the new bank positions on the
-    host, then removal, external source, outer_tr (FP64 kernel), precursors,
-    power and reactivity on the GPU.  Timed end to end (wall clock); the
-    oracle's whole transient on one host core is the CPU baseline."""
+    host, then removal, external source, outer_tr, precursors, power and
+    reactivity on the GPU.  FP64 handle (the FP64 kernel) and mixed handle
+    (the mixed kernel with the step's external source, the nodal update in
+    FP64 either way), each timed end to end (wall clock); the mixed run's
+    relative power and reactivity against the FP64 run's, step by step.
+    The oracle's whole transient on one host core is the CPU baseline."""
     import multiprocessing as mp
 
     import numpy as np
@@ -312,18 +315,24 @@ def transient_leg(steps=2):
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
         t_cpu, ref = pool.apply(_transient_oracle, (text,))
-    walls, parts, rec = [], [], None
-    for i in range(steps + 1):
-        core = Core.from_deck(dk, precision="fp64")
-        t0 = time.perf_counter()
-        rec = rod_eject(core, dk)
-        if i:
-            walls.append(time.perf_counter() - t0)
-            parts.append(core.rod_eject_wall)
-        core.close()
-    t = sum(walls) / len(walls)
+
+    def run(prec):
+        walls, parts, rec = [], [], None
+        for i in range(steps + 1):
+            core = Core.from_deck(dk, precision=prec)
+            t0 = time.perf_counter()
+            rec = rod_eject(core, dk)
+            if i:
+                walls.append(time.perf_counter() - t0)
+                parts.append(core.rod_eject_wall)
+            core.close()
+        return sum(walls) / len(walls), parts, rec
+
+    t, parts, rec = run("fp64")
+    tm, parts_m, rec_m = run("mixed")
     pw = np.array([r[2] for r in ref])
     got = np.array([r[2] for r in rec])
+    got_m = np.array([r[2] for r in rec_m])
     nsteps = len(rec) - 1
     return {"workload": "rod_ejection_3d seed 0: 34x34 radial nodes x 22 planes, 2 groups, SANM, 18 steps "
                         "(0.01 s to 0.1 s, then 0.05 s), theta 0.5",
@@ -332,6 +341,14 @@ def transient_leg(steps=2):
             "steady_state_ms": 1e3 * sum(p[0] for p in parts) / len(parts),
             "steps_wall_ms": 1e3 * sum(p[1] for p in parts) / len(parts),
             "peak_relpow": float(got.max()), "max_relpow_diff_vs_oracle": float(np.max(np.abs(got - pw) / pw)),
+            "mixed": {"ms_per_transient": tm * 1e3, "steps_per_s": nsteps / tm,
+                      "outers": int(sum(r[4] for r in rec_m[1:])), "device_ms": float(sum(r[5] for r in rec_m[1:])),
+                      "steady_state_ms": 1e3 * sum(p[0] for p in parts_m) / len(parts_m),
+                      "steps_wall_ms": 1e3 * sum(p[1] for p in parts_m) / len(parts_m),
+                      "max_relpow_diff_vs_fp64": float(np.max(np.abs(got_m - got) / got)),
+                      "max_rho_diff_vs_fp64": float(np.max(np.abs(np.array([r[1] for r in rec_m])
+                                                                  - np.array([r[1] for r in rec])))),
+                      "steps_at_nout": int(sum(1 for r in rec_m[1:] if r[3]))},
             "cpu_baseline": {"value": nsteps / t_cpu, "unit": "time steps/s", "cores": 1, "kind": "port",
                              "sample": f"the oracle's whole transient on this core ({t_cpu:.1f} s)"}}
 

@@ -437,7 +437,8 @@ adp_status adp_trans_init(adp_handle* h, const adp_trans_opts* opts, const doubl
 /* One time step of trans_calc (mod_trans.f90:332-479) after the host has
  * moved the rods and uploaded the step's cross sections (adp_xs_updt or
  * adp_xs_updt_nodes): removal sigr + 1/(theta v dt) + omega/v, get_exsrc,
- * outer_tr (FP64 kernel, nodal update in its transient form), uPden,
+ * outer_tr (the FP64 kernel, or the mixed kernel on a mixed-precision
+ * handle; nodal update in its transient form, FP64), uPden,
  * PowTot and the reactivity with the step's XS_updt removal.  omeg_mode 1:
  * omega = log(f0/ft)/dt (rod_eject applies it from the second step on when
  * %EXTR is given), 0: omega = 0.  Reaching nout only sets r->maxi. */

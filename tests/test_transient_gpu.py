@@ -1,7 +1,7 @@
 """Rod ejection transient on the GPU (rod_eject, mod_trans.f90:17-160):
 the steady state, KNE1, the adjoint weight, then every time step's
-outer_tr on the FP64 kernel with the nodal update in its transient form,
-against the oracle.
+outer_tr on the FP64 kernel (the mixed kernel for a mixed-precision
+handle) with the nodal update in its transient form, against the oracle.
 
 Bar: the reactivity at t = 0 within 1e-8 (absolute); per step the relative
 power within 1e-6 or 4x the oracle's own rounding sensitivity (the oracle
@@ -62,6 +62,42 @@ def test_synthetic_ejection_matches_oracle(extr):
     core = Core.from_deck(dk, precision="fp64")
     rec = rod_eject(core, dk)
     _compare(rec, [r[0] for r in ref], rho, pw, sens_rho, sens_pow)
+
+
+def test_lmw_mixed_matches_oracle_within_its_rounding_sensitivity():
+    """A mixed-precision handle runs its transient steps on the mixed
+    kernel (FP32 Krylov steps, double-float defect with the step's external
+    source; nodal update in FP64).  On LMW, whose 241 loosely converged
+    steps move the oracle's own power by 3.3e-3 under a change of rounding,
+    it stays within the FP64 path's bars (4x that sensitivity)."""
+    fx = fixture("LMW")
+    dk = deck_from_fixture(fx, mode="RODEJECT")
+    core = Core.from_deck(dk, precision="mixed")
+    rec = rod_eject(core, dk)
+    sens_pow = float(np.max(np.abs(fx["sens_pow"] - fx["out_pow"]) / fx["out_pow"]))
+    sens_rho = float(np.max(np.abs(fx["sens_rho"][1:] - fx["out_rho"][1:])))
+    _compare(rec, fx["out_t"], fx["out_rho"], fx["out_pow"], sens_rho, sens_pow)
+    assert not any(r[3] for r in rec)
+
+
+@pytest.mark.parametrize("extr", [False, True])
+def test_synthetic_ejection_mixed_matches_fp64(extr):
+    """Mixed against FP64 handles on the synthetic ejection: the same
+    outers, power within 1e-6 and reactivity within 1e-8 dollars at every
+    step (measured: 1e-8 and 8e-10)."""
+    dk = deck.parse(synth.rod_ejection_3d(0, n=9, planes=6, extr=extr))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        core = Core.from_deck(dk, precision=prec)
+        out[prec] = rod_eject(core, dk)
+        core.close()
+    a, b = out["fp64"], out["mixed"]
+    assert len(a) == len(b)
+    pa, pb = np.array([r[2] for r in a]), np.array([r[2] for r in b])
+    assert float(np.max(np.abs(pb - pa) / pa)) <= 1e-6
+    assert float(np.max(np.abs(np.array([r[1] for r in b]) - np.array([r[1] for r in a])))) <= 1e-8
+    assert [r[4] for r in a] == [r[4] for r in b]
+    assert not any(r[3] for r in b)
 
 
 def test_step_before_init_is_refused():
