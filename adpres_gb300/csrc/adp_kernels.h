@@ -37,6 +37,7 @@ struct OuterParams {
   double* fs[2];              // [NB] fission source double buffer
   const double* wsrc;         // weight of fs0 in the group source: chi (fwd) / nuf (adj), [ng][NB]
   const double* wfis;         // weight of the flux in the fission source: nuf (fwd) / chi (adj)
+  const double* init_phi;     // k_init_flux: start from this flux ([ng][NBH], halo offset applied), else 1
   const double* sigs;         // [ng(from)][ng(to)][NB]
   double* r;                  // Krylov vectors, halo'd [NBH]
   double* rs;

@@ -1367,9 +1367,14 @@ static adp_status adjoint_frozen(adp_handle* h, double tol, OuterCtl& fwd, Outer
   P.ctl = h->d_ctla;
   P.do_nodal = 0;
   if (tol > 0) P.serc = P.ferc = tol;
+  // Warm start: the converged forward flux and eigenvalue (A^T has the
+  // eigenvalue of A, and the forward flux, positive, overlaps the
+  // fundamental adjoint mode)
+  P.init_phi = h->d_phi[fwd.cur];
   CK(launch_init_flux(P, h->st));
+  P.init_phi = nullptr;
   std::memset(&c, 0, sizeof c);
-  c.Ke = 1.0;
+  c.Ke = fwd.Ke;
   c.need_prologue = 1;
   c.err_node = -1;
   c.wait_ns = h->wait_ns;

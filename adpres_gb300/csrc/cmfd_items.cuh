@@ -5,7 +5,9 @@
 //                     inactive box positions get all-zero rows; row slots in
 //                     reference column order [z-, y-, x-, diag, x+, y+, z+].
 //   init_flux_items : first-call start f0 = 1, fs0 = FSrc(f0)
-//                     (mod_cmfd.f90:448-454, :635-641); one item per row.
+//                     (mod_cmfd.f90:448-454, :635-641), or f0 = a given
+//                     flux (the discrete adjoint's warm start); one item
+//                     per row.
 //   xs_updt_items   : Dsigr_updt (mod_xsec.f90:199-226) with the node checks
 //                     of check_xs (:90-168); one item per (node, group).
 #pragma once
@@ -86,7 +88,7 @@ __device__ __forceinline__ void init_flux_items(const OuterParams& P, int start,
     const bool act = G.nbm[b] & NB_ACTIVE;
     double fs = 0.0;
     for (int g = 0; g < P.ng; ++g) {
-      const double x = act ? 1.0 : 0.0;
+      const double x = act ? (P.init_phi ? P.init_phi[(size_t)g * P.NBH + b] : 1.0) : 0.0;
       P.phi[0][(size_t)g * P.NBH + b] = x;
       P.phi[1][(size_t)g * P.NBH + b] = x;
       fs = fs + x * P.wfis[(size_t)g * G.NB + b];
