@@ -7,7 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = os.environ.get("ADPRES_REFERENCE", "/root/reference")
+# The reference project's tree (its sample decks): ADPRES_REFERENCE, else a
+# checkout named "reference" beside this repository; tests that need it
+# skip where neither exists (the GPU machines have no copy).
+REFERENCE = os.environ.get("ADPRES_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
