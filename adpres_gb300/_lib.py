@@ -154,6 +154,8 @@ SIGNATURES = {
     "adp_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AdpBatchConfig),
                                           ctypes.POINTER(ctypes.c_double)]),
     "adp_batch_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "adp_batch_plan_preview": (ctypes.c_int, [ctypes.c_int, _dp, _dp, _ip, ctypes.c_int, ctypes.POINTER(AdpBatchConfig),
+                                              ctypes.c_int, _ip, _ip, _ip, _ip, _dp]),
     "adp_batch_power": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp]),
     "adp_batch_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp, _ip, _dp]),
     "adp_set_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),

@@ -150,9 +150,6 @@ void drop_graph(adp_batch* b) {
   b->graph_ok = false;
 }
 
-// Team overhead kappa of the duration model t(s) = A (1/s + kappa): least
-// squares over every pair of team sizes some core was timed at (kappa in
-// [0, 0.3] by steps of 0.002); 0.03 when no core has two sizes yet.
 // Key of a time in adp_batch::took: kernel shape and team size.
 int shape_key(const adp_batch_config& c, int s) { return ((c.threads / 256) * 8 + c.blocks_per_sm) * 65536 + s; }
 
@@ -165,6 +162,11 @@ std::map<int, double> times_here(const adp_batch* b, int i) {
   return m;
 }
 
+// Team overhead kappa of the duration model t(s) = A (1/s + kappa): least
+// squares over every pair of team sizes some core was timed at (kappa in
+// [0, 0.3] by steps of 0.002); kDefaultKappa when no core has two sizes.
+constexpr double kDefaultKappa = 0.03;
+
 double fit_kappa(const adp_batch* b) {
   std::vector<double> r, q0, q1;   // t(s1)/t(s0) with 1/s0, 1/s1
   for (int i = 0; i < b->n; ++i) {
@@ -176,8 +178,8 @@ double fit_kappa(const adp_batch* b) {
         q1.push_back(1.0 / c->first);
       }
   }
-  if (r.empty()) return 0.03;
-  double best = 0.03, err_best = 1e300;
+  if (r.empty()) return kDefaultKappa;
+  double best = kDefaultKappa, err_best = 1e300;
   for (int j = 0; j <= 150; ++j) {
     const double k = 0.002 * j;
     double e = 0.0;
@@ -252,21 +254,22 @@ Plan list_schedule(int n, int B, const std::vector<int>& order, SizeRule size,
   return P;
 }
 
-// Longest-first list scheduling with teams (see the file comment).
-void make_plan(adp_batch* b) {
-  const int n = b->n, B = b->blocks;
-  bool meas = true;
-  for (int i = 0; i < n; ++i) meas = meas && b->last_t[i] > 0.0;
-  const int maxteam = std::max(1, std::min(b->cfg.max_team, B));
+// Longest-first list scheduling with teams (see the file comment), on the
+// host alone: n cores on B blocks, teams of at most max_team.  Untimed
+// (dur empty): weights `rows`, team size from the grain.  Timed: dur(i, s)
+// is core i's duration on s blocks.
+Plan plan_schedule(int n, int B, int max_team, double grain_cfg, const std::vector<double>& rows,
+                   const std::function<double(int, int)>& dur_model) {
+  const int maxteam = std::max(1, std::min(max_team, B));
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
   Plan P;
-  if (!meas) {
+  if (!dur_model) {
     // before any solve is timed: weights box rows x groups, team size from
     // the grain
-    const std::vector<double>& w = b->rows;
+    const std::vector<double>& w = rows;
     const double avg = std::accumulate(w.begin(), w.end(), 0.0) / B;
-    const double grain = b->cfg.grain > 0 ? b->cfg.grain : 1.0;
+    const double grain = grain_cfg > 0 ? grain_cfg : 1.0;
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return w[a] > w[c]; });
     struct Grain {
       int cap;
@@ -276,59 +279,70 @@ void make_plan(adp_batch* b) {
         return std::max(1, std::min((int)std::ceil(w[i] * grain / avg - 1e-9), cap));
       }
     } rule{maxteam, w, avg, grain};
-    P = list_schedule(n, B, order, rule, [&](int i, int s) { return w[i] / s; });
-  } else {
-    // timed: for a target end T each core takes the smallest team that
-    // ends by T on the least loaded blocks (else the team that ends
-    // earliest); T runs over [lower bound, 1.3 x lower bound] and the plan
-    // with the earliest predicted end is kept
-    const double kappa = fit_kappa(b);
-    std::vector<double> d1(n);
-    double work = 0.0, longest = 0.0;
-    for (int i = 0; i < n; ++i) {
-      d1[i] = duration(b, i, 1, kappa);
-      double wmin = 1e300;
-      for (int s = 1; s <= maxteam; ++s) wmin = std::min(wmin, s * duration(b, i, s, kappa));
-      work += wmin;
-      longest = std::max(longest, duration(b, i, maxteam, kappa));
-    }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return d1[a] > d1[c]; });
-    // durations per core and team size, computed once
-    std::vector<double> dt((size_t)n * (maxteam + 1));
-    for (int i = 0; i < n; ++i)
-      for (int s = 1; s <= maxteam; ++s) dt[(size_t)i * (maxteam + 1) + s] = duration(b, i, s, kappa);
-    std::function<double(int, int)> dur = [&](int i, int s) { return dt[(size_t)i * (maxteam + 1) + s]; };
-    const double lb = std::max(work / B, longest);
-    struct Fill {
-      int cap;
-      double T;
-      const std::function<double(int, int)>& dur;
-      int operator()(int i, const std::vector<double>& load, const std::vector<int>& idx) const {
-        int best = 1;
-        double fbest = 1e300;
-        for (int s = 1; s <= cap; ++s) {
-          const double f = load[idx[s - 1]] + dur(i, s);
-          if (f <= T) return s;
-          if (f < fbest) {
-            fbest = f;
-            best = s;
-          }
+    return list_schedule(n, B, order, rule, [&](int i, int s) { return w[i] / s; });
+  }
+  // timed: for a target end T each core takes the smallest team that ends
+  // by T on the least loaded blocks (else the team that ends earliest); T
+  // runs over [lower bound, 1.3 x lower bound] and the plan with the
+  // earliest predicted end is kept.  Durations per core and team size are
+  // formed once.
+  std::vector<double> dt((size_t)n * (maxteam + 1));
+  for (int i = 0; i < n; ++i)
+    for (int s = 1; s <= maxteam; ++s) dt[(size_t)i * (maxteam + 1) + s] = dur_model(i, s);
+  std::function<double(int, int)> dur = [&](int i, int s) { return dt[(size_t)i * (maxteam + 1) + s]; };
+  double work = 0.0, longest = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double wmin = 1e300;
+    for (int s = 1; s <= maxteam; ++s) wmin = std::min(wmin, s * dur(i, s));
+    work += wmin;
+    longest = std::max(longest, dur(i, maxteam));
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return dur(a, 1) > dur(c, 1); });
+  const double lb = std::max(work / B, longest);
+  struct Fill {
+    int cap;
+    double T;
+    const std::function<double(int, int)>& dur;
+    int operator()(int i, const std::vector<double>& load, const std::vector<int>& idx) const {
+      int best = 1;
+      double fbest = 1e300;
+      for (int s = 1; s <= cap; ++s) {
+        const double f = load[idx[s - 1]] + dur(i, s);
+        if (f <= T) return s;
+        if (f < fbest) {
+          fbest = f;
+          best = s;
         }
-        return best;
       }
-    };
-    // 61 targets 0.5% apart; fewer (at least 9, over the same range) when
-    // cores x blocks is large, to bound the host time of a plan
-    const int nt = std::max(9, std::min(61, (int)(2.0e7 / ((double)n * B))));
-    bool have = false;
-    for (int j = 0; j < nt; ++j) {
-      Plan Q = list_schedule(n, B, order, Fill{maxteam, lb * (1.0 + 0.3 * j / (nt - 1)), dur}, dur);
-      if (!have || Q.makespan < P.makespan) {
-        P = std::move(Q);
-        have = true;
-      }
+      return best;
+    }
+  };
+  // 61 targets 0.5% apart; fewer (at least 9, over the same range) when
+  // cores x blocks is large, to bound the host time of a plan
+  const int nt = std::max(9, std::min(61, (int)(2.0e7 / ((double)n * B))));
+  bool have = false;
+  for (int j = 0; j < nt; ++j) {
+    Plan Q = list_schedule(n, B, order, Fill{maxteam, lb * (1.0 + 0.3 * j / (nt - 1)), dur}, dur);
+    if (!have || Q.makespan < P.makespan) {
+      P = std::move(Q);
+      have = true;
     }
   }
+  return P;
+}
+
+// The batch's schedule from its cores' times (see the file comment).
+void make_plan(adp_batch* b) {
+  const int n = b->n, B = b->blocks;
+  bool meas = true;
+  for (int i = 0; i < n; ++i) meas = meas && b->last_t[i] > 0.0;
+  std::function<double(int, int)> dur;
+  double kappa = 0.0;
+  if (meas) {
+    kappa = fit_kappa(b);
+    dur = [b, &kappa](int i, int s) { return duration(b, i, s, kappa); };
+  }
+  const Plan P = plan_schedule(n, B, b->cfg.max_team, b->cfg.grain, b->rows, dur);
   b->team = P.team;
   b->tasks.clear();
   b->begin.assign(B + 1, 0);
@@ -648,6 +662,40 @@ adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best_out, double* 
   if (s != ADP_OK) return s;
   if (best_out) *best_out = best;
   if (best_ms) *best_ms = best_t;
+  return ADP_OK;
+}
+
+adp_status adp_batch_plan_preview(int n, const double* rows, const double* t_ns, const int* t_team, int blocks,
+                                  const adp_batch_config* c, int cap, int* team, int* begin, int* task_core,
+                                  int* task_rank, double* makespan) {
+  if (n < 1 || blocks < 1 || !c || !rows || !team || !begin || !task_core || !task_rank || cap < 0 ||
+      (t_ns && !t_team) || c->max_team < 1 || !(c->grain > 0))
+    return bfail(nullptr, ADP_ERR_INPUT, "adp_batch_plan_preview: bad arguments");
+  for (int i = 0; i < n; ++i)
+    if (!(rows[i] > 0) || (t_ns && (!(t_ns[i] > 0) || t_team[i] < 1)))
+      return bfail(nullptr, ADP_ERR_INPUT, "adp_batch_plan_preview: weights and times must be positive");
+  std::vector<double> w(rows, rows + n);
+  std::function<double(int, int)> dur;
+  if (t_ns)
+    dur = [&](int i, int s) {
+      return t_ns[i] * (1.0 / s + kDefaultKappa) / (1.0 / t_team[i] + kDefaultKappa);
+    };
+  const Plan P = plan_schedule(n, blocks, c->max_team, c->grain, w, dur);
+  size_t total = 0;
+  for (const auto& l : P.lists) total += l.size();
+  if (total > (size_t)cap) return bfail(nullptr, ADP_ERR_INPUT, "adp_batch_plan_preview: task capacity too small");
+  size_t k = 0;
+  for (int b = 0; b < blocks; ++b) {
+    begin[b] = (int)k;
+    for (const BatchTask& t : P.lists[b]) {
+      task_core[k] = t.inst;
+      task_rank[k] = t.rank;
+      ++k;
+    }
+  }
+  begin[blocks] = (int)k;
+  for (int i = 0; i < n; ++i) team[i] = P.team[i];
+  if (makespan) *makespan = P.makespan;
   return ADP_OK;
 }
 

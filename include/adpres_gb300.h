@@ -503,6 +503,20 @@ adp_status adp_batch_solve(adp_batch* b, adp_batch_result* res, double* device_m
  * schedule planned with the times of the first), 25 solves of the whole
  * batch.  best_ms is the winner's second solve. */
 adp_status adp_batch_autotune(adp_batch* b, adp_batch_config* best, double* best_ms);
+/* The schedule a batch would run, computed on the host alone (no GPU, no
+ * batch): n cores with weights rows[i] (box rows x groups, the weight
+ * before any solve is timed) and, when t_ns is not NULL, each core's
+ * measured time t_ns[i] on a team of t_team[i] blocks (the timed,
+ * target-end plan, with the duration model t(s) = A (1/s + 0.03)), on
+ * `blocks` blocks with c->max_team and c->grain.  Writes team[n], and for
+ * each block b its tasks begin[b] .. begin[b+1]-1 (begin has blocks + 1
+ * entries) as the core index task_core[k] and the block's rank in that
+ * core's team task_rank[k] (cap entries available), and the predicted end
+ * (makespan, may be NULL).  ADP_ERR_INPUT on bad arguments or too small a
+ * cap (sum of the teams). */
+adp_status adp_batch_plan_preview(int n, const double* rows, const double* t_ns, const int* t_team, int blocks,
+                                  const adp_batch_config* c, int cap, int* team, int* begin, int* task_core,
+                                  int* task_rank, double* makespan);
 adp_status adp_batch_core(adp_batch* b, int i, adp_handle** h);
 /* Per-outer trace of core i from the last adp_batch_solve (as the trace of
  * adp_report; any array may be NULL); returns the number of entries written
