@@ -134,7 +134,9 @@ def test_timed_replans_keep_the_answer_and_the_team_cap(members):
     for a, c in zip(r0, r1):
         assert c["converged"] == 1 and 1 <= c["team"] <= 4 and c["device_ms"] > 0
         assert pcm(a["keff"], c["keff"]) <= 0.01
-        assert a["outers"] == c["outers"]
+        # a new team size groups the sums differently: the stopping outer
+        # may move by one where a criterion sits at its threshold
+        assert abs(a["outers"] - c["outers"]) <= 1
 
 
 def test_many_small_cores_more_cores_than_blocks():
